@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Benchmark of the Neon grid-stencil hot path on GB300.
+
+Default workload: D3Q19 BGK lid-driven cavity, dense grid 384^3, FP32
+populations in SoA planes (the FP32 D3Q19 384^3 case of the cavity
+benchmark, benchmarks/lbm-lid-driven-cavity-flow), lid u = 0.1 along +x,
+Re = 100. A "step" is one pull stream-collide time step over the whole
+lattice; MLUPS = N^3 * steps / time (walls counted, as Metrics.h:39-42).
+
+Prints ONE JSON line. `value` is device-timed with inputs resident in HBM;
+`e2e` is the same metric through the host-buffer C-ABI call
+(ngb_lbm_dense_run_host: H2D of the populations, the steps, D2H of the
+result, all inside the timed region).
+
+`--impl reference` times the CPU restatement of the reference's per-cell
+D3Q19 FP32 arithmetic (the oracle port; the reference cannot be built
+here) on all host threads, on bounded z-slab samples of the same lattice.
+"""
+import argparse
+import ctypes
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "D3Q19 LBM MLUPS"
+UNIT = "MLUPS"
+BYTES_PER_UPDATE = {("d3q19", "f32"): 152, ("d3q19", "f64"): 304, ("d3q19", "f16off"): 76, ("d3q19", "bf16off"): 76,
+                    ("d3q27", "f32"): 216, ("d3q27", "f64"): 432, ("d3q27", "f16off"): 108, ("d3q27", "bf16off"): 108}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=384)
+    ap.add_argument("--lattice", default="d3q19", choices=["d3q19", "d3q27"])
+    ap.add_argument("--storage", default="f32", choices=["f64", "f32", "f16off", "bf16off"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--extra", action="store_true", help="also time the other storage/lattice forms")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """dram bytes per launch recorded by an ncu capture summarised under profiles/."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(p) as f:
+            for line in f:
+                m = re.match(r"\s*traffic_bytes_per_launch:\s*([0-9.eE+]+)", line)
+                if m:
+                    return float(m.group(1))
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(n, seconds=12.0, threads=0):
+    """Oracle port of the reference's D3Q19 FP32 per-cell arithmetic on a z-slab sample of the n^3 lattice."""
+    import numpy as np
+    import oracle
+    import neon_gb300 as ngb
+    L = oracle.lib()
+    threads = threads or L.orc_max_threads()
+    ulb = 0.1
+    omega = ngb.cavity_omega(n, ulb, 100.0)
+    # a slab of the full lattice: all of x and y, a few z planes (+2 walls)
+    nz = max(3, min(n, 2 + int(threads) * 2))
+    V = n * n * nz
+    flags = np.zeros(V, np.uint32)
+    L.orc_cavity_flags(n, n, nz, 19, flags.ctypes.data_as(ctypes.c_void_p))
+    a = np.zeros(19 * V, np.float32)
+    L.orc_cavity_init(n, n, nz, 19, 1, ulb, a.ctypes.data_as(ctypes.c_void_p))
+    b = a.copy()
+    P = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    us = L.orc_time_d3q19_f32(n, n, nz, 1, threads, omega, P(flags), P(a), P(b))
+    steps = max(1, int(seconds * 1e6 / max(us, 1.0)))
+    us = L.orc_time_d3q19_f32(n, n, nz, steps, threads, omega, P(flags), P(a), P(b))
+    mlups = V * steps / us
+    return mlups, threads, "D3Q19 FP32 reference arithmetic, %dx%dx%d slab of the %d^3 lattice, %d steps (%.1f s)" % (
+        n, n, nz, n, steps, us / 1e6)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    L = oracle.lib()
+    threads = L.orc_max_threads()
+    # each step: one timed slab sample (~1 s) of the same workload
+    samples = []
+    for i in range(args.warmup + args.steps):
+        mlups, thr, desc = cpu_sample(args.n, seconds=0.5 if i < args.warmup else 1.0, threads=threads)
+        if i >= args.warmup:
+            samples.append(mlups)
+        if len(samples) >= min(args.steps, 20):
+            break
+    value = sum(samples) / len(samples)
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": args.gpus, "steps": len(samples),
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (lid-driven cavity set-up)",
+            "impl": "reference",
+            "config": {"workload": "D3Q19 BGK lid-driven cavity, dense %d^3, FP32 SoA" % args.n,
+                       "lattice": "d3q19", "storage": "f32", "n": args.n},
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": desc + "; reference not buildable here (needs spdlog/rapidjson/cmake)"},
+            "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import neon_gb300 as ngb
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    ngb.lib()
+    n, lat, st = args.n, args.lattice, args.storage
+    q = 19 if lat == "d3q19" else 27
+    ulb, re_ = 0.1, 100.0
+    omega = ngb.cavity_omega(n, ulb, re_)
+    desc = ngb.lbm_dense_desc(n, n, n, q, st, omega, ngb.lid_wall_terms(q, ulb), box_cavity=True)
+    tdt = {"f64": torch.float64, "f32": torch.float32, "f16off": torch.float16, "bf16off": torch.bfloat16}[st]
+    V = n ** 3
+    fa = torch.empty(q * V, dtype=tdt, device=dev)
+    fb = torch.empty_like(fa)
+    stream = torch.cuda.current_stream(dev)
+    ngb.lbm_cavity_init(desc, ulb, fa, fb, None, stream=stream)
+    ngb.lbm_dense_run(desc, fa, fb, args.warmup + (args.warmup % 2), stream=stream)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- device-resident timing (CUDA events on the launching stream)
+    sampler = ClockSampler(local)
+    barrier()
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ngb.lbm_dense_run(desc, fa, fb, args.steps, stream=stream)
+    e1.record(stream)
+    e1.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    per_step_ms = ms / args.steps
+    value = world * V * args.steps / (ms * 1e3)  # MLUPS, all ranks
+    bpu = BYTES_PER_UPDATE[(lat, st)]
+    peak, peak_kind = measured_peaks()
+    achieved = bpu * V / (per_step_ms * 1e-3) / 1e9
+    traffic = profiled_traffic("lbm_%s_%s_dense_%d.md" % (lat, st, n))
+
+    # ---------------- end to end through the host-buffer C-ABI call
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty(q * V, dtype=tdt, pin_memory=True)
+        host_out = torch.empty_like(host_in)
+        host_in.copy_(fa.cpu())
+        ngb.lbm_dense_run_host(desc, host_in, host_out, fa, fb, 2, stream=stream)  # warm the path
+        barrier()
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        h0.record(stream)
+        ngb.lbm_dense_run_host(desc, host_in, host_out, fa, fb, args.steps, stream=stream)
+        h1.record(stream)
+        h1.synchronize()
+        barrier()
+        ems = h0.elapsed_time(h1)
+        if world > 1:
+            t = torch.tensor([ems], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ems = float(t.item())
+        nbytes = q * V * host_in.element_size()
+        e2e = {"value": round(world * V * args.steps / (ems * 1e3), 2), "unit": UNIT,
+               "h2d_bytes_per_step": nbytes // args.steps, "d2h_bytes_per_step": nbytes // args.steps,
+               "note": "one H2D of the populations, %d steps, one D2H of the result per timed call" % args.steps}
+
+    extra = {}
+    if args.extra and rank == 0:
+        for (l2, s2) in [("d3q19", "f16off"), ("d3q19", "bf16off"), ("d3q27", "f32"), ("d3q27", "f16off"),
+                         ("d3q19", "f64")]:
+            extra["%s_%s" % (l2, s2)] = time_variant(ngb, torch, dev, n if s2 != "f64" else 256, l2, s2, args)
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            mlups, thr, sample = cpu_sample(n)
+            cpu = {"value": round(mlups, 2), "unit": UNIT, "cores": thr, "kind": "port", "sample": sample}
+        line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(per_step_ms, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if st != "f64" else "f64",
+                "data": "synthetic (lid-driven cavity set-up, equilibrium start)",
+                "config": {"workload": "%s BGK lid-driven cavity, dense %d^3, %s SoA populations" % (lat.upper(), n, st),
+                           "lattice": lat, "storage": st, "n": n, "lid_u": ulb, "Re": re_,
+                           "l2": "inputs larger than L2 (2 x %.1f GB population buffers)" % (q * V * fa.element_size() / 1e9),
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "traffic": traffic,
+                             "peak_kind": peak_kind, "bytes_per_update": bpu,
+                             "frac_of_nominal_8TBs": round(achieved / 8000.0, 4)},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks}
+        if extra:
+            line["variants"] = extra
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def time_variant(ngb, torch, dev, n, lat, st, args):
+    q = 19 if lat == "d3q19" else 27
+    ulb = 0.1
+    desc = ngb.lbm_dense_desc(n, n, n, q, st, ngb.cavity_omega(n, ulb, 100.0), ngb.lid_wall_terms(q, ulb))
+    tdt = {"f64": torch.float64, "f32": torch.float32, "f16off": torch.float16, "bf16off": torch.bfloat16}[st]
+    V = n ** 3
+    fa = torch.empty(q * V, dtype=tdt, device=dev)
+    fb = torch.empty_like(fa)
+    s = torch.cuda.current_stream(dev)
+    ngb.lbm_cavity_init(desc, ulb, fa, fb, None, stream=s)
+    ngb.lbm_dense_run(desc, fa, fb, 10, stream=s)
+    steps = max(10, args.steps // 2 * 2)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    ngb.lbm_dense_run(desc, fa, fb, steps, stream=s)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    bpu = BYTES_PER_UPDATE[(lat, st)]
+    del fa, fb
+    torch.cuda.empty_cache()
+    return {"n": n, "mlups": round(V / (ms * 1e3), 1), "ms_per_step": round(ms, 4),
+            "achieved_gbs": round(bpu * V / (ms * 1e-3) / 1e9, 1), "bytes_per_update": bpu}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

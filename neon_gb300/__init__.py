@@ -1,0 +1,167 @@
+"""neon_gb300 — GB300-native (sm_103a) implementation of Neon's grid-stencil hot path.
+
+The product is the C-ABI shared library ``_build/libneon_gb300.so`` built from
+``csrc/`` (declared in ``include/neon_gb300.h``). This module only loads it with
+ctypes and offers thin Python helpers over it; every compute call goes to the
+CUDA library and fails loudly when the library is missing. There is no CPU
+fallback.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_PATH
+
+NGB_OK = 0
+STORE_F64, STORE_F32, STORE_F16OFF, STORE_BF16OFF = 0, 1, 2, 3
+STORAGE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "f16off": STORE_F16OFF, "bf16off": STORE_BF16OFF}
+STORAGE_BYTES = {STORE_F64: 8, STORE_F32: 4, STORE_F16OFF: 2, STORE_BF16OFF: 2}
+CELL_BOUNCEBACK, CELL_MOVINGWALL, CELL_BULK, CELL_UNDEFINED, CELL_OUTLET = 0, 1, 2, 3, 4
+
+_lib = None
+
+
+class NeonError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+
+class LbmDenseDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("q", ctypes.c_int32), ("storage", ctypes.c_int32), ("box_cavity", ctypes.c_int32),
+                ("plane_stride", ctypes.c_int64), ("omega", ctypes.c_double),
+                ("wall_term", (ctypes.c_double * 27) * 2)]
+
+
+def build(force=False):
+    """Compile the CUDA library in-tree (see build.py)."""
+    return _build.build(force=force)
+
+
+def lib():
+    """The loaded C-ABI library. Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NeonError("neon_gb300 CUDA library not built (%s); run neon_gb300.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _declare(L):
+    vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    dp = ctypes.POINTER(LbmDenseDesc)
+    L.ngb_last_error.restype = ctypes.c_char_p
+    L.ngb_version.restype = ctypes.c_int
+    L.ngb_lbm_dense_step.argtypes = [dp, vp, vp, vp, vp]
+    L.ngb_lbm_dense_run.argtypes = [dp, vp, vp, vp, i32, vp]
+    L.ngb_lbm_dense_run_host.argtypes = [dp, vp, vp, vp, vp, vp, i32, vp]
+    L.ngb_lbm_wall_mask.argtypes = [i32, i32, i32, i32, vp, vp]
+    L.ngb_lbm_cavity_init.argtypes = [dp, dbl, vp, vp, vp, vp]
+    L.ngb_lbm_dense_macroscopic.argtypes = [dp, vp, vp, vp, vp, vp]
+    for name, args in _EXTRA_SIGNATURES.items():
+        fn = getattr(L, name, None)
+        if fn is not None:
+            fn.argtypes = args[0]
+            fn.restype = args[1]
+
+
+# Signatures registered by the sub-modules (bgrid, poisson, ...).
+_EXTRA_SIGNATURES = {}
+
+
+def check(rc):
+    if rc != NGB_OK:
+        raise NeonError("neon_gb300 error %d: %s" % (rc, lib().ngb_last_error().decode()))
+    return rc
+
+
+# ----------------------------------------------------------------------------- lattices
+W19 = [1 / 18] * 3 + [1 / 36] * 6 + [1 / 3] + [1 / 18] * 3 + [1 / 36] * 6
+C19 = [(-1, 0, 0), (0, -1, 0), (0, 0, -1), (-1, -1, 0), (-1, 1, 0), (-1, 0, -1), (-1, 0, 1), (0, -1, -1), (0, -1, 1),
+       (0, 0, 0),
+       (1, 0, 0), (0, 1, 0), (0, 0, 1), (1, 1, 0), (1, -1, 0), (1, 0, 1), (1, 0, -1), (0, 1, 1), (0, 1, -1)]
+
+
+def _d27(d):
+    return 0 if d == 0 else (-1 if d == 1 else 1)
+
+
+C27 = [(_d27(q // 9), _d27((q // 3) % 3), _d27(q % 3)) for q in range(27)]
+W27 = [{0: 8 / 27, 1: 2 / 27, 2: 1 / 54, 3: 1 / 216}[sum(c != 0 for c in v)] for v in C27]
+
+
+def lattice(q):
+    return (C19, W19) if q == 19 else (C27, W27)
+
+
+def cavity_omega(n, ulb, re):
+    """omega = 1 / (3 nu + 0.5) with nu = ulb (N - 2) / Re (Config.cpp:105-111)."""
+    nu = ulb * (n - 2) / re
+    return 1.0 / (3.0 * nu + 0.5)
+
+
+def lid_wall_terms(q, ulb, ulid=(1.0, 0.0, 0.0)):
+    """Populations held by moving-wall nodes: -6 w_k ulb (c_k . ulid) (RunCavityTwoPop.cu:177-185)."""
+    c, w = lattice(q)
+    return [-6.0 * w[k] * ulb * (c[k][0] * ulid[0] + c[k][1] * ulid[1] + c[k][2] * ulid[2]) for k in range(q)]
+
+
+def lbm_dense_desc(nx, ny, nz, q, storage, omega, moving_wall_terms=None, box_cavity=True, plane_stride=0,
+                   bounce_back_terms=None):
+    d = LbmDenseDesc()
+    d.nx, d.ny, d.nz, d.q = nx, ny, nz, q
+    d.storage = STORAGE_NAMES[storage] if isinstance(storage, str) else storage
+    d.box_cavity = 1 if box_cavity else 0
+    d.plane_stride = plane_stride
+    d.omega = omega
+    for k in range(27):
+        d.wall_term[0][k] = bounce_back_terms[k] if bounce_back_terms and k < len(bounce_back_terms) else 0.0
+        d.wall_term[1][k] = moving_wall_terms[k] if moving_wall_terms and k < len(moving_wall_terms) else 0.0
+    return d
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return ctypes.c_void_p(t.data_ptr())
+    return ctypes.c_void_p(int(t))
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+def lbm_dense_step(desc, fin, fout, flags=None, stream=None):
+    return check(lib().ngb_lbm_dense_step(ctypes.byref(desc), _ptr(fin), _ptr(fout), _ptr(flags), _stream(stream)))
+
+
+def lbm_dense_run(desc, fa, fb, nsteps, flags=None, stream=None):
+    return check(lib().ngb_lbm_dense_run(ctypes.byref(desc), _ptr(fa), _ptr(fb), _ptr(flags), int(nsteps),
+                                         _stream(stream)))
+
+
+def lbm_dense_run_host(desc, host_in, host_out, fa, fb, nsteps, flags=None, stream=None):
+    return check(lib().ngb_lbm_dense_run_host(ctypes.byref(desc), _ptr(host_in), _ptr(host_out), _ptr(fa), _ptr(fb),
+                                              _ptr(flags), int(nsteps), _stream(stream)))
+
+
+def lbm_wall_mask(nx, ny, nz, q, flags, stream=None):
+    return check(lib().ngb_lbm_wall_mask(nx, ny, nz, q, _ptr(flags), _stream(stream)))
+
+
+def lbm_cavity_init(desc, ulb, fa, fb=None, flags=None, stream=None):
+    return check(lib().ngb_lbm_cavity_init(ctypes.byref(desc), float(ulb), _ptr(fa), _ptr(fb), _ptr(flags),
+                                           _stream(stream)))
+
+
+def lbm_dense_macroscopic(desc, fin, rho=None, u=None, flags=None, stream=None):
+    return check(lib().ngb_lbm_dense_macroscopic(ctypes.byref(desc), _ptr(fin), _ptr(flags), _ptr(rho), _ptr(u),
+                                                 _stream(stream)))

@@ -1,0 +1,143 @@
+// Shared device/host helpers of the neon_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdarg>
+
+#include "../../include/neon_gb300.h"
+
+namespace ngb {
+
+// ------------------------------------------------------------------ errors
+// Every C-ABI entry point returns an ngb status and never throws; the last
+// error message is kept per host thread (ngb_last_error()).
+void set_error(const char* fmt, ...);
+void clear_error();
+
+#define NGB_CHECK_ARG(cond, ...)                 \
+    do {                                         \
+        if (!(cond)) {                           \
+            ::ngb::set_error(__VA_ARGS__);       \
+            return NGB_ERR_INVALID;              \
+        }                                        \
+    } while (0)
+
+#define NGB_CUDA_TRY(expr)                                                                                \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            ::ngb::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return NGB_ERR_CUDA;                                                                          \
+        }                                                                                                 \
+    } while (0)
+
+// Launch-error check after a <<<>>> launch.
+#define NGB_LAUNCH_CHECK(name)                                                                   \
+    do {                                                                                         \
+        cudaError_t e_ = cudaGetLastError();                                                     \
+        if (e_ != cudaSuccess) {                                                                 \
+            ::ngb::set_error("launch of %s failed: %s", name, cudaGetErrorString(e_));           \
+            return NGB_ERR_CUDA;                                                                 \
+        }                                                                                        \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ------------------------------------------------------------------ lattices
+// D3Q19 in Neon's order (benchmarks/lbm-lid-driven-cavity-flow/src/D3Q19.h:23-44):
+// 0..8 go directions, 9 rest, 10..18 the opposites of 0..8.
+template <int Q>
+struct Lattice;
+
+template <>
+struct Lattice<19> {
+    static constexpr int Q = 19;
+    __host__ __device__ static constexpr int cx(int q)
+    {
+        constexpr int v[19] = {-1, 0, 0, -1, -1, -1, -1, 0, 0, 0, 1, 0, 0, 1, 1, 1, 1, 0, 0};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int cy(int q)
+    {
+        constexpr int v[19] = {0, -1, 0, -1, 1, 0, 0, -1, -1, 0, 0, 1, 0, 1, -1, 0, 0, 1, 1};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int cz(int q)
+    {
+        constexpr int v[19] = {0, 0, -1, 0, 0, -1, 1, -1, 1, 0, 0, 0, 1, 0, 0, 1, -1, 1, -1};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int opp(int q) { return q == 9 ? 9 : (q < 9 ? q + 10 : q - 10); }
+    __host__ __device__ static constexpr double w(int q)
+    {
+        return q == 9 ? 1. / 3. : ((q % 10) < 3 ? 1. / 18. : 1. / 36.);
+    }
+};
+
+// D3Q27 in the order of apps/lbmMultiRes/lattice.h:14-42: q = 9a + 3b + c with
+// digit 0 -> 0, 1 -> -1, 2 -> +1 for (cx, cy, cz); the rest population is q = 0.
+template <>
+struct Lattice<27> {
+    static constexpr int Q = 27;
+    __host__ __device__ static constexpr int dig(int d) { return d == 0 ? 0 : (d == 1 ? -1 : 1); }
+    __host__ __device__ static constexpr int cx(int q) { return dig(q / 9); }
+    __host__ __device__ static constexpr int cy(int q) { return dig((q / 3) % 3); }
+    __host__ __device__ static constexpr int cz(int q) { return dig(q % 3); }
+    __host__ __device__ static constexpr int flip(int d) { return d == 0 ? 0 : 3 - d; }
+    __host__ __device__ static constexpr int opp(int q) { return 9 * flip(q / 9) + 3 * flip((q / 3) % 3) + flip(q % 3); }
+    __host__ __device__ static constexpr double w(int q)
+    {
+        return ((cx(q) != 0) + (cy(q) != 0) + (cz(q) != 0)) == 0   ? 8. / 27.
+               : ((cx(q) != 0) + (cy(q) != 0) + (cz(q) != 0)) == 1 ? 2. / 27.
+               : ((cx(q) != 0) + (cy(q) != 0) + (cz(q) != 0)) == 2 ? 1. / 54.
+                                                                    : 1. / 216.;
+    }
+};
+
+// ------------------------------------------------------------------ flags
+// Packed cell flag: bits 0..26 wall-neighbour mask (bit q set iff the pull
+// source x - c_q is not a fluid node), bits 28..31 classification.
+__host__ __device__ inline uint32_t flag_mask(uint32_t f) { return f & 0x07ffffffu; }
+__host__ __device__ inline int      flag_class(uint32_t f) { return int(f >> 28); }
+__host__ __device__ inline uint32_t make_flag(uint32_t mask, int cls) { return (mask & 0x07ffffffu) | (uint32_t(cls) << 28); }
+
+// A node other cells stream from normally (no bounce-back across it).
+__host__ __device__ inline bool is_fluid_class(int c) { return c == NGB_CELL_BULK || c == NGB_CELL_OUTLET; }
+
+// ------------------------------------------------------------------ storage
+// Storage policies: how a population value is held in HBM and turned into the
+// compute type. The "off" forms hold g = f - w_q in 16 bits.
+struct StoreF64 {
+    using T = double;
+    static constexpr int id = NGB_STORE_F64;
+};
+struct StoreF32 {
+    using T = float;
+    static constexpr int id = NGB_STORE_F32;
+};
+struct StoreF16Off {
+    using T = __half;
+    static constexpr int id = NGB_STORE_F16OFF;
+};
+struct StoreBF16Off {
+    using T = __nv_bfloat16;
+    static constexpr int id = NGB_STORE_BF16OFF;
+};
+
+// g = f - w (compute type float) from the stored value.
+__device__ __forceinline__ float load_g(const float* p, float w) { return __ldg(p) - w; }
+__device__ __forceinline__ float load_g(const __half* p, float) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ float load_g(const __nv_bfloat16* p, float) { return __bfloat162float(__ldg(p)); }
+__device__ __forceinline__ void  store_g(float* p, float g, float w) { *p = w + g; }
+__device__ __forceinline__ void  store_g(__half* p, float g, float) { *p = __float2half_rn(g); }
+__device__ __forceinline__ void  store_g(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
+
+inline size_t storage_bytes(int storage)
+{
+    return storage == NGB_STORE_F64 ? 8 : (storage == NGB_STORE_F32 ? 4 : 2);
+}
+
+}  // namespace ngb

@@ -1,0 +1,254 @@
+// Dense single-partition LBM pull stream-collide kernels (D3Q19 / D3Q27).
+//
+// Layout: population (x, y, z, q) at x + nx*(y + ny*z) + q*stride (SoA planes).
+// One thread per cell, x fastest: every population plane is read with one
+// coalesced (at most +-1-element shifted) row access per warp and written
+// with one aligned row access, so each population element crosses HBM once
+// per step: 2 * Q * sizeof(storage) bytes per lattice update.
+#pragma once
+#include "common.cuh"
+
+namespace ngb {
+
+constexpr int kLbmBlockX = 128;
+
+template <typename C>
+struct DenseParams {
+    int32_t nx, ny, nz;
+    int32_t box;      // 1: analytic cavity classification
+    int64_t stride;   // elements between planes
+    C       omega;
+    C       wall[2][27];  // wall term by wall class (bounce-back, moving wall), compute type
+};
+
+// Classification and wall mask of cell (x,y,z) for the analytic lid-driven
+// cavity (RunCavityTwoPop.cu:208-224 + LbmTools.h:327-376): faces are walls,
+// y = ny-1 is the moving lid; for interior cells bit q is set iff x - c_q is
+// on a face. `lidbits` gets bit q set iff that face node is on the lid.
+template <int Q>
+__device__ __forceinline__ int box_classify(int x, int y, int z, int nx, int ny, int nz, uint32_t& mask, uint32_t& lidbits)
+{
+    mask = 0;
+    lidbits = 0;
+    if (y == ny - 1) return NGB_CELL_MOVINGWALL;
+    if (x == 0 || x == nx - 1 || y == 0 || z == 0 || z == nz - 1) return NGB_CELL_BOUNCEBACK;
+    const bool xl = x == 1, xh = x == nx - 2, yl = y == 1, yh = y == ny - 2, zl = z == 1, zh = z == nz - 2;
+    if (!(xl | xh | yl | yh | zl | zh)) return NGB_CELL_BULK;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int  cx = Lattice<Q>::cx(q), cy = Lattice<Q>::cy(q), cz = Lattice<Q>::cz(q);
+        const bool w = (cx > 0 && xl) || (cx < 0 && xh) || (cy > 0 && yl) || (cy < 0 && yh) || (cz > 0 && zl) || (cz < 0 && zh);
+        if (w) mask |= 1u << q;
+        if (cy < 0 && yh) lidbits |= 1u << q;
+    }
+    return NGB_CELL_BULK;
+}
+
+// Wall class of the pull source of direction q of a bulk cell in flags mode.
+__device__ __forceinline__ int source_class(const uint32_t* __restrict__ flags, int64_t src)
+{
+    return flag_class(__ldg(flags + src));
+}
+
+// Common cell prologue: returns the class; for bulk cells fills mask and
+// per-direction wall class bits (bit q set -> the source is a moving wall).
+template <int Q, typename C>
+__device__ __forceinline__ int cell_setup(const DenseParams<C>& p, const uint32_t* __restrict__ flags, int x, int y, int z,
+                                          int64_t cell, uint32_t& mask, uint32_t& lidbits)
+{
+    if (p.box) return box_classify<Q>(x, y, z, p.nx, p.ny, p.nz, mask, lidbits);
+    const uint32_t f = __ldg(flags + cell);
+    const int      cls = flag_class(f);
+    mask = flag_mask(f);
+    lidbits = 0;
+    if (cls == NGB_CELL_BULK) {
+        // A bulk cell on the domain face has sources outside the domain: it is
+        // not updated (keeps every access inside the arrays).
+        if (x == 0 || y == 0 || z == 0 || x == p.nx - 1 || y == p.ny - 1 || z == p.nz - 1) return NGB_CELL_UNDEFINED;
+        if (mask) {
+            const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny;
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                if (mask & (1u << q)) {
+                    const int64_t src = cell - Lattice<Q>::cx(q) - Lattice<Q>::cy(q) * sy - Lattice<Q>::cz(q) * sz;
+                    if (source_class(flags, src) == NGB_CELL_MOVINGWALL) lidbits |= 1u << q;
+                }
+            }
+        }
+    }
+    return cls;
+}
+
+// Outlet node: zero-gradient outflow, copies the x-1 neighbour's populations.
+template <int Q, typename S>
+__device__ __forceinline__ void outlet_copy(const S* __restrict__ fin, S* __restrict__ fout, int64_t stride, int64_t cell, int x)
+{
+    if (x == 0) return;
+#pragma unroll
+    for (int q = 0; q < Q; q++) fout[q * stride + cell] = fin[q * stride + cell - 1];
+}
+
+// ------------------------------------------------------------------ FP32 compute (shifted)
+// Works on g_q = f_q - w_q: rho = 1 + sum g, j = sum c g (sum c w = 0),
+// eq_q - w_q = w_q (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 |u|^2)),
+// g' = g + omega ((eq - w) - g). Same BGK as LbmTools.h:198-282, evaluated
+// on O(Ma) deviations so FP32 keeps ~7 significant digits of the physics.
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f32_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                   const uint32_t* __restrict__ flags, DenseParams<float> p)
+{
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    const int64_t cell = x + sy * y + sz * z;
+    uint32_t      mask, lidbits;
+    const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
+    if (cls == NGB_CELL_OUTLET) {
+        outlet_copy<Q>(fin, fout, stride, cell, x);
+        return;
+    }
+    if (cls != NGB_CELL_BULK) return;
+
+    float g[Q];
+    if (mask == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            g[q] = load_g(fin + q * stride + src, float(L::w(q)));
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (mask & (1u << q)) {
+                // half-way bounce-back: f_q = f_{opp q}(x) + wall term of the source node
+                const int   o = L::opp(q);
+                const float wt = (lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o];
+                g[q] = load_g(fin + o * stride + cell, float(L::w(o))) + wt;
+            } else {
+                const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+                g[q] = load_g(fin + q * stride + src, float(L::w(q)));
+            }
+        }
+    }
+
+    float drho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        drho += g[q];
+        if (L::cx(q) > 0) jx += g[q];
+        if (L::cx(q) < 0) jx -= g[q];
+        if (L::cy(q) > 0) jy += g[q];
+        if (L::cy(q) < 0) jy -= g[q];
+        if (L::cz(q) > 0) jz += g[q];
+        if (L::cz(q) < 0) jz -= g[q];
+    }
+    const float rho = 1.f + drho;
+    const float inv = 1.f / rho;
+    const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+    const float usqr = 1.5f * (ux * ux + uy * uy + uz * uz);
+    const float om = p.omega;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const float cu = float(L::cx(q)) * ux + float(L::cy(q)) * uy + float(L::cz(q)) * uz;
+        const float w = float(L::w(q));
+        const float eqg = w * (drho + rho * (3.f * cu + 4.5f * cu * cu - usqr));
+        const float go = g[q] + om * (eqg - g[q]);
+        store_g(fout + q * stride + cell, go, w);
+    }
+}
+
+// ------------------------------------------------------------------ FP64 compute (reference arithmetic)
+// D3Q19: the expression shapes of LbmTools.h:78-282 in double (compile with
+// --fmad=false for IEEE operation order). D3Q27: the project's per-direction
+// BGK (rho = sum f, u = sum c f / rho, eq = rho w (1 + 3cu + 4.5cu^2 - usqr)).
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                   const uint32_t* __restrict__ flags, DenseParams<double> p)
+{
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    const int64_t cell = x + sy * y + sz * z;
+    uint32_t      mask, lidbits;
+    const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
+    if (cls == NGB_CELL_OUTLET) {
+        outlet_copy<Q>(fin, fout, stride, cell, x);
+        return;
+    }
+    if (cls != NGB_CELL_BULK) return;
+
+    S pop[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (mask & (1u << q)) {
+            const int o = L::opp(q);
+            const S   wt = S((lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o]);
+            pop[q] = __ldg(fin + o * stride + cell) + wt;
+        } else {
+            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            pop[q] = __ldg(fin + q * stride + src);
+        }
+    }
+    using Cd = double;
+    const Cd omega = p.omega;
+    if constexpr (Q == 19) {
+#define P(I) static_cast<Cd>(pop[I])
+        const Cd X_M1 = P(0) + P(3) + P(4) + P(5) + P(6);
+        const Cd X_P1 = P(10) + P(13) + P(14) + P(15) + P(16);
+        const Cd X_0 = P(9) + P(1) + P(2) + P(7) + P(8) + P(11) + P(12) + P(17) + P(18);
+        const Cd Y_M1 = P(1) + P(3) + P(7) + P(8) + P(14);
+        const Cd Y_P1 = P(4) + P(11) + P(13) + P(17) + P(18);
+        const Cd Z_M1 = P(2) + P(5) + P(7) + P(16) + P(18);
+        const Cd Z_P1 = P(6) + P(8) + P(12) + P(15) + P(17);
+        const Cd rho = X_M1 + X_P1 + X_0;
+        const Cd u0 = (X_P1 - X_M1) / rho;
+        const Cd u1 = (Y_P1 - Y_M1) / rho;
+        const Cd u2 = (Z_P1 - Z_M1) / rho;
+        const Cd usqr = 1.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+        const Cd cu[9] = {u0, u1, u2, u0 + u1, u0 - u1, u0 + u2, u0 - u2, u1 + u2, u1 - u2};
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const Cd wk = k < 3 ? (1. / 18.) : (1. / 36.);
+            const Cd eq = rho * wk * (1. - 3. * cu[k] + 4.5 * cu[k] * cu[k] - usqr);
+            const Cd eqopp = eq + rho * wk * 6. * cu[k];
+            const Cd out = (1. - omega) * P(k) + omega * eq;
+            const Cd outopp = (1. - omega) * P(k + 10) + omega * eqopp;
+            fout[k * stride + cell] = static_cast<S>(out);
+            fout[(k + 10) * stride + cell] = static_cast<S>(outopp);
+        }
+        const Cd eq9 = rho * (1. / 3.) * (1. - usqr);
+        fout[9 * stride + cell] = static_cast<S>((1. - omega) * P(9) + omega * eq9);
+#undef P
+    } else {
+        Cd f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) f[q] = Cd(pop[q]);
+        Cd rho = 0, mx = 0, my = 0, mz = 0;
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            rho += f[q];
+            mx += Cd(L::cx(q)) * f[q];
+            my += Cd(L::cy(q)) * f[q];
+            mz += Cd(L::cz(q)) * f[q];
+        }
+        const Cd ux = mx / rho, uy = my / rho, uz = mz / rho;
+        const Cd usqr = Cd(1.5) * (ux * ux + uy * uy + uz * uz);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const Cd cu = Cd(L::cx(q)) * ux + Cd(L::cy(q)) * uy + Cd(L::cz(q)) * uz;
+            const Cd eq = rho * Cd(L::w(q)) * (Cd(1) + Cd(3) * cu + Cd(4.5) * cu * cu - usqr);
+            fout[q * stride + cell] = static_cast<S>((Cd(1) - omega) * f[q] + omega * eq);
+        }
+    }
+}
+
+// Host-side launchers (lbm_dense.cu / lbm_dense_f64.cu).
+int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
+                         cudaStream_t s);
+int launch_lbm_dense_f64(int Q, const void* fin, void* fout, const uint32_t* flags, const DenseParams<double>& p, cudaStream_t s);
+
+}  // namespace ngb

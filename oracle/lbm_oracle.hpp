@@ -1,0 +1,375 @@
+// ORACLE — test infrastructure only.
+//
+// CPU restatement of the Neon lid-driven-cavity LBM path, used by the tests,
+// by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker.
+// Nothing in the product library links or calls this code.
+//
+// Follows (paths relative to the Neon repository):
+//   benchmarks/lbm-lid-driven-cavity-flow/src/D3Q19.h:23-132      velocity set, opposites, weights
+//   benchmarks/lbm-lid-driven-cavity-flow/src/CellType.h:3-35     cell classification
+//   benchmarks/lbm-lid-driven-cavity-flow/src/LbmTools.h:78-168   pull stream with half-way bounce-back
+//   benchmarks/lbm-lid-driven-cavity-flow/src/LbmTools.h:171-195  macroscopic moments
+//   benchmarks/lbm-lid-driven-cavity-flow/src/LbmTools.h:198-282  unrolled BGK collision
+//   benchmarks/lbm-lid-driven-cavity-flow/src/LbmTools.h:284-325  the iteration container (bulk cells only)
+//   benchmarks/lbm-lid-driven-cavity-flow/src/LbmTools.h:327-376  wall-neighbour mask
+//   benchmarks/lbm-lid-driven-cavity-flow/src/RunCavityTwoPop.cu:159-242  problem set-up
+//   benchmarks/lbm-lid-driven-cavity-flow/src/Config.cpp:105-111  nu / omega
+//   apps/lbmMultiRes/lattice.h:14-77                               D3Q27 velocity set and weights
+//
+// The arithmetic of the D3Q19 step keeps the reference's expression shapes
+// (including its double-precision literals), so that instantiating with
+// <double,double> or <float,float> reproduces the reference's own rounding
+// on a CPU with FP contraction disabled (-ffp-contract=off).
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cmath>
+#include <array>
+#include <vector>
+
+namespace oracle {
+
+// ---------------------------------------------------------------- lattices
+// D3Q19 in Neon's order: 0..8 "go" directions, 9 the rest population,
+// 10..18 the opposites of 0..8 (D3Q19.h:23-44, 62-82).
+static const int kC19[19][3] = {
+    {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1}, {-1, 0, 1}, {0, -1, -1}, {0, -1, 1},
+    {0, 0, 0},
+    {1, 0, 0},  {0, 1, 0},  {0, 0, 1},  {1, 1, 0},   {1, -1, 0}, {1, 0, 1},   {1, 0, -1}, {0, 1, 1},   {0, 1, -1}};
+static const double kW19[19] = {
+    1. / 18., 1. / 18., 1. / 18., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36.,
+    1. / 3.,
+    1. / 18., 1. / 18., 1. / 18., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36., 1. / 36.};
+inline int opp19(int q) { return q == 9 ? 9 : (q < 9 ? q + 10 : q - 10); }
+
+// D3Q27 in the order of apps/lbmMultiRes/lattice.h:14-42: index = 9*a + 3*b + c
+// with digit 0 -> 0, 1 -> -1, 2 -> +1 for (cx, cy, cz); the rest population first.
+inline int d27_digit_to_c(int d) { return d == 0 ? 0 : (d == 1 ? -1 : 1); }
+inline int c27(int q, int axis)
+{
+    const int a = q / 9, b = (q / 3) % 3, c = q % 3;
+    return d27_digit_to_c(axis == 0 ? a : (axis == 1 ? b : c));
+}
+inline int opp27(int q)
+{
+    auto flip = [](int d) { return d == 0 ? 0 : 3 - d; };
+    return 9 * flip(q / 9) + 3 * flip((q / 3) % 3) + flip(q % 3);
+}
+inline double w27(int q)
+{
+    int nz = (c27(q, 0) != 0) + (c27(q, 1) != 0) + (c27(q, 2) != 0);
+    return nz == 0 ? 8. / 27. : (nz == 1 ? 2. / 27. : (nz == 2 ? 1. / 54. : 1. / 216.));
+}
+
+// ---------------------------------------------------------------- cell type
+// CellType.h:3-35: {uint32 wallNghBitflag; classification}.
+enum Classification : int { bounceBack = 0, movingWall = 1, bulk = 2, undefined = 3 };
+struct CellType {
+    uint32_t wallNghBitflag = 0;
+    int      classification = bulk;
+};
+
+// ---------------------------------------------------------------- storage conversions
+// IEEE-754 binary16 / bfloat16 with round-to-nearest-even, written from the
+// format definitions (used for the equilibrium-offset storage forms).
+inline uint16_t f32_to_f16(float f)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return uint16_t(sign | 0x7c00u | (ax > 0x7f800000u ? 0x200u : 0u));
+    if (ax >= 0x477ff000u) return uint16_t(sign | 0x7c00u);  // rounds to infinity
+    if (ax < 0x38800000u) {                                   // half subnormal or zero
+        const int e = int(ax >> 23);
+        if (e == 0) return uint16_t(sign);
+        const uint32_t m = (ax & 0x7fffffu) | 0x800000u;
+        const int      shift = 126 - e;
+        if (shift >= 25) return uint16_t(sign);
+        uint32_t       r = m >> shift;
+        const uint32_t rem = m & ((1u << shift) - 1u);
+        const uint32_t half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (r & 1u))) r++;
+        return uint16_t(sign | r);
+    }
+    uint32_t       r = ((((ax >> 23) - 127u + 15u) << 10) | ((ax & 0x7fffffu) >> 13));
+    const uint32_t rem = ax & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (r & 1u))) r++;
+    return uint16_t(sign | r);
+}
+inline float f16_to_f32(uint16_t h)
+{
+    const uint32_t sign = uint32_t(h & 0x8000u) << 16;
+    const uint32_t e = (h >> 10) & 0x1fu;
+    const uint32_t m = h & 0x3ffu;
+    uint32_t       x;
+    if (e == 0) {
+        if (m == 0) {
+            x = sign;
+        } else {  // subnormal: m * 2^-24
+            float v = float(m) * (1.0f / 16777216.0f);
+            std::memcpy(&x, &v, 4);
+            x |= sign;
+        }
+    } else if (e == 31) {
+        x = sign | 0x7f800000u | (m << 13);
+    } else {
+        x = sign | ((e - 15u + 127u) << 23) | (m << 13);
+    }
+    float f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+inline uint16_t f32_to_bf16(float f)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    if ((x & 0x7fffffffu) > 0x7f800000u) return uint16_t((x >> 16) | 0x40u);
+    const uint32_t lsb = (x >> 16) & 1u;
+    x += 0x7fffu + lsb;
+    return uint16_t(x >> 16);
+}
+inline float bf16_to_f32(uint16_t b)
+{
+    uint32_t x = uint32_t(b) << 16;
+    float    f;
+    std::memcpy(&f, &x, 4);
+    return f;
+}
+
+// ---------------------------------------------------------------- set-up
+// Config.cpp:105-111
+inline double cavity_omega(int N, double ulb, double Re)
+{
+    const double nu = ulb * double(N - 2) / Re;
+    return 1. / (3. * nu + 0.5);
+}
+
+// Stored value of population k at a wall node (RunCavityTwoPop.cu:168-206):
+// 0 for resting walls, -6 w_k u_lb (c_k . u_lid) on the moving lid.
+inline double wall_term19(int k, bool lid, double ulb)
+{
+    if (!lid) return 0.0;
+    const double ulid[3] = {1., 0., 0.};
+    return -6. * kW19[k] * ulb * (kC19[k][0] * ulid[0] + kC19[k][1] * ulid[1] + kC19[k][2] * ulid[2]);
+}
+inline double wall_term27(int k, bool lid, double ulb)
+{
+    if (!lid) return 0.0;
+    return -6. * w27(k) * ulb * double(c27(k, 0));
+}
+
+inline bool on_box_face(int x, int y, int z, int nx, int ny, int nz)
+{
+    return x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+}
+
+// Population layout of a single-partition Neon dField (dField_imp.h:71-77):
+// element (x, y, z, q) at x + y*nx + z*nx*ny + q*nx*ny*nz.
+inline size_t lin(int x, int y, int z, int nx, int ny) { return size_t(x) + size_t(nx) * (size_t(y) + size_t(ny) * size_t(z)); }
+
+template <typename S>
+void cavity_init_populations(int nx, int ny, int nz, int Q, double ulb, S* pop)
+{
+    const size_t V = size_t(nx) * ny * nz;
+    for (int q = 0; q < Q; q++)
+        for (int z = 0; z < nz; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++) {
+                    double w = Q == 19 ? kW19[q] : w27(q);
+                    double val = w;
+                    if (on_box_face(x, y, z, nx, ny, nz)) {
+                        const bool lid = (y == ny - 1);
+                        val = Q == 19 ? wall_term19(q, lid, ulb) : wall_term27(q, lid, ulb);
+                    }
+                    pop[q * V + lin(x, y, z, nx, ny)] = S(val);
+                }
+}
+
+inline void cavity_init_flags(int nx, int ny, int nz, CellType* flag)
+{
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                CellType c;
+                c.classification = bulk;
+                if (on_box_face(x, y, z, nx, ny, nz)) c.classification = (y == ny - 1) ? movingWall : bounceBack;
+                flag[lin(x, y, z, nx, ny)] = c;
+            }
+}
+
+// LbmTools.h:327-376: for bulk cells, bit q is set iff the pull source x - c_q
+// is not bulk (a missing neighbour counts as "undefined", i.e. not bulk).
+inline void compute_wall_mask(int nx, int ny, int nz, int Q, CellType* flag)
+{
+    std::vector<CellType> in(flag, flag + size_t(nx) * ny * nz);
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                CellType c = in[lin(x, y, z, nx, ny)];
+                c.wallNghBitflag = 0;
+                if (c.classification != bulk) continue;
+                for (int q = 0; q < Q; q++) {
+                    const int cx = Q == 19 ? kC19[q][0] : c27(q, 0);
+                    const int cy = Q == 19 ? kC19[q][1] : c27(q, 1);
+                    const int cz = Q == 19 ? kC19[q][2] : c27(q, 2);
+                    if (cx == 0 && cy == 0 && cz == 0) continue;
+                    const int sx = x - cx, sy = y - cy, sz = z - cz;
+                    int       cls = undefined;
+                    if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = in[lin(sx, sy, sz, nx, ny)].classification;
+                    if (cls != bulk) c.wallNghBitflag |= (uint32_t(1) << q);
+                }
+                flag[lin(x, y, z, nx, ny)] = c;
+            }
+}
+
+// ---------------------------------------------------------------- D3Q19 step (reference arithmetic)
+// One pull stream-collide step over every bulk cell (LbmTools.h:284-325).
+// S = storage type, C = compute type.
+template <typename S, typename C>
+void d3q19_step(int nx, int ny, int nz, const S* fin, S* fout, const CellType* flag, C omega,
+                int z_begin = 0, int z_end = -1)
+{
+    const size_t V = size_t(nx) * ny * nz;
+    if (z_end < 0) z_end = nz;
+    auto at = [&](int x, int y, int z, int q) -> S { return fin[size_t(q) * V + lin(x, y, z, nx, ny)]; };
+    for (int z = z_begin; z < z_end; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (cell.classification != bulk) continue;
+                const uint32_t m = cell.wallNghBitflag;
+                S              pop[19];
+                // Pull stream (LbmTools.h:78-168): population q arrives from x - c_q;
+                // if that node is a wall, the opposite population of this cell is
+                // reflected and the wall's stored term is added.
+                for (int go = 0; go < 9; go++) {
+                    const int bk = go + 10;
+                    const int gx = kC19[go][0], gy = kC19[go][1], gz = kC19[go][2];
+                    if (m & (uint32_t(1) << go))
+                        pop[go] = at(x, y, z, bk) + at(x - gx, y - gy, z - gz, bk);
+                    else
+                        pop[go] = at(x - gx, y - gy, z - gz, go);
+                    if (m & (uint32_t(1) << bk))
+                        pop[bk] = at(x, y, z, go) + at(x + gx, y + gy, z + gz, go);
+                    else
+                        pop[bk] = at(x + gx, y + gy, z + gz, bk);
+                }
+                pop[9] = at(x, y, z, 9);
+
+                // Macroscopic moments (LbmTools.h:171-195), grouped sums in the same order.
+#define P(I) static_cast<C>(pop[I])
+                const C X_M1 = P(0) + P(3) + P(4) + P(5) + P(6);
+                const C X_P1 = P(10) + P(13) + P(14) + P(15) + P(16);
+                const C X_0 = P(9) + P(1) + P(2) + P(7) + P(8) + P(11) + P(12) + P(17) + P(18);
+                const C Y_M1 = P(1) + P(3) + P(7) + P(8) + P(14);
+                const C Y_P1 = P(4) + P(11) + P(13) + P(17) + P(18);
+                const C Z_M1 = P(2) + P(5) + P(7) + P(16) + P(18);
+                const C Z_P1 = P(6) + P(8) + P(12) + P(15) + P(17);
+                const C rho = X_M1 + X_P1 + X_0;
+                const C u0 = (X_P1 - X_M1) / rho;
+                const C u1 = (Y_P1 - Y_M1) / rho;
+                const C u2 = (Z_P1 - Z_M1) / rho;
+                const C usqr = 1.5 * (u0 * u0 + u1 * u1 + u2 * u2);
+
+                // BGK (LbmTools.h:198-282): the "go" equilibria, their opposites via
+                // + rho w 6 (c.u), then (1 - omega) f + omega eq.
+                const C cu[9] = {u0, u1, u2, u0 + u1, u0 - u1, u0 + u2, u0 - u2, u1 + u2, u1 - u2};
+                for (int k = 0; k < 9; k++) {
+                    const double wk = k < 3 ? (1. / 18.) : (1. / 36.);
+                    // cu[k] here is c_{opp k} . u; the go direction has c_k . u = -cu[k].
+                    const C eq = rho * wk * (1. - 3. * cu[k] + 4.5 * cu[k] * cu[k] - usqr);
+                    const C eqopp = eq + rho * wk * 6. * cu[k];
+                    const C out = (1. - omega) * P(k) + omega * eq;
+                    const C outopp = (1. - omega) * P(k + 10) + omega * eqopp;
+                    fout[size_t(k) * V + lin(x, y, z, nx, ny)] = static_cast<S>(out);
+                    fout[size_t(k + 10) * V + lin(x, y, z, nx, ny)] = static_cast<S>(outopp);
+                }
+                {
+                    const C eq9 = rho * (1. / 3.) * (1. - usqr);
+                    const C out9 = (1. - omega) * P(9) + omega * eq9;
+                    fout[size_t(9) * V + lin(x, y, z, nx, ny)] = static_cast<S>(out9);
+                }
+#undef P
+            }
+}
+
+// ---------------------------------------------------------------- generic BGK step (D3Q19 / D3Q27, any storage)
+// The project's own D3Q19/D3Q27 BGK in a plain per-direction form, used for
+// D3Q27 (which the reference does not have as single-resolution BGK) and for
+// the equilibrium-offset storage forms. Storage is accessed through Load/Store
+// functors so that f16/bf16 offsets (g = f - w) share this code.
+//   rho = sum_q f_q; u = sum_q c_q f_q / rho
+//   eq_q = rho w_q (1 + 3 c.u + 4.5 (c.u)^2 - 1.5 |u|^2)
+//   f_q' = (1 - omega) f_q + omega eq_q
+// Wall rule identical to the D3Q19 reference step: bit q set -> f(x, opp q) + wall term.
+template <typename C, int Q, typename Load, typename Store, typename WallTerm>
+void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Load load, Store store, WallTerm wall,
+                      int z_begin = 0, int z_end = -1)
+{
+    if (z_end < 0) z_end = nz;
+    int    cx[Q], cy[Q], cz[Q], op[Q];
+    double w[Q];
+    for (int q = 0; q < Q; q++) {
+        cx[q] = Q == 19 ? kC19[q][0] : c27(q, 0);
+        cy[q] = Q == 19 ? kC19[q][1] : c27(q, 1);
+        cz[q] = Q == 19 ? kC19[q][2] : c27(q, 2);
+        op[q] = Q == 19 ? opp19(q) : opp27(q);
+        w[q] = Q == 19 ? kW19[q] : w27(q);
+    }
+    for (int z = z_begin; z < z_end; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (cell.classification != bulk) continue;
+                C f[Q];
+                for (int q = 0; q < Q; q++) {
+                    const int sx = x - cx[q], sy = y - cy[q], sz = z - cz[q];
+                    if (cell.wallNghBitflag & (uint32_t(1) << q)) {
+                        int cls = undefined;
+                        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = flag[lin(sx, sy, sz, nx, ny)].classification;
+                        f[q] = load(x, y, z, op[q]) + wall(cls, op[q]);
+                    } else {
+                        f[q] = load(sx, sy, sz, q);
+                    }
+                }
+                C rho = 0, mx = 0, my = 0, mz = 0;
+                for (int q = 0; q < Q; q++) {
+                    rho += f[q];
+                    mx += C(cx[q]) * f[q];
+                    my += C(cy[q]) * f[q];
+                    mz += C(cz[q]) * f[q];
+                }
+                const C ux = mx / rho, uy = my / rho, uz = mz / rho;
+                const C usqr = C(1.5) * (ux * ux + uy * uy + uz * uz);
+                for (int q = 0; q < Q; q++) {
+                    const C cu = C(cx[q]) * ux + C(cy[q]) * uy + C(cz[q]) * uz;
+                    const C eq = rho * C(w[q]) * (C(1) + C(3) * cu + C(4.5) * cu * cu - usqr);
+                    const C out = (C(1) - omega) * f[q] + omega * eq;
+                    store(x, y, z, q, out);
+                }
+            }
+}
+
+// Macroscopic velocity of every bulk cell from a population field (compute in double).
+template <typename Load>
+void velocity_field(int nx, int ny, int nz, int Q, const CellType* flag, Load load, double* u /* 3*V, SoA */)
+{
+    const size_t V = size_t(nx) * ny * nz;
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const size_t i = lin(x, y, z, nx, ny);
+                u[i] = u[V + i] = u[2 * V + i] = 0.0;
+                if (flag[i].classification != bulk) continue;
+                double rho = 0, m[3] = {0, 0, 0};
+                for (int q = 0; q < Q; q++) {
+                    const double f = load(x, y, z, q);
+                    rho += f;
+                    for (int a = 0; a < 3; a++) m[a] += double(Q == 19 ? kC19[q][a] : c27(q, a)) * f;
+                }
+                for (int a = 0; a < 3; a++) u[a * V + i] = m[a] / rho;
+            }
+}
+
+}  // namespace oracle

@@ -1,0 +1,152 @@
+"""GPU parity of the dense LBM step (C-ABI) against the CPU oracle.
+
+Cavity of benchmarks/lbm-lid-driven-cavity-flow (lid u along +x on y = N-1,
+Re = 100, nu = u (N-2) / Re, equilibrium start). Tolerances: FP64 1e-12 and
+FP32 1e-5 relative (max-norm over all populations); FP16/BF16-offset storage
+is compared through the velocity field.
+"""
+import numpy as np
+import pytest
+
+from helpers import P, STORE_DTYPE, oracle_cavity, oracle_velocity, rel_max
+
+pytestmark = pytest.mark.gpu
+
+def _tdtype(storage):
+    import torch
+    return {0: torch.float64, 1: torch.float32, 2: torch.float16, 3: torch.bfloat16}[storage]
+
+
+def gpu_cavity(ngb, cuda, n, q, storage, steps, ulb=0.1, re=100.0, box=True, use_run=True):
+    import torch
+    V = n ** 3
+    omega = ngb.cavity_omega(n, ulb, re)
+    desc = ngb.lbm_dense_desc(n, n, n, q, storage, omega, ngb.lid_wall_terms(q, ulb), box_cavity=box)
+    fa = torch.empty(q * V, dtype=_tdtype(storage), device=cuda)
+    fb = torch.empty_like(fa)
+    flags = torch.empty(V, dtype=torch.int32, device=cuda)
+    ngb.lbm_cavity_init(desc, ulb, fa, fb, flags)
+    if use_run:
+        ngb.lbm_dense_run(desc, fa, fb, steps, flags=None if box else flags)
+    else:
+        for t in range(steps):
+            src, dst = (fa, fb) if t % 2 == 0 else (fb, fa)
+            ngb.lbm_dense_step(desc, src, dst, flags=None if box else flags)
+    torch.cuda.synchronize()
+    out = fa if steps % 2 == 0 else fb
+    return desc, out, flags
+
+
+def to_numpy_storage(t, storage):
+    import torch
+    if storage in (2, 3):
+        return t.view(torch.int16).cpu().numpy().view(np.uint16)
+    return t.cpu().numpy()
+
+
+def test_flags_match_oracle(ngb, orc, cuda):
+    for q in (19, 27):
+        n = 12
+        _, _, flags = gpu_cavity(ngb, cuda, n, q, 1, 0)
+        ref = np.zeros(n ** 3, np.uint32)
+        orc.orc_cavity_flags(n, n, n, q, P(ref))
+        assert np.array_equal(flags.cpu().numpy().view(np.uint32), ref)
+
+
+@pytest.mark.parametrize("box", [True, False])
+def test_d3q19_f64_cavity_64_1000_steps(ngb, orc, cuda, box):
+    """Config 0: D3Q19 BGK cavity, dGrid 64^3, FP64, 1000 steps, all populations <= 1e-12."""
+    n, steps = 64, 1000
+    _, out, _ = gpu_cavity(ngb, cuda, n, 19, 0, steps, box=box)
+    ref, _, _ = oracle_cavity(orc, n, 19, 0, steps)
+    err = rel_max(out.cpu().numpy(), ref)
+    assert err <= 1e-12, err
+
+
+def test_d3q19_f32_cavity(ngb, orc, cuda):
+    n, steps = 48, 1000
+    _, out, _ = gpu_cavity(ngb, cuda, n, 19, 1, steps)
+    ref, _, _ = oracle_cavity(orc, n, 19, 1, steps)
+    err = rel_max(out.cpu().numpy(), ref)
+    assert err <= 1e-5, err
+
+
+def test_d3q27_f64_cavity(ngb, orc, cuda):
+    n, steps = 32, 300
+    _, out, _ = gpu_cavity(ngb, cuda, n, 27, 0, steps)
+    ref, _, _ = oracle_cavity(orc, n, 27, 0, steps)
+    err = rel_max(out.cpu().numpy(), ref)
+    assert err <= 1e-12, err
+
+
+def test_d3q27_f32_cavity(ngb, orc, cuda):
+    n, steps = 32, 300
+    _, out, _ = gpu_cavity(ngb, cuda, n, 27, 1, steps)
+    ref, _, _ = oracle_cavity(orc, n, 27, 1, steps)
+    err = rel_max(out.cpu().numpy(), ref)
+    assert err <= 1e-5, err
+
+
+@pytest.mark.parametrize("q", [19, 27])
+@pytest.mark.parametrize("storage,tol_vs_oracle,tol_vs_f64", [(2, 2e-4, 1e-3), (3, 2e-3, 1e-2)])
+def test_offset_storage_velocity(ngb, orc, cuda, q, storage, tol_vs_oracle, tol_vs_f64):
+    """FP16/BF16 g = f - w storage with FP32 collision: velocity vs the oracle's
+    same-storage run and vs the FP64 reference run."""
+    n, steps = 32, 400
+    desc, out, flags = gpu_cavity(ngb, cuda, n, q, storage, steps)
+    import torch
+    u = torch.zeros(3 * n ** 3, dtype=torch.float64, device=cuda)
+    ngb.lbm_dense_macroscopic(desc, out, u=u)
+    u = u.cpu().numpy()
+    pop16, oflags, _ = oracle_cavity(orc, n, q, storage, steps)
+    u16 = oracle_velocity(orc, n, q, storage, oflags, pop16)
+    pop64, _, _ = oracle_cavity(orc, n, q, 0, steps)
+    u64 = oracle_velocity(orc, n, q, 0, oflags, pop64)
+    e_or = np.linalg.norm(u - u16) / np.linalg.norm(u64)
+    e_64 = np.linalg.norm(u - u64) / np.linalg.norm(u64)
+    assert e_or <= tol_vs_oracle, e_or
+    assert e_64 <= tol_vs_f64, e_64
+
+
+@pytest.mark.parametrize("storage", [0, 1, 2])
+def test_run_graph_equals_steps_and_is_deterministic(ngb, cuda, storage):
+    import torch
+    n, steps = 24, 70
+    _, a, _ = gpu_cavity(ngb, cuda, n, 19, storage, steps, use_run=True)
+    _, b, _ = gpu_cavity(ngb, cuda, n, 19, storage, steps, use_run=False)
+    _, c, _ = gpu_cavity(ngb, cuda, n, 19, storage, steps, use_run=True)
+    assert torch.equal(a, b)
+    assert torch.equal(a, c)
+
+
+def test_macroscopic_matches_oracle(ngb, orc, cuda):
+    import torch
+    n, steps = 20, 50
+    desc, out, flags = gpu_cavity(ngb, cuda, n, 19, 0, steps)
+    u = torch.zeros(3 * n ** 3, dtype=torch.float64, device=cuda)
+    rho = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
+    ngb.lbm_dense_macroscopic(desc, out, rho=rho, u=u)
+    pop, oflags, _ = oracle_cavity(orc, n, 19, 0, steps)
+    uo = oracle_velocity(orc, n, 19, 0, oflags, pop)
+    bulk = (oflags >> 28) == 2
+    un = u.cpu().numpy().reshape(3, -1)
+    assert np.abs(un[:, bulk] - uo.reshape(3, -1)[:, bulk]).max() <= 1e-13
+    # moving-wall cells report u_x = lid speed (LbmTools.h:411-427)
+    lid = (oflags >> 28) == 1
+    assert np.allclose(un[0, lid], 0.1, rtol=1e-12)
+
+
+def test_invalid_arguments_report_errors(ngb, cuda):
+    import ctypes
+    import torch
+    d = ngb.lbm_dense_desc(8, 8, 8, 19, "f32", 1.0)
+    x = torch.empty(19 * 512, device=cuda)
+    with pytest.raises(ngb.NeonError, match="distinct"):
+        ngb.lbm_dense_step(d, x, x)
+    d.q = 7
+    with pytest.raises(ngb.NeonError, match="q must be 19 or 27"):
+        ngb.lbm_dense_step(d, x, torch.empty_like(x))
+    d.q = 19
+    d.box_cavity = 0
+    with pytest.raises(ngb.NeonError, match="flags required"):
+        ngb.lbm_dense_step(d, x, torch.empty_like(x))
