@@ -54,7 +54,8 @@ def lib():
         L.orc_cavity_init.argtypes = [c_int, c_int, c_int, c_int, c_int, c_double, c_void_p]
         L.orc_cavity_flags.argtypes = [c_int, c_int, c_int, c_int, c_void_p]
         L.orc_wall_mask.argtypes = [c_int, c_int, c_int, c_int, c_void_p]
-        L.orc_velocity.argtypes = [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]
+        L.orc_velocity.argtypes = [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p]
         L.orc_time_d3q19_f32.argtypes = [c_int, c_int, c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]
         L.orc_time_d3q19_f32.restype = c_double
         for f in ("orc_f32_to_f16", "orc_f16_to_f32", "orc_f32_to_bf16", "orc_bf16_to_f32"):

@@ -351,24 +351,46 @@ void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Loa
             }
 }
 
-// Macroscopic velocity of every bulk cell from a population field (compute in double).
-template <typename Load>
-void velocity_field(int nx, int ny, int nz, int Q, const CellType* flag, Load load, double* u /* 3*V, SoA */)
+// Density and velocity (LbmTools.h:383-437, computeRhoAndU), in double:
+// bulk cells pull their populations exactly like the step (wall rule
+// included) and take rho = sum f, u = sum c f / rho; moving-wall cells report
+// rho = 1 and u_a = f_a / (6/18) from their stored lid term (a = 0, 1, 2 in
+// the D3Q19 order; D3Q27 moving walls report 0); every other cell 0.
+template <typename Load, typename WallTerm>
+void rho_u_field(int nx, int ny, int nz, int Q, const CellType* flag, Load load, WallTerm wall, double* rho_out,
+                 double* u /* 3*V, SoA */)
 {
     const size_t V = size_t(nx) * ny * nz;
     for (int z = 0; z < nz; z++)
         for (int y = 0; y < ny; y++)
             for (int x = 0; x < nx; x++) {
                 const size_t i = lin(x, y, z, nx, ny);
-                u[i] = u[V + i] = u[2 * V + i] = 0.0;
-                if (flag[i].classification != bulk) continue;
-                double rho = 0, m[3] = {0, 0, 0};
-                for (int q = 0; q < Q; q++) {
-                    const double f = load(x, y, z, q);
-                    rho += f;
-                    for (int a = 0; a < 3; a++) m[a] += double(Q == 19 ? kC19[q][a] : c27(q, a)) * f;
+                double       rho = 0, m[3] = {0, 0, 0};
+                if (flag[i].classification == bulk) {
+                    for (int q = 0; q < Q; q++) {
+                        const int cx = Q == 19 ? kC19[q][0] : c27(q, 0);
+                        const int cy = Q == 19 ? kC19[q][1] : c27(q, 1);
+                        const int cz = Q == 19 ? kC19[q][2] : c27(q, 2);
+                        const int o = Q == 19 ? opp19(q) : opp27(q);
+                        double    f;
+                        if (flag[i].wallNghBitflag & (uint32_t(1) << q)) {
+                            const int sx = x - cx, sy = y - cy, sz = z - cz;
+                            int       cls = undefined;
+                            if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = flag[lin(sx, sy, sz, nx, ny)].classification;
+                            f = load(x, y, z, o) + wall(cls, o);
+                        } else {
+                            f = load(x - cx, y - cy, z - cz, q);
+                        }
+                        rho += f;
+                        m[0] += double(cx) * f, m[1] += double(cy) * f, m[2] += double(cz) * f;
+                    }
+                    for (int a = 0; a < 3; a++) m[a] /= rho;
+                } else if (flag[i].classification == movingWall) {
+                    rho = 1.0;
+                    for (int a = 0; a < 3; a++) m[a] = Q == 19 ? wall(movingWall, a) / (6. * 1. / 18.) : 0.0;
                 }
-                for (int a = 0; a < 3; a++) u[a * V + i] = m[a] / rho;
+                if (rho_out) rho_out[i] = rho;
+                for (int a = 0; a < 3; a++) u[a * V + i] = m[a];
             }
 }
 

@@ -180,12 +180,15 @@ int orc_lbm_run(int nx, int ny, int nz, int Q, int storage, int mode, int comput
     return 0;
 }
 
-// Velocity (3 x V, SoA) of every bulk cell from a population field.
-int orc_velocity(int nx, int ny, int nz, int Q, int storage, const uint32_t* packed, const void* pop, double* u)
+// Density (V, may be NULL) and velocity (3 x V, SoA) as computeRhoAndU
+// (LbmTools.h:383-437); wall = 4 x 27 wall terms by classification.
+int orc_velocity(int nx, int ny, int nz, int Q, int storage, const double* wall, const uint32_t* packed, const void* pop,
+                 double* rho, double* u)
 {
     const size_t          V = size_t(nx) * ny * nz;
     std::vector<CellType> flag(V);
     for (size_t i = 0; i < V; i++) flag[i] = unpack(packed[i]);
+    auto wt = [&](int cls, int q) -> double { return (wall && cls >= 0 && cls < 4) ? wall[cls * 27 + q] : 0.0; };
     auto load = [&](int x, int y, int z, int q) -> double {
         const size_t i = size_t(q) * V + lin(x, y, z, nx, ny);
         switch (storage) {
@@ -195,7 +198,7 @@ int orc_velocity(int nx, int ny, int nz, int Q, int storage, const uint32_t* pac
             default: return double(bf16_to_f32(static_cast<const uint16_t*>(pop)[i])) + double(float(weight(Q, q)));
         }
     };
-    velocity_field(nx, ny, nz, Q, flag.data(), load, u);
+    rho_u_field(nx, ny, nz, Q, flag.data(), load, wt, rho, u);
     return 0;
 }
 

@@ -45,9 +45,11 @@ def oracle_cavity(orc, n, q, storage, steps, ulb=0.1, re=100.0, mode=None, compu
     return (a if steps % 2 == 0 else b), flags, omega
 
 
-def oracle_velocity(orc, n, q, storage, flags, pop):
+def oracle_velocity(orc, n, q, storage, flags, pop, ulb=0.1, rho=None):
+    """Velocity field as computeRhoAndU (LbmTools.h:383-437): pulled populations on bulk cells."""
     u = np.zeros(3 * n ** 3)
-    orc.orc_velocity(n, n, n, q, storage, P(flags), P(pop), P(u))
+    wt = wall_table(q, ulb, storage)
+    orc.orc_velocity(n, n, n, q, storage, P(wt), P(flags), P(pop), P(rho) if rho is not None else None, P(u))
     return u
 
 
