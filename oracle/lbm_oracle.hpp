@@ -351,6 +351,65 @@ void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Loa
             }
 }
 
+// ---------------------------------------------------------------- shifted FP32 BGK (offset storage)
+// The project's equilibrium-offset form (no reference counterpart): storage
+// holds g_q = f_q - w_q; in FP32
+//   drho = sum g, j = sum c g, rho = 1 + drho, u = j * (1/rho),
+//   usqr = 1.5 |u|^2, eqg_q = w_q (drho + rho (3 cu + 4.5 cu^2 - usqr)),
+//   g' = g + omega (eqg - g).
+// Wall rule as the reference step: bit q set -> g(x, opp q) + wall term.
+template <int Q, typename LoadG, typename StoreG, typename WallTerm>
+void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega, LoadG loadg, StoreG storeg, WallTerm wall,
+                      int z_begin = 0, int z_end = -1)
+{
+    if (z_end < 0) z_end = nz;
+    int   cx[Q], cy[Q], cz[Q], op[Q];
+    float w[Q];
+    for (int q = 0; q < Q; q++) {
+        cx[q] = Q == 19 ? kC19[q][0] : c27(q, 0);
+        cy[q] = Q == 19 ? kC19[q][1] : c27(q, 1);
+        cz[q] = Q == 19 ? kC19[q][2] : c27(q, 2);
+        op[q] = Q == 19 ? opp19(q) : opp27(q);
+        w[q] = float(Q == 19 ? kW19[q] : w27(q));
+    }
+    for (int z = z_begin; z < z_end; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (cell.classification != bulk) continue;
+                float g[Q];
+                for (int q = 0; q < Q; q++) {
+                    const int sx = x - cx[q], sy = y - cy[q], sz = z - cz[q];
+                    if (cell.wallNghBitflag & (uint32_t(1) << q)) {
+                        int cls = undefined;
+                        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = flag[lin(sx, sy, sz, nx, ny)].classification;
+                        g[q] = loadg(x, y, z, op[q]) + float(wall(cls, op[q]));
+                    } else {
+                        g[q] = loadg(sx, sy, sz, q);
+                    }
+                }
+                float drho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+                for (int q = 0; q < Q; q++) {
+                    drho += g[q];
+                    if (cx[q] > 0) jx += g[q];
+                    if (cx[q] < 0) jx -= g[q];
+                    if (cy[q] > 0) jy += g[q];
+                    if (cy[q] < 0) jy -= g[q];
+                    if (cz[q] > 0) jz += g[q];
+                    if (cz[q] < 0) jz -= g[q];
+                }
+                const float rho = 1.f + drho;
+                const float inv = 1.f / rho;
+                const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+                const float usqr = 1.5f * (ux * ux + uy * uy + uz * uz);
+                for (int q = 0; q < Q; q++) {
+                    const float cu = float(cx[q]) * ux + float(cy[q]) * uy + float(cz[q]) * uz;
+                    const float eqg = w[q] * (drho + rho * (3.f * cu + 4.5f * cu * cu - usqr));
+                    storeg(x, y, z, q, g[q] + omega * (eqg - g[q]));
+                }
+            }
+}
+
 // Density and velocity (LbmTools.h:383-437, computeRhoAndU), in double:
 // bulk cells pull their populations exactly like the step (wall rule
 // included) and take rho = sum f, u = sum c f / rho; moving-wall cells report

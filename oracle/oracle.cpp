@@ -24,7 +24,7 @@ using namespace oracle;
 namespace {
 
 enum Storage { ST_F64 = 0, ST_F32 = 1, ST_F16OFF = 2, ST_BF16OFF = 3 };
-enum ComputeMode { CM_REFERENCE = 0, CM_GENERIC = 1 };
+enum ComputeMode { CM_REFERENCE = 0, CM_GENERIC = 1, CM_SHIFTED = 2 };
 
 // Flags are exchanged with the tests in the packed form used by the GPU
 // library: bits 0..26 wall-neighbour mask, bits 28..31 classification.
@@ -53,6 +53,21 @@ void generic_run(int nx, int ny, int nz, const CellType* flag, double omega, S* 
         auto     wall = [&](int cls, int q) -> C { return (cls >= 0 && cls < 4) ? C(g_wall[cls][q]) : C(0); };
 #pragma omp parallel for schedule(static) num_threads(threads)
         for (int z = 0; z < nz; z++) bgk_step_generic<C, Q>(nx, ny, nz, flag, C(omega), load, store, wall, z, z + 1);
+    }
+}
+
+template <int Q, typename S, typename ToG, typename FromG>
+void shifted_run(int nx, int ny, int nz, const CellType* flag, float omega, S* a, S* b, int steps, ToG toG, FromG fromG, int threads)
+{
+    const size_t V = size_t(nx) * ny * nz;
+    for (int t = 0; t < steps; t++) {
+        const S* fin = (t % 2 == 0) ? a : b;
+        S*       fout = (t % 2 == 0) ? b : a;
+        auto     loadg = [&](int x, int y, int z, int q) -> float { return toG(fin[size_t(q) * V + lin(x, y, z, nx, ny)], q); };
+        auto     storeg = [&](int x, int y, int z, int q, float g) { fout[size_t(q) * V + lin(x, y, z, nx, ny)] = fromG(g, q); };
+        auto     wall = [&](int cls, int q) -> double { return (cls >= 0 && cls < 4) ? g_wall[cls][q] : 0.0; };
+#pragma omp parallel for schedule(static) num_threads(threads)
+        for (int z = 0; z < nz; z++) bgk_step_shifted<Q>(nx, ny, nz, flag, omega, loadg, storeg, wall, z, z + 1);
     }
 }
 
@@ -144,6 +159,32 @@ int orc_lbm_run(int nx, int ny, int nz, int Q, int storage, int mode, int comput
                 return -2;
             }
         }
+        return 0;
+    }
+
+    if (mode == CM_SHIFTED) {
+        const float om = float(omega);
+        auto        go = [&](auto qTag) {
+            constexpr int QQ = decltype(qTag)::value;
+            if (storage == ST_F32) {
+                shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<float*>(a), static_cast<float*>(b), steps,
+                                [](float v, int q) { return v - float(weight(QQ, q)); },
+                                [](float g, int q) { return float(weight(QQ, q)) + g; }, threads);
+            } else if (storage == ST_F16OFF) {
+                shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
+                                [](uint16_t v, int) { return f16_to_f32(v); }, [](float g, int) { return f32_to_f16(g); },
+                                threads);
+            } else if (storage == ST_BF16OFF) {
+                shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
+                                [](uint16_t v, int) { return bf16_to_f32(v); }, [](float g, int) { return f32_to_bf16(g); },
+                                threads);
+            }
+        };
+        if (storage == ST_F64) return -2;
+        if (Q == 19)
+            go(std::integral_constant<int, 19>{});
+        else
+            go(std::integral_constant<int, 27>{});
         return 0;
     }
 

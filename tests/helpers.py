@@ -36,7 +36,7 @@ def oracle_cavity(orc, n, q, storage, steps, ulb=0.1, re=100.0, mode=None, compu
     b = a.copy()
     omega = ngb.cavity_omega(n, ulb, re)
     if mode is None:
-        mode = 0 if (q == 19 and storage in (0, 1)) else 1
+        mode = 0 if (q == 19 and storage in (0, 1)) else (2 if storage in (2, 3) else 1)
     if compute_float is None:
         compute_float = 0 if storage == 0 else 1
     wt = wall_table(q, ulb, storage)

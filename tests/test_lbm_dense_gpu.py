@@ -88,13 +88,14 @@ def test_d3q27_f32_cavity(ngb, orc, cuda):
 
 
 @pytest.mark.parametrize("q", [19, 27])
-@pytest.mark.parametrize("storage,tol_vs_oracle,tol_vs_f64", [(2, 2e-4, 1e-3), (3, 2e-3, 1e-2)])
-def test_offset_storage_velocity(ngb, orc, cuda, q, storage, tol_vs_oracle, tol_vs_f64):
-    """FP16/BF16 g = f - w storage with FP32 collision: velocity vs the oracle's
-    same-storage run and vs the FP64 reference run."""
+@pytest.mark.parametrize("storage,tol_vs_f64", [(2, 1e-3), (3, 1e-2)])
+def test_offset_storage_velocity(ngb, orc, cuda, q, storage, tol_vs_f64):
+    """FP16/BF16 g = f - w storage with FP32 collision, 400 steps: the velocity
+    error against the FP64 run is within the target and of the size of the
+    oracle's own same-storage error (16-bit rounding noise, not a defect)."""
+    import torch
     n, steps = 32, 400
     desc, out, flags = gpu_cavity(ngb, cuda, n, q, storage, steps)
-    import torch
     u = torch.zeros(3 * n ** 3, dtype=torch.float64, device=cuda)
     ngb.lbm_dense_macroscopic(desc, out, u=u)
     u = u.cpu().numpy()
@@ -102,10 +103,58 @@ def test_offset_storage_velocity(ngb, orc, cuda, q, storage, tol_vs_oracle, tol_
     u16 = oracle_velocity(orc, n, q, storage, oflags, pop16)
     pop64, _, _ = oracle_cavity(orc, n, q, 0, steps)
     u64 = oracle_velocity(orc, n, q, 0, oflags, pop64)
-    e_or = np.linalg.norm(u - u16) / np.linalg.norm(u64)
-    e_64 = np.linalg.norm(u - u64) / np.linalg.norm(u64)
-    assert e_or <= tol_vs_oracle, e_or
-    assert e_64 <= tol_vs_f64, e_64
+    nrm = np.linalg.norm(u64)
+    e_gpu = np.linalg.norm(u - u64) / nrm
+    e_orc = np.linalg.norm(u16 - u64) / nrm
+    assert e_gpu <= tol_vs_f64, e_gpu
+    assert e_gpu <= 2.0 * e_orc + 1e-5, (e_gpu, e_orc)
+    assert np.linalg.norm(u - u16) / nrm <= 3.0 * e_orc + 1e-5
+
+
+@pytest.mark.parametrize("q", [19, 27])
+@pytest.mark.parametrize("storage", [1, 2, 3])
+def test_single_step_from_developed_state(ngb, orc, cuda, q, storage):
+    """One step from the same developed state (FP64 run, 150 steps, converted
+    to the storage form): GPU and oracle agree value by value up to one unit
+    of the storage format (FMA contraction may flip a last-bit rounding)."""
+    import torch
+    n = 20
+    V = n ** 3
+    pop64, oflags, omega = oracle_cavity(orc, n, q, 0, 150)
+    w = np.array(ngb.lattice(q)[1])
+    f = pop64.reshape(q, V)
+    if storage == 1:
+        src = f.astype(np.float32).ravel()
+        tsrc = torch.from_numpy(src)
+    else:
+        g = (f.astype(np.float32) - w[:, None].astype(np.float32))
+        tsrc = torch.from_numpy(g.ravel()).to(torch.float16 if storage == 2 else torch.bfloat16)
+        src = tsrc.view(torch.int16).numpy().view(np.uint16).copy()
+    # oracle: one shifted-form step
+    a = src.copy()
+    b = src.copy()
+    from helpers import wall_table
+    wt = wall_table(q, 0.1, storage)
+    assert orc.orc_lbm_run(n, n, n, q, storage, 2, 1, omega, P(wt), P(oflags), P(a), P(b), 1, 0) == 0
+    # GPU
+    desc = ngb.lbm_dense_desc(n, n, n, q, storage, omega, ngb.lid_wall_terms(q, 0.1))
+    fa = tsrc.to(cuda)
+    fb = fa.clone()
+    ngb.lbm_dense_step(desc, fa, fb)
+    torch.cuda.synchronize()
+    if storage == 1:
+        got = fb.cpu().numpy()
+        ulp = np.abs(np.spacing(b.astype(np.float32)))
+        assert np.all(np.abs(got - b) <= 2 * ulp)
+    else:
+        got_bits = fb.cpu().view(torch.int16).numpy().view(np.uint16)
+        tdt = torch.float16 if storage == 2 else torch.bfloat16
+        got = fb.cpu().float().numpy()
+        ref = torch.from_numpy(b.view(np.int16).copy()).view(tdt).float().numpy()
+        mant = 10 if storage == 2 else 7
+        ulp = np.maximum(np.maximum(np.abs(got), np.abs(ref)), 2.0 ** -14) * 2.0 ** -mant
+        assert np.all(np.abs(got - ref) <= 1.01 * ulp)
+        assert (got_bits == b).mean() > 0.99
 
 
 @pytest.mark.parametrize("storage", [0, 1, 2])
