@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", INCLUDE, "-I", CSRC]
 # FP64 reference-arithmetic units: no contraction into FMA.
-NO_FMAD = {"lbm_dense_f64.cu", "bgrid_lbm_f64.cu", "poisson_f64.cu"}
+NO_FMAD = {"lbm_dense_f64.cu", "lbm_pair.cu", "bgrid_lbm_f64.cu", "poisson_f64.cu"}
 
 
 def nvcc():

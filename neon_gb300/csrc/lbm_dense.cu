@@ -8,33 +8,6 @@
 
 namespace ngb {
 
-int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
-                         cudaStream_t s)
-{
-    const dim3 grid((p.nx + kLbmBlockX - 1) / kLbmBlockX, p.ny, p.nz), block(kLbmBlockX);
-#define NGB_LBM_CASE(QQ, T)                                                                                                   \
-    lbm_dense_f32_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p); \
-    break;
-    if (Q == 19) {
-        switch (storage) {
-            case NGB_STORE_F32: NGB_LBM_CASE(19, float)
-            case NGB_STORE_F16OFF: NGB_LBM_CASE(19, __half)
-            case NGB_STORE_BF16OFF: NGB_LBM_CASE(19, __nv_bfloat16)
-            default: set_error("unsupported storage %d", storage); return NGB_ERR_UNSUPPORTED;
-        }
-    } else {
-        switch (storage) {
-            case NGB_STORE_F32: NGB_LBM_CASE(27, float)
-            case NGB_STORE_F16OFF: NGB_LBM_CASE(27, __half)
-            case NGB_STORE_BF16OFF: NGB_LBM_CASE(27, __nv_bfloat16)
-            default: set_error("unsupported storage %d", storage); return NGB_ERR_UNSUPPORTED;
-        }
-    }
-#undef NGB_LBM_CASE
-    NGB_LAUNCH_CHECK("lbm_dense_f32_kernel");
-    return NGB_OK;
-}
-
 namespace {
 
 int validate(const ngb_lbm_dense_desc* d)

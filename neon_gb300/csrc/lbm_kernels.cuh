@@ -88,77 +88,6 @@ __device__ __forceinline__ void outlet_copy(const S* __restrict__ fin, S* __rest
     for (int q = 0; q < Q; q++) fout[q * stride + cell] = fin[q * stride + cell - 1];
 }
 
-// ------------------------------------------------------------------ FP32 compute (shifted)
-// Works on g_q = f_q - w_q: rho = 1 + sum g, j = sum c g (sum c w = 0),
-// eq_q - w_q = w_q (drho + rho (3 c.u + 4.5 (c.u)^2 - 1.5 |u|^2)),
-// g' = g + omega ((eq - w) - g). Same BGK as LbmTools.h:198-282, evaluated
-// on O(Ma) deviations so FP32 keeps ~7 significant digits of the physics.
-template <int Q, typename S>
-__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f32_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                   const uint32_t* __restrict__ flags, DenseParams<float> p)
-{
-    using L = Lattice<Q>;
-    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= p.nx) return;
-    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
-    const int64_t cell = x + sy * y + sz * z;
-    uint32_t      mask, lidbits;
-    const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
-    if (cls == NGB_CELL_OUTLET) {
-        outlet_copy<Q>(fin, fout, stride, cell, x);
-        return;
-    }
-    if (cls != NGB_CELL_BULK) return;
-
-    float g[Q];
-    if (mask == 0) {
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-            g[q] = load_g(fin + q * stride + src, float(L::w(q)));
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            if (mask & (1u << q)) {
-                // half-way bounce-back: f_q = f_{opp q}(x) + wall term of the source node
-                const int   o = L::opp(q);
-                const float wt = (lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o];
-                g[q] = load_g(fin + o * stride + cell, float(L::w(o))) + wt;
-            } else {
-                const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-                g[q] = load_g(fin + q * stride + src, float(L::w(q)));
-            }
-        }
-    }
-
-    float drho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        drho += g[q];
-        if (L::cx(q) > 0) jx += g[q];
-        if (L::cx(q) < 0) jx -= g[q];
-        if (L::cy(q) > 0) jy += g[q];
-        if (L::cy(q) < 0) jy -= g[q];
-        if (L::cz(q) > 0) jz += g[q];
-        if (L::cz(q) < 0) jz -= g[q];
-    }
-    const float rho = 1.f + drho;
-    const float inv = 1.f / rho;
-    const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-    const float usqr = 1.5f * (ux * ux + uy * uy + uz * uz);
-    const float om = p.omega;
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        const float cu = float(L::cx(q)) * ux + float(L::cy(q)) * uy + float(L::cz(q)) * uz;
-        const float w = float(L::w(q));
-        const float eqg = w * (drho + rho * (3.f * cu + 4.5f * cu * cu - usqr));
-        const float go = g[q] + om * (eqg - g[q]);
-        store_g(fout + q * stride + cell, go, w);
-    }
-}
-
 // ------------------------------------------------------------------ FP64 compute (reference arithmetic)
 // D3Q19: the expression shapes of LbmTools.h:78-282 in double (compile with
 // --fmad=false for IEEE operation order). D3Q27: the project's per-direction

@@ -1,0 +1,299 @@
+// Dense LBM pull stream-collide, FP32 compute on equilibrium-shifted values,
+// two x-adjacent cells per thread.
+//
+// Each thread owns the cell pair (x0, x0+1), x0 even. Every population plane
+// is read with one aligned 2-element load per thread (8 B for FP32, 4 B for
+// the 16-bit offset forms) when the source is x-aligned, and with two aligned
+// loads plus a byte permute when the source is shifted by +-1 in x; the
+// result is stored with one aligned 2-element store. The BGK arithmetic runs
+// on float2 with Blackwell's packed FP32 instructions (fma/add/mul .f32x2),
+// halving the issued math instructions per cell.
+//
+// The arithmetic is an explicit sequence of IEEE operations (this file is
+// compiled with --fmad=false; every fused multiply-add is written out), so a
+// CPU restatement using std::fmaf at the same places reproduces it bit for bit:
+//   drho = sum_q g_q (q ascending); j_a = sum_{c_a>0} g - sum_{c_a<0} g
+//   rho = 1 + drho; inv = 1 / rho; u = j * inv
+//   usq = fma(uz, uz, fma(uy, uy, ux*ux)); rus = rho * (1.5 * usq); base = drho - rus
+//   u3 = 3 u; per weight class: wr = w rho, wb = w base
+//   per q: t = c . u3 (adds in x, y, z order); a = fma(0.5 t, t, t)
+//          eqg = fma(wr, a, wb); g' = fma(omega, eqg - g, g)
+#pragma once
+#include "lbm_kernels.cuh"
+
+namespace ngb {
+
+constexpr int kPairX = 32;  // pairs per block row (64 cells)
+constexpr int kPairY = 4;   // rows per block
+
+// ------------------------------------------------------------------ packed FP32 helpers
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float  add2(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float  sub2(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float  mul2(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float  fma2(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <typename V>
+__device__ __forceinline__ V splat(float a);
+template <>
+__device__ __forceinline__ float2 splat<float2>(float a) { return make_float2(a, a); }
+template <>
+__device__ __forceinline__ float splat<float>(float a) { return a; }
+__device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float  neg(float a) { return -a; }
+__device__ __forceinline__ float2 recip(float2 a) { return make_float2(1.f / a.x, 1.f / a.y); }
+__device__ __forceinline__ float  recip(float a) { return 1.f / a; }
+
+// ------------------------------------------------------------------ storage access in pairs
+template <typename S>
+struct PairIO;
+
+template <>
+struct PairIO<float> {
+    using Word = float2;
+    __device__ __forceinline__ static Word load(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+    // (a.hi, b.lo)
+    __device__ __forceinline__ static Word mid(Word a, Word b) { return make_float2(a.y, b.x); }
+    __device__ __forceinline__ static float2 to_g(Word v, float w) { return make_float2(v.x - w, v.y - w); }
+    __device__ __forceinline__ static float  to_g1(float v, float w) { return v - w; }
+    __device__ __forceinline__ static void   store(float* p, float2 g, float w)
+    {
+        *reinterpret_cast<float2*>(p) = make_float2(w + g.x, w + g.y);
+    }
+    __device__ __forceinline__ static void store1(float* p, float g, float w) { *p = w + g; }
+};
+
+template <>
+struct PairIO<__half> {
+    using Word = __half2;
+    __device__ __forceinline__ static Word load(const __half* p) { return __ldg(reinterpret_cast<const __half2*>(p)); }
+    __device__ __forceinline__ static Word mid(Word a, Word b) { return __halves2half2(__high2half(a), __low2half(b)); }
+    __device__ __forceinline__ static float2 to_g(Word v, float) { return __half22float2(v); }
+    __device__ __forceinline__ static float  to_g1(__half v, float) { return __half2float(v); }
+    __device__ __forceinline__ static void   store(__half* p, float2 g, float)
+    {
+        *reinterpret_cast<__half2*>(p) = __floats2half2_rn(g.x, g.y);
+    }
+    __device__ __forceinline__ static void store1(__half* p, float g, float) { *p = __float2half_rn(g); }
+};
+
+template <>
+struct PairIO<__nv_bfloat16> {
+    using Word = __nv_bfloat162;
+    __device__ __forceinline__ static Word load(const __nv_bfloat16* p)
+    {
+        return __ldg(reinterpret_cast<const __nv_bfloat162*>(p));
+    }
+    __device__ __forceinline__ static Word mid(Word a, Word b) { return __halves2bfloat162(__high2bfloat16(a), __low2bfloat16(b)); }
+    __device__ __forceinline__ static float2 to_g(Word v, float) { return __bfloat1622float2(v); }
+    __device__ __forceinline__ static float  to_g1(__nv_bfloat16 v, float) { return __bfloat162float(v); }
+    __device__ __forceinline__ static void   store(__nv_bfloat16* p, float2 g, float)
+    {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(g.x, g.y);
+    }
+    __device__ __forceinline__ static void store1(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
+};
+
+// Scalar pull of one cell's populations as g (wall rule included).
+template <int Q, typename S>
+__device__ __forceinline__ void pull_one(const S* __restrict__ fin, int64_t stride, int64_t cell, int64_t sy, int64_t sz,
+                                         uint32_t mask, uint32_t lidbits, const DenseParams<float>& p, float* g)
+{
+    using L = Lattice<Q>;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (mask & (1u << q)) {
+            const int   o = L::opp(q);
+            const float wt = (lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o];
+            g[q] = PairIO<S>::to_g1(__ldg(fin + o * stride + cell), float(L::w(o))) + wt;
+        } else {
+            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            g[q] = PairIO<S>::to_g1(__ldg(fin + q * stride + src), float(L::w(q)));
+        }
+    }
+}
+
+template <int Q>
+struct WeightClass;
+template <>
+struct WeightClass<19> {
+    static constexpr int n = 3;
+    __host__ __device__ static constexpr int of(int q) { return q == 9 ? 0 : ((q % 10) < 3 ? 1 : 2); }
+    __host__ __device__ static constexpr double w(int k) { return k == 0 ? 1. / 3. : (k == 1 ? 1. / 18. : 1. / 36.); }
+};
+template <>
+struct WeightClass<27> {
+    static constexpr int n = 4;
+    __host__ __device__ static constexpr int of(int q)
+    {
+        return (Lattice<27>::cx(q) != 0) + (Lattice<27>::cy(q) != 0) + (Lattice<27>::cz(q) != 0);
+    }
+    __host__ __device__ static constexpr double w(int k)
+    {
+        return k == 0 ? 8. / 27. : (k == 1 ? 2. / 27. : (k == 2 ? 1. / 54. : 1. / 216.));
+    }
+};
+
+// t = c_q . u3 with adds in x, y, z order (first non-zero component starts the sum).
+template <int Q, typename V>
+__device__ __forceinline__ V cdot(int q, V u3x, V u3y, V u3z)
+{
+    using L = Lattice<Q>;
+    V          t = splat<V>(0.f);
+    bool       started = false;
+    const int  c[3] = {L::cx(q), L::cy(q), L::cz(q)};
+    const V    u[3] = {u3x, u3y, u3z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (c[a] == 0) continue;
+        if (!started) {
+            t = c[a] > 0 ? u[a] : neg(u[a]);
+            started = true;
+        } else {
+            t = c[a] > 0 ? add2(t, u[a]) : sub2(t, u[a]);
+        }
+    }
+    return t;
+}
+
+// Shifted BGK on V = float (one cell) or float2 (a cell pair): g -> g' in place.
+template <int Q, typename V>
+__device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
+{
+    using L = Lattice<Q>;
+    V drho = g[0];
+#pragma unroll
+    for (int q = 1; q < Q; q++) drho = add2(drho, g[q]);
+    V    jp[3] = {splat<V>(0.f), splat<V>(0.f), splat<V>(0.f)}, jm[3] = {splat<V>(0.f), splat<V>(0.f), splat<V>(0.f)};
+    bool sp[3] = {false, false, false}, sm[3] = {false, false, false};
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int c[3] = {L::cx(q), L::cy(q), L::cz(q)};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (c[a] > 0) {
+                jp[a] = sp[a] ? add2(jp[a], g[q]) : g[q];
+                sp[a] = true;
+            } else if (c[a] < 0) {
+                jm[a] = sm[a] ? add2(jm[a], g[q]) : g[q];
+                sm[a] = true;
+            }
+        }
+    }
+    const V jx = sub2(jp[0], jm[0]), jy = sub2(jp[1], jm[1]), jz = sub2(jp[2], jm[2]);
+    const V rho = add2(splat<V>(1.f), drho);
+    const V inv = recip(rho);
+    const V ux = mul2(jx, inv), uy = mul2(jy, inv), uz = mul2(jz, inv);
+    const V usq = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
+    const V rus = mul2(rho, mul2(splat<V>(1.5f), usq));
+    const V base = sub2(drho, rus);
+    const V u3x = mul2(splat<V>(3.f), ux), u3y = mul2(splat<V>(3.f), uy), u3z = mul2(splat<V>(3.f), uz);
+    V       wr[WeightClass<Q>::n], wb[WeightClass<Q>::n];
+#pragma unroll
+    for (int k = 0; k < WeightClass<Q>::n; k++) {
+        const float wk = float(WeightClass<Q>::w(k));
+        wr[k] = mul2(splat<V>(wk), rho);
+        wb[k] = mul2(splat<V>(wk), base);
+    }
+    const V om = splat<V>(omega);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int k = WeightClass<Q>::of(q);
+        const V   t = cdot<Q, V>(q, u3x, u3y, u3z);
+        const V   a = fma2(mul2(splat<V>(0.5f), t), t, t);
+        const V   eqg = fma2(wr[k], a, wb[k]);
+        g[q] = fma2(om, sub2(eqg, g[q]), g[q]);
+    }
+}
+
+template <int Q, typename S>
+__global__ void __launch_bounds__(kPairX* kPairY, (Q == 19 ? 4 : 3)) lbm_dense_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                       const uint32_t* __restrict__ flags, DenseParams<float> p)
+{
+    using L = Lattice<Q>;
+    using IO = PairIO<S>;
+    const int x0 = 2 * (blockIdx.x * kPairX + threadIdx.x);
+    const int y = blockIdx.y * kPairY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x0 >= p.nx || y >= p.ny) return;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    const int64_t cell0 = x0 + sy * y + sz * z;
+
+    uint32_t  m0, l0, m1, l1;
+    const int c0 = cell_setup<Q>(p, flags, x0, y, z, cell0, m0, l0);
+    const int c1 = cell_setup<Q>(p, flags, x0 + 1, y, z, cell0 + 1, m1, l1);
+    const bool b0 = c0 == NGB_CELL_BULK, b1 = c1 == NGB_CELL_BULK;
+    if (c0 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell0, x0);
+    if (c1 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell0 + 1, x0 + 1);
+    if (!b0 && !b1) return;
+
+    float2 g[Q];
+    if (b0 && b1 && (m0 | m1) == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int     cx = L::cx(q);
+            const int64_t row = cell0 - L::cy(q) * sy - L::cz(q) * sz;  // source row, x = x0
+            const S*      base = fin + q * stride + row;
+            typename IO::Word v;
+            if (cx == 0) {
+                v = IO::load(base);
+            } else if (cx > 0) {  // source x0-1, x0
+                v = IO::mid(IO::load(base - 2), IO::load(base));
+            } else {  // source x0+1, x0+2
+                v = IO::mid(IO::load(base), IO::load(base + 2));
+            }
+            g[q] = IO::to_g(v, float(L::w(q)));
+        }
+    } else {
+        float ga[Q], gb[Q];
+        if (b0) pull_one<Q, S>(fin, stride, cell0, sy, sz, m0, l0, p, ga);
+        if (b1) pull_one<Q, S>(fin, stride, cell0 + 1, sy, sz, m1, l1, p, gb);
+#pragma unroll
+        for (int q = 0; q < Q; q++) g[q] = make_float2(b0 ? ga[q] : 0.f, b1 ? gb[q] : 0.f);
+    }
+
+    bgk_shifted<Q, float2>(g, p.omega);
+
+    // ---- store
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        S*          dst = fout + q * stride + cell0;
+        const float w = float(L::w(q));
+        if (b0 && b1) {
+            IO::store(dst, g[q], w);
+        } else {
+            if (b0) IO::store1(dst, g[q].x, w);
+            if (b1) IO::store1(dst + 1, g[q].y, w);
+        }
+    }
+}
+
+// One cell per thread (odd nx or unaligned buffers): same arithmetic as the pair kernel.
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                     const uint32_t* __restrict__ flags, DenseParams<float> p)
+{
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    const int64_t cell = x + sy * y + sz * z;
+    uint32_t      mask, lidbits;
+    const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
+    if (cls == NGB_CELL_OUTLET) {
+        outlet_copy<Q>(fin, fout, stride, cell, x);
+        return;
+    }
+    if (cls != NGB_CELL_BULK) return;
+    float g[Q];
+    pull_one<Q, S>(fin, stride, cell, sy, sz, mask, lidbits, p, g);
+    bgk_shifted<Q, float>(g, p.omega);
+#pragma unroll
+    for (int q = 0; q < Q; q++) PairIO<S>::store1(fout + q * stride + cell, g[q], float(L::w(q)));
+}
+
+}  // namespace ngb

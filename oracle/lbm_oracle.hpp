@@ -351,24 +351,27 @@ void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Loa
             }
 }
 
-// ---------------------------------------------------------------- shifted FP32 BGK (offset storage)
-// The project's equilibrium-offset form (no reference counterpart): storage
-// holds g_q = f_q - w_q; in FP32
-//   drho = sum g, j = sum c g, rho = 1 + drho, u = j * (1/rho),
-//   usqr = 1.5 |u|^2, eqg_q = w_q (drho + rho (3 cu + 4.5 cu^2 - usqr)),
-//   g' = g + omega (eqg - g).
+// ---------------------------------------------------------------- shifted FP32 BGK
+// The project's equilibrium-shifted FP32 form (used for FP32 storage and for
+// the FP16/BF16 offset storage; no reference counterpart). Storage holds
+// f_q (FP32) or g_q = f_q - w_q (16-bit). Every operation is IEEE single
+// precision in this exact order, fused multiply-adds written as std::fmaf:
+//   drho = g_0 + g_1 + ... + g_{Q-1};  j_a = (sum_{c_a>0} g) - (sum_{c_a<0} g), q ascending
+//   rho = 1 + drho; inv = 1 / rho; u_a = j_a * inv
+//   usq = fma(uz, uz, fma(uy, uy, ux * ux)); rus = rho * (1.5 * usq); base = drho - rus
+//   u3_a = 3 * u_a; per weight w: wr = w * rho, wb = w * base
+//   per q: t = c_q . u3 (signed adds in x, y, z order); a = fma(0.5 * t, t, t)
+//          eqg = fma(wr, a, wb); g' = fma(omega, eqg - g, g)
 // Wall rule as the reference step: bit q set -> g(x, opp q) + wall term.
 template <int Q, typename LoadG, typename StoreG, typename WallTerm>
 void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega, LoadG loadg, StoreG storeg, WallTerm wall,
                       int z_begin = 0, int z_end = -1)
 {
     if (z_end < 0) z_end = nz;
-    int   cx[Q], cy[Q], cz[Q], op[Q];
+    int   c[Q][3], op[Q];
     float w[Q];
     for (int q = 0; q < Q; q++) {
-        cx[q] = Q == 19 ? kC19[q][0] : c27(q, 0);
-        cy[q] = Q == 19 ? kC19[q][1] : c27(q, 1);
-        cz[q] = Q == 19 ? kC19[q][2] : c27(q, 2);
+        for (int a = 0; a < 3; a++) c[q][a] = Q == 19 ? kC19[q][a] : c27(q, a);
         op[q] = Q == 19 ? opp19(q) : opp27(q);
         w[q] = float(Q == 19 ? kW19[q] : w27(q));
     }
@@ -379,7 +382,7 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
                 if (cell.classification != bulk) continue;
                 float g[Q];
                 for (int q = 0; q < Q; q++) {
-                    const int sx = x - cx[q], sy = y - cy[q], sz = z - cz[q];
+                    const int sx = x - c[q][0], sy = y - c[q][1], sz = z - c[q][2];
                     if (cell.wallNghBitflag & (uint32_t(1) << q)) {
                         int cls = undefined;
                         if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = flag[lin(sx, sy, sz, nx, ny)].classification;
@@ -388,24 +391,44 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
                         g[q] = loadg(sx, sy, sz, q);
                     }
                 }
-                float drho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
-                for (int q = 0; q < Q; q++) {
-                    drho += g[q];
-                    if (cx[q] > 0) jx += g[q];
-                    if (cx[q] < 0) jx -= g[q];
-                    if (cy[q] > 0) jy += g[q];
-                    if (cy[q] < 0) jy -= g[q];
-                    if (cz[q] > 0) jz += g[q];
-                    if (cz[q] < 0) jz -= g[q];
-                }
+                float drho = g[0];
+                for (int q = 1; q < Q; q++) drho = drho + g[q];
+                float jp[3] = {0, 0, 0}, jm[3] = {0, 0, 0};
+                bool  sp[3] = {false, false, false}, sm[3] = {false, false, false};
+                for (int q = 0; q < Q; q++)
+                    for (int a = 0; a < 3; a++) {
+                        if (c[q][a] > 0) {
+                            jp[a] = sp[a] ? jp[a] + g[q] : g[q];
+                            sp[a] = true;
+                        } else if (c[q][a] < 0) {
+                            jm[a] = sm[a] ? jm[a] + g[q] : g[q];
+                            sm[a] = true;
+                        }
+                    }
+                const float jx = jp[0] - jm[0], jy = jp[1] - jm[1], jz = jp[2] - jm[2];
                 const float rho = 1.f + drho;
                 const float inv = 1.f / rho;
                 const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-                const float usqr = 1.5f * (ux * ux + uy * uy + uz * uz);
+                const float usq = std::fmaf(uz, uz, std::fmaf(uy, uy, ux * ux));
+                const float rus = rho * (1.5f * usq);
+                const float base = drho - rus;
+                const float u3[3] = {3.f * ux, 3.f * uy, 3.f * uz};
                 for (int q = 0; q < Q; q++) {
-                    const float cu = float(cx[q]) * ux + float(cy[q]) * uy + float(cz[q]) * uz;
-                    const float eqg = w[q] * (drho + rho * (3.f * cu + 4.5f * cu * cu - usqr));
-                    storeg(x, y, z, q, g[q] + omega * (eqg - g[q]));
+                    const float wr = w[q] * rho, wb = w[q] * base;
+                    float       t = 0.f;
+                    bool        started = false;
+                    for (int a = 0; a < 3; a++) {
+                        if (c[q][a] == 0) continue;
+                        if (!started) {
+                            t = c[q][a] > 0 ? u3[a] : -u3[a];
+                            started = true;
+                        } else {
+                            t = c[q][a] > 0 ? t + u3[a] : t - u3[a];
+                        }
+                    }
+                    const float a = std::fmaf(0.5f * t, t, t);
+                    const float eqg = std::fmaf(wr, a, wb);
+                    storeg(x, y, z, q, std::fmaf(omega, eqg - g[q], g[q]));
                 }
             }
 }

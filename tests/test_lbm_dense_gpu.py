@@ -115,8 +115,9 @@ def test_offset_storage_velocity(ngb, orc, cuda, q, storage, tol_vs_f64):
 @pytest.mark.parametrize("storage", [1, 2, 3])
 def test_single_step_from_developed_state(ngb, orc, cuda, q, storage):
     """One step from the same developed state (FP64 run, 150 steps, converted
-    to the storage form): GPU and oracle agree value by value up to one unit
-    of the storage format (FMA contraction may flip a last-bit rounding)."""
+    to the storage form): the GPU's FP32 shifted-form arithmetic is an explicit
+    IEEE operation sequence that the oracle mirrors with std::fmaf, so every
+    stored value is bit-identical."""
     import torch
     n = 20
     V = n ** 3
@@ -125,38 +126,40 @@ def test_single_step_from_developed_state(ngb, orc, cuda, q, storage):
     f = pop64.reshape(q, V)
     if storage == 1:
         src = f.astype(np.float32).ravel()
-        tsrc = torch.from_numpy(src)
+        tsrc = torch.from_numpy(src.copy())
     else:
         g = (f.astype(np.float32) - w[:, None].astype(np.float32))
         tsrc = torch.from_numpy(g.ravel()).to(torch.float16 if storage == 2 else torch.bfloat16)
         src = tsrc.view(torch.int16).numpy().view(np.uint16).copy()
-    # oracle: one shifted-form step
     a = src.copy()
     b = src.copy()
     from helpers import wall_table
     wt = wall_table(q, 0.1, storage)
     assert orc.orc_lbm_run(n, n, n, q, storage, 2, 1, omega, P(wt), P(oflags), P(a), P(b), 1, 0) == 0
-    # GPU
     desc = ngb.lbm_dense_desc(n, n, n, q, storage, omega, ngb.lid_wall_terms(q, 0.1))
     fa = tsrc.to(cuda)
     fb = fa.clone()
     ngb.lbm_dense_step(desc, fa, fb)
     torch.cuda.synchronize()
-    if storage == 1:
-        got = fb.cpu().numpy()
-        # values are f = w + g'; FMA contraction changes g' in its last bits,
-        # so allow a few units of the smallest population weight's spacing
-        ulp = np.spacing(np.maximum(np.abs(b), np.float32(w.min())).astype(np.float32))
-        assert np.all(np.abs(got - b) <= 4 * ulp), float((np.abs(got - b) / ulp).max())
-    else:
-        got_bits = fb.cpu().view(torch.int16).numpy().view(np.uint16)
-        tdt = torch.float16 if storage == 2 else torch.bfloat16
-        got = fb.cpu().float().numpy()
-        ref = torch.from_numpy(b.view(np.int16).copy()).view(tdt).float().numpy()
-        mant = 10 if storage == 2 else 7
-        ulp = np.maximum(np.maximum(np.abs(got), np.abs(ref)), 2.0 ** -14) * 2.0 ** -mant
-        assert np.all(np.abs(got - ref) <= 1.01 * ulp)
-        assert (got_bits == b).mean() > 0.99
+    got = fb.cpu()
+    got = got.numpy() if storage == 1 else got.view(torch.int16).numpy().view(np.uint16)
+    assert np.array_equal(got.view(np.uint32) if storage == 1 else got, b.view(np.uint32) if storage == 1 else b)
+
+
+@pytest.mark.parametrize("n", [18, 17])
+@pytest.mark.parametrize("q", [19, 27])
+@pytest.mark.parametrize("storage", [1, 2, 3])
+def test_shifted_forms_bit_exact_over_steps(ngb, orc, cuda, n, q, storage):
+    """60 steps from the equilibrium start, even n (two cells per thread) and
+    odd n (one cell per thread): bit-identical to the oracle's shifted form."""
+    steps = 60
+    _, out, _ = gpu_cavity(ngb, cuda, n, q, storage, steps)
+    ref, _, _ = oracle_cavity(orc, n, q, storage, steps, mode=2, compute_float=1)
+    import torch
+    got = out.cpu()
+    got = got.numpy().view(np.uint32) if storage == 1 else got.view(torch.int16).numpy().view(np.uint16)
+    ref = ref.view(np.uint32) if storage == 1 else ref
+    assert np.array_equal(got, ref), int((got != ref).sum())
 
 
 @pytest.mark.parametrize("storage", [0, 1, 2])
