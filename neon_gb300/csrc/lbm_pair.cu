@@ -1,6 +1,7 @@
 // Instantiations of the two-cells-per-thread dense LBM kernel. Compiled with
 // --fmad=false: the kernel writes every fused multiply-add explicitly.
 #include "lbm_pair.cuh"
+#include <cstdlib>
 
 namespace ngb {
 
@@ -38,8 +39,16 @@ int launch_lbm_dense_pair(int Q, int storage, const void* fin, void* fout, const
 int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
                          cudaStream_t s)
 {
-    int rc = launch_lbm_dense_pair(Q, storage, fin, fout, flags, p, s);
-    if (rc != NGB_ERR_UNSUPPORTED) return rc;
+    // Kernel shape: one cell per thread (default) or two (NGB_LBM_PAIR=1, tuning only;
+    // both run the same IEEE operation sequence).
+    static const bool use_pair = [] {
+        const char* e = getenv("NGB_LBM_PAIR");
+        return e && e[0] == '1';
+    }();
+    if (use_pair) {
+        int rc = launch_lbm_dense_pair(Q, storage, fin, fout, flags, p, s);
+        if (rc != NGB_ERR_UNSUPPORTED) return rc;
+    }
     const dim3 grid((p.nx + kLbmBlockX - 1) / kLbmBlockX, p.ny, p.nz), block(kLbmBlockX);
 #define NGB_ONE(QQ, T) \
     lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)

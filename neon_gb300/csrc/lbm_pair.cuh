@@ -97,21 +97,32 @@ struct PairIO<__nv_bfloat16> {
     __device__ __forceinline__ static void store1(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
 };
 
-// Scalar pull of one cell's populations as g (wall rule included).
+// Scalar pull of one cell's populations as g (wall rule included). Addresses
+// are the cell's own pointer plus a per-direction offset that depends only on
+// kernel parameters (warp-uniform), so each load costs one address add.
 template <int Q, typename S>
 __device__ __forceinline__ void pull_one(const S* __restrict__ fin, int64_t stride, int64_t cell, int64_t sy, int64_t sz,
                                          uint32_t mask, uint32_t lidbits, const DenseParams<float>& p, float* g)
 {
     using L = Lattice<Q>;
+    const S* P = fin + cell;
+    if (mask == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int64_t off = q * stride - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            g[q] = PairIO<S>::to_g1(__ldg(P + off), float(L::w(q)));
+        }
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         if (mask & (1u << q)) {
             const int   o = L::opp(q);
             const float wt = (lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o];
-            g[q] = PairIO<S>::to_g1(__ldg(fin + o * stride + cell), float(L::w(o))) + wt;
+            g[q] = PairIO<S>::to_g1(__ldg(P + o * stride), float(L::w(o))) + wt;
         } else {
-            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-            g[q] = PairIO<S>::to_g1(__ldg(fin + q * stride + src), float(L::w(q)));
+            const int64_t off = q * stride - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            g[q] = PairIO<S>::to_g1(__ldg(P + off), float(L::w(q)));
         }
     }
 }
@@ -292,8 +303,9 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* _
     float g[Q];
     pull_one<Q, S>(fin, stride, cell, sy, sz, mask, lidbits, p, g);
     bgk_shifted<Q, float>(g, p.omega);
+    S* D = fout + cell;
 #pragma unroll
-    for (int q = 0; q < Q; q++) PairIO<S>::store1(fout + q * stride + cell, g[q], float(L::w(q)));
+    for (int q = 0; q < Q; q++) PairIO<S>::store1(D + q * stride, g[q], float(L::w(q)));
 }
 
 }  // namespace ngb
