@@ -39,15 +39,36 @@ int launch_lbm_dense_pair(int Q, int storage, const void* fin, void* fout, const
 int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
                          cudaStream_t s)
 {
-    // Kernel shape: one cell per thread (default) or two (NGB_LBM_PAIR=1, tuning only;
-    // both run the same IEEE operation sequence).
-    static const bool use_pair = [] {
-        const char* e = getenv("NGB_LBM_PAIR");
-        return e && e[0] == '1';
+    // Kernel shape (all run the same IEEE operation sequence per cell):
+    // NGB_LBM_VARIANT = 0 one cell per thread, 1 two cells along x, 2 two cells along z.
+    static const int variant = [] {
+        const char* e = getenv("NGB_LBM_VARIANT");
+        return e ? atoi(e) : 0;
     }();
-    if (use_pair) {
+    if (variant == 1) {
         int rc = launch_lbm_dense_pair(Q, storage, fin, fout, flags, p, s);
         if (rc != NGB_ERR_UNSUPPORTED) return rc;
+    }
+    if (variant == 2) {
+        const dim3 g2((p.nx + kLbmBlockX - 1) / kLbmBlockX, p.ny, (p.nz + 1) / 2), b2(kLbmBlockX);
+#define NGB_ZP(QQ, T) \
+    lbm_dense_zpair_kernel<QQ, T><<<g2, b2, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)
+        const bool q19z = Q == 19;
+        switch (storage) {
+            case NGB_STORE_F32:
+                if (q19z) NGB_ZP(19, float); else NGB_ZP(27, float);
+                break;
+            case NGB_STORE_F16OFF:
+                if (q19z) NGB_ZP(19, __half); else NGB_ZP(27, __half);
+                break;
+            case NGB_STORE_BF16OFF:
+                if (q19z) NGB_ZP(19, __nv_bfloat16); else NGB_ZP(27, __nv_bfloat16);
+                break;
+            default: set_error("unsupported storage %d", storage); return NGB_ERR_UNSUPPORTED;
+        }
+#undef NGB_ZP
+        NGB_LAUNCH_CHECK("lbm_dense_zpair_kernel");
+        return NGB_OK;
     }
     const dim3 grid((p.nx + kLbmBlockX - 1) / kLbmBlockX, p.ny, p.nz), block(kLbmBlockX);
 #define NGB_ONE(QQ, T) \

@@ -282,6 +282,66 @@ __global__ void __launch_bounds__(kPairX* kPairY, (Q == 19 ? 4 : 3)) lbm_dense_p
     }
 }
 
+// Two cells per thread stacked in z, (x, y, z0) and (x, y, z0+1): every load is
+// a plain per-cell load (no x realignment), the two cells' populations are
+// packed lane-wise into float2 and collided with the packed FP32x2 math.
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_zpair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                    const uint32_t* __restrict__ flags, DenseParams<float> p)
+{
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    const int y = blockIdx.y, z0 = 2 * blockIdx.z;
+    if (x >= p.nx) return;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    const int64_t cell0 = x + sy * y + sz * z0, cell1 = cell0 + sz;
+    const bool    has1 = z0 + 1 < p.nz;
+    uint32_t      m0, l0, m1 = 0, l1 = 0;
+    const int     c0 = cell_setup<Q>(p, flags, x, y, z0, cell0, m0, l0);
+    const int     c1 = has1 ? cell_setup<Q>(p, flags, x, y, z0 + 1, cell1, m1, l1) : NGB_CELL_UNDEFINED;
+    if (c0 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell0, x);
+    if (c1 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell1, x);
+    const bool b0 = c0 == NGB_CELL_BULK, b1 = c1 == NGB_CELL_BULK;
+    if (!b0 && !b1) return;
+    float2 g[Q];
+    if (b0 && b1 && (m0 | m1) == 0) {
+        const S* P0 = fin + cell0;
+        const S* P1 = fin + cell1;
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int64_t off = q * stride - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            g[q] = make_float2(PairIO<S>::to_g1(__ldg(P0 + off), float(L::w(q))), PairIO<S>::to_g1(__ldg(P1 + off), float(L::w(q))));
+        }
+    } else {
+        float t[Q];
+        if (b0) {
+            pull_one<Q, S>(fin, stride, cell0, sy, sz, m0, l0, p, t);
+#pragma unroll
+            for (int q = 0; q < Q; q++) g[q].x = t[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q; q++) g[q].x = 0.f;
+        }
+        if (b1) {
+            pull_one<Q, S>(fin, stride, cell1, sy, sz, m1, l1, p, t);
+#pragma unroll
+            for (int q = 0; q < Q; q++) g[q].y = t[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q; q++) g[q].y = 0.f;
+        }
+    }
+    bgk_shifted<Q, float2>(g, p.omega);
+    S* D0 = fout + cell0;
+    S* D1 = fout + cell1;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const float w = float(L::w(q));
+        if (b0) PairIO<S>::store1(D0 + q * stride, g[q].x, w);
+        if (b1) PairIO<S>::store1(D1 + q * stride, g[q].y, w);
+    }
+}
+
 // One cell per thread (odd nx or unaligned buffers): same arithmetic as the pair kernel.
 template <int Q, typename S>
 __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* __restrict__ fin, S* __restrict__ fout,
