@@ -123,6 +123,106 @@ int ngb_lbm_cavity_init(const ngb_lbm_dense_desc* desc, double ulb, void* fa, vo
 int ngb_lbm_dense_macroscopic(const ngb_lbm_dense_desc* desc, const void* fin, const uint32_t* flags, double* rho,
                               double* u, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Block-sparse grid (bGrid, 8x8x8 blocks), single partition
+ * ---------------------------------------------------------------------- */
+
+/* Candidate blocks per axis: ceil(n / 8). */
+#define NGB_BGRID_BLOCKS(n) (((n) + 7) / 8)
+#define NGB_BGRID_NO_BLOCK 0xffffffffu
+
+/* Phase 1 of the bGrid construction on the device. `active` is a dense
+ * nx*ny*nz byte map (x fastest, non-zero = active voxel). Fills
+ * block_of[bnx*bny*bnz] (x fastest) with the data-block index of every
+ * candidate block, or -1 when none of its voxels is inside the domain and
+ * active, and writes the number of data blocks to *n_blocks (device) .
+ * Data-block order is the single-partition order of Neon: z, then y, then x
+ * fastest over candidate blocks (SpanDecomposition.h:71-96,
+ * SpanClassifier.h:228-237, SpanClassifier.cpp:7-20). */
+int ngb_bgrid_count(int32_t nx, int32_t ny, int32_t nz, const uint8_t* active, int32_t* block_of, uint32_t* n_blocks,
+                    void* stream);
+
+/* Phase 2: per data block, origin (3 x int32: block index * 8,
+ * Partitioner1D.h:212-255), active bitmask (16 x uint32, bit x + 8y + 64z,
+ * bGrid_imp.h:80-136 / StaticBlock.h:79-98) and 27-entry connectivity
+ * (entry i + 3j + 9k = data block at offset (i-1, j-1, k-1) or
+ * NGB_BGRID_NO_BLOCK, bGrid_imp.h:139-172). n_active_voxels (device,
+ * uint64) receives the active-voxel count. Arrays hold n_blocks entries. */
+int ngb_bgrid_fill(int32_t nx, int32_t ny, int32_t nz, const uint8_t* active, const int32_t* block_of, int32_t* origin,
+                   uint32_t* mask, uint32_t* conn, unsigned long long* n_active_voxels, void* stream);
+
+/* Block-sparse lattice. Population (block b, voxel i + 8j + 64k, q) lives
+ * at ((b*q + q)*512 + i + 8j + 64k) — per-block SoA as a Neon bField
+ * (bPartition_imp.h:95-107). A neighbour that is outside every data block or
+ * not active counts as a non-fluid node ("undefined"), as bPartition's
+ * invalid NghData does (bPartition_imp.h:109-124). */
+typedef struct ngb_bgrid_desc {
+    int32_t         n_blocks;
+    int32_t         q;       /* 19 or 27 */
+    int32_t         storage; /* ngb_storage */
+    int32_t         pad;
+    double          omega;
+    double          wall_term[2][27]; /* as ngb_lbm_dense_desc */
+    const int32_t*  origin;           /* device arrays from ngb_bgrid_fill */
+    const uint32_t* mask;
+    const uint32_t* conn;
+} ngb_bgrid_desc;
+
+/* Wall-neighbour mask of every bulk voxel of a bGrid flag field (uint32 per
+ * voxel, per-block layout b*512 + i + 8j + 64k), in place; classifications
+ * are kept. Same rule as ngb_lbm_wall_mask with bGrid neighbour resolution. */
+int ngb_bgrid_wall_mask(const ngb_bgrid_desc* desc, uint32_t* flags, void* stream);
+
+/* One pull stream-collide step on a bGrid: replaces LbmContainers::iteration
+ * on Neon::bGrid (LbmTools.h:284-325 run through blockSpan::launchLambdaOnSpanCUDA,
+ * LambdaExecutor.h:103-115). Same arithmetic as ngb_lbm_dense_step. */
+int ngb_bgrid_lbm_step(const ngb_bgrid_desc* desc, const void* fin, void* fout, const uint32_t* flags, void* stream);
+
+/* Momentum-exchange force (3 doubles, device) on every bounce-back node, from
+ * the populations `fin` that the next step reads: F = sum over bulk voxels x
+ * and directions q whose pull source x - c_q is a bounce-back node of
+ * 2 c_{opp q} f_{opp q}(x). New (the reference computes no drag).
+ * Deterministic: fixed per-block partials reduced in block order; `partials`
+ * is caller scratch of 3 * n_blocks doubles. */
+int ngb_bgrid_drag(const ngb_bgrid_desc* desc, const void* fin, const uint32_t* flags, double* partials, double* force,
+                   void* stream);
+
+/* Geometry of the flow-over-sphere case on a dense byte map: voxel active
+ * iff within `band` of the sphere surface (or inside it) or within
+ * `tube_band` of a tube of radius `tube_r` whose axis runs along x through
+ * control points every `ctrl_dx` voxels at (y, z) = tube_c + amplitude *
+ * (2u - 1), u from std::mt19937_64(seed) (53-bit uniforms, y then z per
+ * point), linearly interpolated. Classes (uint8 per voxel): bounce-back
+ * inside the sphere, moving wall (inlet) at x = 0, outlet at x = nx-1, bulk
+ * otherwise; inactive voxels get NGB_CELL_UNDEFINED. */
+typedef struct ngb_sphere_tube {
+    int32_t  nx, ny, nz;
+    int32_t  ctrl_dx;
+    double   sphere_c[3];
+    double   sphere_r;
+    double   band;
+    double   tube_c[2];
+    double   tube_r;
+    double   tube_band;
+    double   amplitude;
+    uint64_t seed;
+} ngb_sphere_tube;
+int ngb_geometry_sphere_tube(const ngb_sphere_tube* g, uint8_t* active, uint8_t* cls, void* stream);
+
+/* Scatter a dense per-voxel uint8 class map into a bGrid flag field
+ * (classification only, mask 0): flags[b*512 + v] = class of the voxel. */
+int ngb_bgrid_flags_from_dense(const ngb_bgrid_desc* desc, int32_t nx, int32_t ny, int32_t nz, const uint8_t* cls,
+                               uint32_t* flags, void* stream);
+
+/* Integer 6-neighbour operator of Neon's domain-stencil tests on a bGrid
+ * (TestData::laplace, TestData.h:412-443, through bPartition::getNghData):
+ * b = a - count * sum of valid neighbours, int64, cardinality 1. */
+int ngb_bgrid_laplace_i64(const ngb_bgrid_desc* desc, const int64_t* a, int64_t* b, void* stream);
+
+/* Same operator on a dense single-partition dGrid (validity = inside the box,
+ * dPartition.h:228-263). */
+int ngb_dense_laplace_i64(int32_t nx, int32_t ny, int32_t nz, const int64_t* a, int64_t* b, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -68,8 +68,33 @@ def _declare(L):
             fn.restype = args[1]
 
 
-# Signatures registered by the sub-modules (bgrid, poisson, ...).
-_EXTRA_SIGNATURES = {}
+class BGridDesc(ctypes.Structure):
+    _fields_ = [("n_blocks", ctypes.c_int32), ("q", ctypes.c_int32), ("storage", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("omega", ctypes.c_double), ("wall_term", (ctypes.c_double * 27) * 2),
+                ("origin", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("conn", ctypes.c_void_p)]
+
+
+class SphereTube(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("ctrl_dx", ctypes.c_int32),
+                ("sphere_c", ctypes.c_double * 3), ("sphere_r", ctypes.c_double), ("band", ctypes.c_double),
+                ("tube_c", ctypes.c_double * 2), ("tube_r", ctypes.c_double), ("tube_band", ctypes.c_double),
+                ("amplitude", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+_vp, _i32, _dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_double
+_bd = ctypes.POINTER(BGridDesc)
+# Signatures of the entry points beyond the dense LBM ones: name -> (argtypes, restype).
+_EXTRA_SIGNATURES = {
+    "ngb_bgrid_count": ([_i32, _i32, _i32, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_bgrid_fill": ([_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_bgrid_wall_mask": ([_bd, _vp, _vp], ctypes.c_int),
+    "ngb_bgrid_lbm_step": ([_bd, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_bgrid_drag": ([_bd, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_geometry_sphere_tube": ([ctypes.POINTER(SphereTube), _vp, _vp, _vp], ctypes.c_int),
+    "ngb_bgrid_flags_from_dense": ([_bd, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_bgrid_laplace_i64": ([_bd, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_dense_laplace_i64": ([_i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+}
 
 
 def check(rc):
@@ -165,3 +190,90 @@ def lbm_cavity_init(desc, ulb, fa, fb=None, flags=None, stream=None):
 def lbm_dense_macroscopic(desc, fin, rho=None, u=None, flags=None, stream=None):
     return check(lib().ngb_lbm_dense_macroscopic(ctypes.byref(desc), _ptr(fin), _ptr(flags), _ptr(rho), _ptr(u),
                                                  _stream(stream)))
+
+
+# ----------------------------------------------------------------------------- bGrid
+class BGrid:
+    """A block-sparse grid (8^3 blocks) built on the device from a dense byte
+    activity map (torch uint8 tensor on cuda, nx*ny*nz, x fastest).
+    Mirrors Neon::bGrid's construction (bGrid_imp.h:19-246) for one partition."""
+
+    def __init__(self, nx, ny, nz, active, stream=None):
+        import torch
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.bnx, self.bny, self.bnz = (nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8
+        dev = active.device
+        self.block_of = torch.empty(self.bnx * self.bny * self.bnz, dtype=torch.int32, device=dev)
+        nb = torch.zeros(1, dtype=torch.int32, device=dev)
+        check(lib().ngb_bgrid_count(nx, ny, nz, _ptr(active), _ptr(self.block_of), _ptr(nb), _stream(stream)))
+        self.n_blocks = int(nb.item())
+        n = max(self.n_blocks, 1)
+        self.origin = torch.empty(3 * n, dtype=torch.int32, device=dev)
+        self.mask = torch.empty(16 * n, dtype=torch.int32, device=dev)
+        self.conn = torch.empty(27 * n, dtype=torch.int32, device=dev)
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+        check(lib().ngb_bgrid_fill(nx, ny, nz, _ptr(active), _ptr(self.block_of), _ptr(self.origin), _ptr(self.mask),
+                                   _ptr(self.conn), _ptr(cnt), _stream(stream)))
+        self.n_active_voxels = int(cnt.item())
+
+    def desc(self, q=19, storage="f32", omega=1.0, moving_wall_terms=None, bounce_back_terms=None):
+        d = BGridDesc()
+        d.n_blocks, d.q = self.n_blocks, q
+        d.storage = STORAGE_NAMES[storage] if isinstance(storage, str) else storage
+        d.omega = omega
+        for k in range(27):
+            d.wall_term[0][k] = bounce_back_terms[k] if bounce_back_terms and k < len(bounce_back_terms) else 0.0
+            d.wall_term[1][k] = moving_wall_terms[k] if moving_wall_terms and k < len(moving_wall_terms) else 0.0
+        d.origin, d.mask, d.conn = self.origin.data_ptr(), self.mask.data_ptr(), self.conn.data_ptr()
+        return d
+
+
+def bgrid_wall_mask(desc, flags, stream=None):
+    return check(lib().ngb_bgrid_wall_mask(ctypes.byref(desc), _ptr(flags), _stream(stream)))
+
+
+def bgrid_lbm_step(desc, fin, fout, flags, stream=None):
+    return check(lib().ngb_bgrid_lbm_step(ctypes.byref(desc), _ptr(fin), _ptr(fout), _ptr(flags), _stream(stream)))
+
+
+def bgrid_drag(desc, fin, flags, partials, force, stream=None):
+    return check(lib().ngb_bgrid_drag(ctypes.byref(desc), _ptr(fin), _ptr(flags), _ptr(partials), _ptr(force),
+                                      _stream(stream)))
+
+
+def bgrid_flags_from_dense(desc, nx, ny, nz, cls, flags, stream=None):
+    return check(lib().ngb_bgrid_flags_from_dense(ctypes.byref(desc), nx, ny, nz, _ptr(cls), _ptr(flags),
+                                                  _stream(stream)))
+
+
+def bgrid_laplace_i64(desc, a, b, stream=None):
+    return check(lib().ngb_bgrid_laplace_i64(ctypes.byref(desc), _ptr(a), _ptr(b), _stream(stream)))
+
+
+def dense_laplace_i64(nx, ny, nz, a, b, stream=None):
+    return check(lib().ngb_dense_laplace_i64(nx, ny, nz, _ptr(a), _ptr(b), _stream(stream)))
+
+
+def sphere_tube(nx, ny, nz, sphere_c, sphere_r, band, tube_c, tube_r, tube_band, amplitude, ctrl_dx, seed):
+    g = SphereTube()
+    g.nx, g.ny, g.nz, g.ctrl_dx = nx, ny, nz, ctrl_dx
+    for a in range(3):
+        g.sphere_c[a] = sphere_c[a]
+    g.sphere_r, g.band = sphere_r, band
+    g.tube_c[0], g.tube_c[1] = tube_c
+    g.tube_r, g.tube_band, g.amplitude, g.seed = tube_r, tube_band, amplitude, seed
+    return g
+
+
+def geometry_sphere_tube(g, active, cls, stream=None):
+    return check(lib().ngb_geometry_sphere_tube(ctypes.byref(g), _ptr(active), _ptr(cls), _stream(stream)))
+
+
+def sphere_config(scale=1):
+    """The flow-over-sphere case, 512x256x256 box at scale 1 (sizes divided by
+    `scale`): sphere r = 32 at (128,128,128); active within 48 voxels of the
+    sphere surface or of a radius-40 tube along x whose axis wanders +-24
+    voxels through control points every 64 voxels (seed 2024)."""
+    s = scale
+    return sphere_tube(512 // s, 256 // s, 256 // s, (128 / s, 128 / s, 128 / s), 32 / s, 48 / s, (128 / s, 128 / s),
+                       40 / s, 48 / s, 24 / s, max(1, 64 // s), 2024)

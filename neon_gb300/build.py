@@ -19,10 +19,11 @@ LIB_NAME = "libneon_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "--expt-relaxed-constexpr",
           "-I", INCLUDE, "-I", CSRC]
 # FP64 reference-arithmetic units: no contraction into FMA.
-NO_FMAD = {"lbm_dense_f64.cu", "lbm_pair.cu", "bgrid_lbm_f64.cu", "poisson_f64.cu"}
+NO_FMAD = {"lbm_dense_f64.cu", "lbm_shifted.cu", "bgrid_lbm.cu", "poisson_f64.cu"}
 
 
 def nvcc():

@@ -1,0 +1,344 @@
+// bGrid LBM step, momentum-exchange drag and the flow-over-sphere geometry.
+// Compiled with --fmad=false (the FP32 step shares the explicit IEEE
+// sequence of the dense kernel; FP64 keeps the reference operation order).
+#include "bgrid.cuh"
+#include "lbm_shifted.cuh"
+#include <random>
+#include <vector>
+
+namespace ngb {
+namespace {
+
+template <typename C>
+struct BParams {
+    C               omega;
+    C               wall[2][27];
+    const uint32_t* mask;
+    const uint32_t* conn;
+};
+
+template <typename S>
+__device__ __forceinline__ double as_f(S v, double w);
+template <>
+__device__ __forceinline__ double as_f<double>(double v, double) { return v; }
+template <>
+__device__ __forceinline__ double as_f<float>(float v, double) { return v; }
+template <>
+__device__ __forceinline__ double as_f<__half>(__half v, double w) { return double(__half2float(v)) + double(float(w)); }
+template <>
+__device__ __forceinline__ double as_f<__nv_bfloat16>(__nv_bfloat16 v, double w)
+{
+    return double(__bfloat162float(v)) + double(float(w));
+}
+
+// Moving-wall bits of the masked directions (source class == moving wall).
+template <int Q>
+__device__ __forceinline__ uint32_t bgrid_lidbits(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ mask,
+                                                  const uint32_t* __restrict__ conn, uint32_t b, int i, int j, int k, uint32_t m)
+{
+    uint32_t lid = 0;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (!(m & (1u << q))) continue;
+        uint32_t nb;
+        int      nv;
+        if (bgrid_valid_ngh(mask, conn, b, i, j, k, -Lattice<Q>::cx(q), -Lattice<Q>::cy(q), -Lattice<Q>::cz(q), nb, nv) &&
+            flag_class(__ldg(flags + size_t(nb) * kBlockVoxels + nv)) == NGB_CELL_MOVINGWALL)
+            lid |= 1u << q;
+    }
+    return lid;
+}
+
+template <int Q, typename S, bool F64>
+__global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                 const uint32_t* __restrict__ flags,
+                                                                 BParams<typename std::conditional<F64, double, float>::type> p)
+{
+    using L = Lattice<Q>;
+    const uint32_t b = blockIdx.x;
+    const int      v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
+    const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
+    const int      cls = flag_class(f);
+    const size_t   bq = size_t(b) * Q;
+    if (cls == NGB_CELL_OUTLET) {  // zero-gradient outflow: copy the x-1 neighbour
+        uint32_t nb;
+        int      nv;
+        if (bgrid_valid_ngh(p.mask, p.conn, b, i, j, k, -1, 0, 0, nb, nv)) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) fout[(bq + q) * kBlockVoxels + v] = fin[(size_t(nb) * Q + q) * kBlockVoxels + nv];
+        }
+        return;
+    }
+    if (cls != NGB_CELL_BULK) return;
+    const uint32_t m = flag_mask(f);
+    const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, p.conn, b, i, j, k, m) : 0u;
+    const bool     interior = (i >= 1 && i <= 6 && j >= 1 && j <= 6 && k >= 1 && k <= 6);
+
+    if constexpr (F64) {
+        S pop[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (m & (1u << q)) {
+                const int o = L::opp(q);
+                pop[q] = __ldg(fin + (bq + o) * kBlockVoxels + v) + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            } else if (interior) {
+                pop[q] = __ldg(fin + (bq + q) * kBlockVoxels + v - L::cx(q) - 8 * L::cy(q) - 64 * L::cz(q));
+            } else {
+                int            nv;
+                const uint32_t nb = bgrid_ngh(p.conn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
+                pop[q] = __ldg(fin + (size_t(nb) * Q + q) * kBlockVoxels + nv);
+            }
+        }
+        S out[Q];
+        bgk_f64_ref<Q, S>(pop, p.omega, out);
+#pragma unroll
+        for (int q = 0; q < Q; q++) fout[(bq + q) * kBlockVoxels + v] = out[q];
+    } else {
+        float g[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (m & (1u << q)) {
+                const int o = L::opp(q);
+                g[q] = PairIO<S>::to_g1(__ldg(fin + (bq + o) * kBlockVoxels + v), float(L::w(o))) +
+                       ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            } else if (interior) {
+                g[q] = PairIO<S>::to_g1(__ldg(fin + (bq + q) * kBlockVoxels + v - L::cx(q) - 8 * L::cy(q) - 64 * L::cz(q)),
+                                        float(L::w(q)));
+            } else {
+                int            nv;
+                const uint32_t nb = bgrid_ngh(p.conn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
+                g[q] = PairIO<S>::to_g1(__ldg(fin + (size_t(nb) * Q + q) * kBlockVoxels + nv), float(L::w(q)));
+            }
+        }
+        bgk_shifted<Q, float>(g, p.omega);
+#pragma unroll
+        for (int q = 0; q < Q; q++) PairIO<S>::store1(fout + (bq + q) * kBlockVoxels + v, g[q], float(L::w(q)));
+    }
+}
+
+// ---------------------------------------------------------------- drag
+template <int Q, typename S>
+__global__ void __launch_bounds__(kBlockVoxels) bgrid_drag_kernel(const S* __restrict__ fin, const uint32_t* __restrict__ flags,
+                                                                  const uint32_t* __restrict__ mask,
+                                                                  const uint32_t* __restrict__ conn, double* partials)
+{
+    using L = Lattice<Q>;
+    const uint32_t b = blockIdx.x;
+    const int      v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
+    const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
+    double         F[3] = {0, 0, 0};
+    if (flag_class(f) == NGB_CELL_BULK && flag_mask(f)) {
+        const uint32_t m = flag_mask(f);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (!(m & (1u << q))) continue;
+            uint32_t nb;
+            int      nv;
+            if (!bgrid_valid_ngh(mask, conn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nb, nv)) continue;
+            if (flag_class(__ldg(flags + size_t(nb) * kBlockVoxels + nv)) != NGB_CELL_BOUNCEBACK) continue;
+            const int    o = L::opp(q);
+            const double fo = as_f<S>(fin[(size_t(b) * Q + o) * kBlockVoxels + v], L::w(o));
+            F[0] += 2.0 * L::cx(o) * fo;
+            F[1] += 2.0 * L::cy(o) * fo;
+            F[2] += 2.0 * L::cz(o) * fo;
+        }
+    }
+    // fixed-order block reduction: warp butterfly, then warp 0 over the 16 warp sums
+    __shared__ double red[3][kBlockVoxels / 32];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        double x = F[a];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((v & 31) == 0) red[a][v >> 5] = x;
+    }
+    __syncthreads();
+    if (v < 32) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            double x = v < kBlockVoxels / 32 ? red[a][v] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (v == 0) partials[3 * size_t(b) + a] = x;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) drag_final_kernel(const double* __restrict__ partials, int n, double* force)
+{
+    __shared__ double red[3][256];
+    double            s[3] = {0, 0, 0};
+    for (int b = threadIdx.x; b < n; b += 256)
+        for (int a = 0; a < 3; a++) s[a] += partials[3 * size_t(b) + a];
+    for (int a = 0; a < 3; a++) red[a][threadIdx.x] = s[a];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int a = 0; a < 3; a++) red[a][threadIdx.x] += red[a][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) force[threadIdx.x] = red[threadIdx.x][0];
+}
+
+// ---------------------------------------------------------------- geometry
+constexpr int kMaxCtrl = 256;
+struct GeomParams {
+    int    nx, ny, nz, ctrl_dx, n_ctrl;
+    double sc[3], r, band, tr, tband;
+    double cy[kMaxCtrl], cz[kMaxCtrl];
+};
+
+__global__ void sphere_tube_kernel(GeomParams g, uint8_t* active, uint8_t* cls)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const double dx = double(x) - g.sc[0], dy = double(y) - g.sc[1], dz = double(z) - g.sc[2];
+    const double d2 = dx * dx + dy * dy + dz * dz;
+    const double rs = g.r + g.band;
+    bool         act = d2 <= rs * rs;
+    const int    seg = x / g.ctrl_dx;
+    const double t = double(x - seg * g.ctrl_dx) / double(g.ctrl_dx);
+    const double ay = g.cy[seg] + t * (g.cy[seg + 1] - g.cy[seg]);
+    const double az = g.cz[seg] + t * (g.cz[seg + 1] - g.cz[seg]);
+    const double ty = double(y) - ay, tz = double(z) - az;
+    const double rt = g.tr + g.tband;
+    act = act || (ty * ty + tz * tz <= rt * rt);
+    int c = NGB_CELL_UNDEFINED;
+    if (act) {
+        if (d2 <= g.r * g.r)
+            c = NGB_CELL_BOUNCEBACK;
+        else if (x == 0)
+            c = NGB_CELL_MOVINGWALL;
+        else if (x == g.nx - 1)
+            c = NGB_CELL_OUTLET;
+        else
+            c = NGB_CELL_BULK;
+    }
+    const size_t cell = size_t(x) + size_t(g.nx) * (size_t(y) + size_t(g.ny) * z);
+    if (active) active[cell] = act ? 1 : 0;
+    if (cls) cls[cell] = uint8_t(c);
+}
+
+int validate(const ngb_bgrid_desc* d)
+{
+    NGB_CHECK_ARG(d, "desc is NULL");
+    NGB_CHECK_ARG(d->n_blocks >= 0, "n_blocks < 0");
+    NGB_CHECK_ARG(d->q == 19 || d->q == 27, "q must be 19 or 27 (got %d)", d->q);
+    NGB_CHECK_ARG(d->storage >= NGB_STORE_F64 && d->storage <= NGB_STORE_BF16OFF, "bad storage %d", d->storage);
+    NGB_CHECK_ARG(d->n_blocks == 0 || (d->origin && d->mask && d->conn), "bGrid arrays must be non-NULL");
+    return NGB_OK;
+}
+
+}  // namespace
+
+int launch_bgrid_lbm(const ngb_bgrid_desc* d, const void* fin, void* fout, const uint32_t* flags, cudaStream_t s)
+{
+    if (d->n_blocks == 0) return NGB_OK;
+    const bool q19 = d->q == 19;
+    if (d->storage == NGB_STORE_F64) {
+        BParams<double> p{};
+        p.omega = d->omega;
+        for (int c = 0; c < 2; c++)
+            for (int q = 0; q < 27; q++) p.wall[c][q] = d->wall_term[c][q];
+        p.mask = d->mask, p.conn = d->conn;
+        if (q19)
+            bgrid_lbm_kernel<19, double, true><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const double*>(fin),
+                                                                                   static_cast<double*>(fout), flags, p);
+        else
+            bgrid_lbm_kernel<27, double, true><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const double*>(fin),
+                                                                                   static_cast<double*>(fout), flags, p);
+    } else {
+        BParams<float> p{};
+        p.omega = float(d->omega);
+        for (int c = 0; c < 2; c++)
+            for (int q = 0; q < 27; q++) p.wall[c][q] = float(d->wall_term[c][q]);
+        p.mask = d->mask, p.conn = d->conn;
+#define NGB_B(QQ, T) \
+    bgrid_lbm_kernel<QQ, T, false><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)
+        switch (d->storage) {
+            case NGB_STORE_F32:
+                if (q19) NGB_B(19, float); else NGB_B(27, float);
+                break;
+            case NGB_STORE_F16OFF:
+                if (q19) NGB_B(19, __half); else NGB_B(27, __half);
+                break;
+            default:
+                if (q19) NGB_B(19, __nv_bfloat16); else NGB_B(27, __nv_bfloat16);
+                break;
+        }
+#undef NGB_B
+    }
+    NGB_LAUNCH_CHECK("bgrid_lbm_kernel");
+    return NGB_OK;
+}
+
+}  // namespace ngb
+
+using namespace ngb;
+
+extern "C" {
+
+int ngb_bgrid_lbm_step(const ngb_bgrid_desc* d, const void* fin, void* fout, const uint32_t* flags, void* stream)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(fin && fout && fin != fout && flags, "fin/fout/flags must be non-NULL and fin != fout");
+    return launch_bgrid_lbm(d, fin, fout, flags, as_stream(stream));
+}
+
+int ngb_bgrid_drag(const ngb_bgrid_desc* d, const void* fin, const uint32_t* flags, double* partials, double* force, void* stream)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(fin && flags && partials && force, "NULL argument");
+    cudaStream_t s = as_stream(stream);
+    if (d->n_blocks == 0) {
+        NGB_CUDA_TRY(cudaMemsetAsync(force, 0, 3 * sizeof(double), s));
+        return NGB_OK;
+    }
+    const bool q19 = d->q == 19;
+#define NGB_D(QQ, T) \
+    bgrid_drag_kernel<QQ, T><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const T*>(fin), flags, d->mask, d->conn, partials)
+    switch (d->storage) {
+        case NGB_STORE_F64:
+            if (q19) NGB_D(19, double); else NGB_D(27, double);
+            break;
+        case NGB_STORE_F32:
+            if (q19) NGB_D(19, float); else NGB_D(27, float);
+            break;
+        case NGB_STORE_F16OFF:
+            if (q19) NGB_D(19, __half); else NGB_D(27, __half);
+            break;
+        default:
+            if (q19) NGB_D(19, __nv_bfloat16); else NGB_D(27, __nv_bfloat16);
+            break;
+    }
+#undef NGB_D
+    NGB_LAUNCH_CHECK("bgrid_drag_kernel");
+    drag_final_kernel<<<1, 256, 0, s>>>(partials, d->n_blocks, force);
+    NGB_LAUNCH_CHECK("drag_final_kernel");
+    return NGB_OK;
+}
+
+int ngb_geometry_sphere_tube(const ngb_sphere_tube* g, uint8_t* active, uint8_t* cls, void* stream)
+{
+    NGB_CHECK_ARG(g, "geometry is NULL");
+    NGB_CHECK_ARG(g->nx > 0 && g->ny > 0 && g->nz > 0 && g->ny <= 65535 && g->nz <= 65535, "bad dims");
+    NGB_CHECK_ARG(g->ctrl_dx > 0, "ctrl_dx must be positive");
+    NGB_CHECK_ARG(active || cls, "nothing to write");
+    GeomParams p{};
+    p.nx = g->nx, p.ny = g->ny, p.nz = g->nz, p.ctrl_dx = g->ctrl_dx;
+    p.n_ctrl = g->nx / g->ctrl_dx + 2;
+    NGB_CHECK_ARG(p.n_ctrl <= kMaxCtrl, "too many tube control points (nx / ctrl_dx + 2 > %d)", kMaxCtrl);
+    for (int a = 0; a < 3; a++) p.sc[a] = g->sphere_c[a];
+    p.r = g->sphere_r, p.band = g->band, p.tr = g->tube_r, p.tband = g->tube_band;
+    std::mt19937_64 rng(g->seed);
+    auto            u01 = [&]() { return double(rng() >> 11) * (1.0 / 9007199254740992.0); };
+    for (int c = 0; c < p.n_ctrl; c++) {
+        p.cy[c] = g->tube_c[0] + g->amplitude * (2.0 * u01() - 1.0);
+        p.cz[c] = g->tube_c[1] + g->amplitude * (2.0 * u01() - 1.0);
+    }
+    sphere_tube_kernel<<<dim3((g->nx + 127) / 128, g->ny, g->nz), 128, 0, as_stream(stream)>>>(p, active, cls);
+    NGB_LAUNCH_CHECK("sphere_tube_kernel");
+    return NGB_OK;
+}
+
+}  // extern "C"

@@ -79,11 +79,13 @@ __device__ __forceinline__ int cell_setup(const DenseParams<C>& p, const uint32_
     return cls;
 }
 
-// Outlet node: zero-gradient outflow, copies the x-1 neighbour's populations.
+// Outlet node: zero-gradient outflow, copies the x-1 neighbour's populations
+// when that neighbour exists (inside the box and not "undefined").
 template <int Q, typename S>
-__device__ __forceinline__ void outlet_copy(const S* __restrict__ fin, S* __restrict__ fout, int64_t stride, int64_t cell, int x)
+__device__ __forceinline__ void outlet_copy(const S* __restrict__ fin, S* __restrict__ fout, int64_t stride, int64_t cell, int x,
+                                            const uint32_t* __restrict__ flags)
 {
-    if (x == 0) return;
+    if (x == 0 || flag_class(__ldg(flags + cell - 1)) == NGB_CELL_UNDEFINED) return;
 #pragma unroll
     for (int q = 0; q < Q; q++) fout[q * stride + cell] = fin[q * stride + cell - 1];
 }
@@ -92,38 +94,14 @@ __device__ __forceinline__ void outlet_copy(const S* __restrict__ fin, S* __rest
 // D3Q19: the expression shapes of LbmTools.h:78-282 in double (compile with
 // --fmad=false for IEEE operation order). D3Q27: the project's per-direction
 // BGK (rho = sum f, u = sum c f / rho, eq = rho w (1 + 3cu + 4.5cu^2 - usqr)).
+// FP64 BGK of the reference (D3Q19: LbmTools.h:171-282 expression shapes;
+// D3Q27: the project's per-direction form), on pulled populations.
 template <int Q, typename S>
-__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                   const uint32_t* __restrict__ flags, DenseParams<double> p)
+__device__ __forceinline__ void bgk_f64_ref(const S (&pop)[Q], double omega_, S (&out)[Q])
 {
     using L = Lattice<Q>;
-    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= p.nx) return;
-    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
-    const int64_t cell = x + sy * y + sz * z;
-    uint32_t      mask, lidbits;
-    const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
-    if (cls == NGB_CELL_OUTLET) {
-        outlet_copy<Q>(fin, fout, stride, cell, x);
-        return;
-    }
-    if (cls != NGB_CELL_BULK) return;
-
-    S pop[Q];
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        if (mask & (1u << q)) {
-            const int o = L::opp(q);
-            const S   wt = S((lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o]);
-            pop[q] = __ldg(fin + o * stride + cell) + wt;
-        } else {
-            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-            pop[q] = __ldg(fin + q * stride + src);
-        }
-    }
     using Cd = double;
-    const Cd omega = p.omega;
+    const Cd omega = omega_;
     if constexpr (Q == 19) {
 #define P(I) static_cast<Cd>(pop[I])
         const Cd X_M1 = P(0) + P(3) + P(4) + P(5) + P(6);
@@ -144,13 +122,11 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __re
             const Cd wk = k < 3 ? (1. / 18.) : (1. / 36.);
             const Cd eq = rho * wk * (1. - 3. * cu[k] + 4.5 * cu[k] * cu[k] - usqr);
             const Cd eqopp = eq + rho * wk * 6. * cu[k];
-            const Cd out = (1. - omega) * P(k) + omega * eq;
-            const Cd outopp = (1. - omega) * P(k + 10) + omega * eqopp;
-            fout[k * stride + cell] = static_cast<S>(out);
-            fout[(k + 10) * stride + cell] = static_cast<S>(outopp);
+            out[k] = static_cast<S>((1. - omega) * P(k) + omega * eq);
+            out[k + 10] = static_cast<S>((1. - omega) * P(k + 10) + omega * eqopp);
         }
         const Cd eq9 = rho * (1. / 3.) * (1. - usqr);
-        fout[9 * stride + cell] = static_cast<S>((1. - omega) * P(9) + omega * eq9);
+        out[9] = static_cast<S>((1. - omega) * P(9) + omega * eq9);
 #undef P
     } else {
         Cd f[Q];
@@ -170,9 +146,45 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __re
         for (int q = 0; q < Q; q++) {
             const Cd cu = Cd(L::cx(q)) * ux + Cd(L::cy(q)) * uy + Cd(L::cz(q)) * uz;
             const Cd eq = rho * Cd(L::w(q)) * (Cd(1) + Cd(3) * cu + Cd(4.5) * cu * cu - usqr);
-            fout[q * stride + cell] = static_cast<S>((Cd(1) - omega) * f[q] + omega * eq);
+            out[q] = static_cast<S>((Cd(1) - omega) * f[q] + omega * eq);
         }
     }
+}
+
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                   const uint32_t* __restrict__ flags, DenseParams<double> p)
+{
+    using L = Lattice<Q>;
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= p.nx) return;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    const int64_t cell = x + sy * y + sz * z;
+    uint32_t      mask, lidbits;
+    const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
+    if (cls == NGB_CELL_OUTLET) {
+        outlet_copy<Q>(fin, fout, stride, cell, x, flags);
+        return;
+    }
+    if (cls != NGB_CELL_BULK) return;
+
+    S pop[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (mask & (1u << q)) {
+            const int o = L::opp(q);
+            const S   wt = S((lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o]);
+            pop[q] = __ldg(fin + o * stride + cell) + wt;
+        } else {
+            const int64_t src = cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
+            pop[q] = __ldg(fin + q * stride + src);
+        }
+    }
+    S out[Q];
+    bgk_f64_ref<Q, S>(pop, p.omega, out);
+#pragma unroll
+    for (int q = 0; q < Q; q++) fout[q * stride + cell] = out[q];
 }
 
 // Host-side launchers (lbm_dense.cu / lbm_dense_f64.cu).

@@ -1,0 +1,31 @@
+// Instantiations of the two-cells-per-thread dense LBM kernel. Compiled with
+// --fmad=false: the kernel writes every fused multiply-add explicitly.
+#include "lbm_shifted.cuh"
+
+namespace ngb {
+
+int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
+                         cudaStream_t s)
+{
+    const dim3 grid((p.nx + kLbmBlockX - 1) / kLbmBlockX, p.ny, p.nz), block(kLbmBlockX);
+#define NGB_ONE(QQ, T) \
+    lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)
+    const bool q19 = Q == 19;
+    switch (storage) {
+        case NGB_STORE_F32:
+            if (q19) NGB_ONE(19, float); else NGB_ONE(27, float);
+            break;
+        case NGB_STORE_F16OFF:
+            if (q19) NGB_ONE(19, __half); else NGB_ONE(27, __half);
+            break;
+        case NGB_STORE_BF16OFF:
+            if (q19) NGB_ONE(19, __nv_bfloat16); else NGB_ONE(27, __nv_bfloat16);
+            break;
+        default: set_error("unsupported storage %d", storage); return NGB_ERR_UNSUPPORTED;
+    }
+#undef NGB_ONE
+    NGB_LAUNCH_CHECK("lbm_dense_single_kernel");
+    return NGB_OK;
+}
+
+}  // namespace ngb

@@ -1,13 +1,10 @@
-// Dense LBM pull stream-collide, FP32 compute on equilibrium-shifted values,
-// two x-adjacent cells per thread.
-//
-// Each thread owns the cell pair (x0, x0+1), x0 even. Every population plane
-// is read with one aligned 2-element load per thread (8 B for FP32, 4 B for
-// the 16-bit offset forms) when the source is x-aligned, and with two aligned
-// loads plus a byte permute when the source is shifted by +-1 in x; the
-// result is stored with one aligned 2-element store. The BGK arithmetic runs
-// on float2 with Blackwell's packed FP32 instructions (fma/add/mul .f32x2),
-// halving the issued math instructions per cell.
+// Dense LBM pull stream-collide, FP32 compute on equilibrium-shifted values
+// (g = f - w), one cell per thread, x fastest: each population plane is read
+// with one coalesced (+-1-element shifted) row access per warp and written with
+// one aligned row access, so every population element crosses HBM once per
+// step. Plane offsets depend only on kernel parameters (warp-uniform).
+// The BGK helper also has a float2 form for Blackwell's packed FP32x2
+// instructions (fma/add/mul .f32x2), used where two cells share a thread.
 //
 // The arithmetic is an explicit sequence of IEEE operations (this file is
 // compiled with --fmad=false; every fused multiply-add is written out), so a
@@ -22,9 +19,6 @@
 #include "lbm_kernels.cuh"
 
 namespace ngb {
-
-constexpr int kPairX = 32;  // pairs per block row (64 cells)
-constexpr int kPairY = 4;   // rows per block
 
 // ------------------------------------------------------------------ packed FP32 helpers
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
@@ -220,129 +214,7 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
     }
 }
 
-template <int Q, typename S>
-__global__ void __launch_bounds__(kPairX* kPairY, (Q == 19 ? 4 : 3)) lbm_dense_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                       const uint32_t* __restrict__ flags, DenseParams<float> p)
-{
-    using L = Lattice<Q>;
-    using IO = PairIO<S>;
-    const int x0 = 2 * (blockIdx.x * kPairX + threadIdx.x);
-    const int y = blockIdx.y * kPairY + threadIdx.y;
-    const int z = blockIdx.z;
-    if (x0 >= p.nx || y >= p.ny) return;
-    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
-    const int64_t cell0 = x0 + sy * y + sz * z;
-
-    uint32_t  m0, l0, m1, l1;
-    const int c0 = cell_setup<Q>(p, flags, x0, y, z, cell0, m0, l0);
-    const int c1 = cell_setup<Q>(p, flags, x0 + 1, y, z, cell0 + 1, m1, l1);
-    const bool b0 = c0 == NGB_CELL_BULK, b1 = c1 == NGB_CELL_BULK;
-    if (c0 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell0, x0);
-    if (c1 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell0 + 1, x0 + 1);
-    if (!b0 && !b1) return;
-
-    float2 g[Q];
-    if (b0 && b1 && (m0 | m1) == 0) {
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const int     cx = L::cx(q);
-            const int64_t row = cell0 - L::cy(q) * sy - L::cz(q) * sz;  // source row, x = x0
-            const S*      base = fin + q * stride + row;
-            typename IO::Word v;
-            if (cx == 0) {
-                v = IO::load(base);
-            } else if (cx > 0) {  // source x0-1, x0
-                v = IO::mid(IO::load(base - 2), IO::load(base));
-            } else {  // source x0+1, x0+2
-                v = IO::mid(IO::load(base), IO::load(base + 2));
-            }
-            g[q] = IO::to_g(v, float(L::w(q)));
-        }
-    } else {
-        float ga[Q], gb[Q];
-        if (b0) pull_one<Q, S>(fin, stride, cell0, sy, sz, m0, l0, p, ga);
-        if (b1) pull_one<Q, S>(fin, stride, cell0 + 1, sy, sz, m1, l1, p, gb);
-#pragma unroll
-        for (int q = 0; q < Q; q++) g[q] = make_float2(b0 ? ga[q] : 0.f, b1 ? gb[q] : 0.f);
-    }
-
-    bgk_shifted<Q, float2>(g, p.omega);
-
-    // ---- store
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        S*          dst = fout + q * stride + cell0;
-        const float w = float(L::w(q));
-        if (b0 && b1) {
-            IO::store(dst, g[q], w);
-        } else {
-            if (b0) IO::store1(dst, g[q].x, w);
-            if (b1) IO::store1(dst + 1, g[q].y, w);
-        }
-    }
-}
-
-// Two cells per thread stacked in z, (x, y, z0) and (x, y, z0+1): every load is
-// a plain per-cell load (no x realignment), the two cells' populations are
-// packed lane-wise into float2 and collided with the packed FP32x2 math.
-template <int Q, typename S>
-__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_zpair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                    const uint32_t* __restrict__ flags, DenseParams<float> p)
-{
-    using L = Lattice<Q>;
-    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
-    const int y = blockIdx.y, z0 = 2 * blockIdx.z;
-    if (x >= p.nx) return;
-    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
-    const int64_t cell0 = x + sy * y + sz * z0, cell1 = cell0 + sz;
-    const bool    has1 = z0 + 1 < p.nz;
-    uint32_t      m0, l0, m1 = 0, l1 = 0;
-    const int     c0 = cell_setup<Q>(p, flags, x, y, z0, cell0, m0, l0);
-    const int     c1 = has1 ? cell_setup<Q>(p, flags, x, y, z0 + 1, cell1, m1, l1) : NGB_CELL_UNDEFINED;
-    if (c0 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell0, x);
-    if (c1 == NGB_CELL_OUTLET) outlet_copy<Q>(fin, fout, stride, cell1, x);
-    const bool b0 = c0 == NGB_CELL_BULK, b1 = c1 == NGB_CELL_BULK;
-    if (!b0 && !b1) return;
-    float2 g[Q];
-    if (b0 && b1 && (m0 | m1) == 0) {
-        const S* P0 = fin + cell0;
-        const S* P1 = fin + cell1;
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const int64_t off = q * stride - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-            g[q] = make_float2(PairIO<S>::to_g1(__ldg(P0 + off), float(L::w(q))), PairIO<S>::to_g1(__ldg(P1 + off), float(L::w(q))));
-        }
-    } else {
-        float t[Q];
-        if (b0) {
-            pull_one<Q, S>(fin, stride, cell0, sy, sz, m0, l0, p, t);
-#pragma unroll
-            for (int q = 0; q < Q; q++) g[q].x = t[q];
-        } else {
-#pragma unroll
-            for (int q = 0; q < Q; q++) g[q].x = 0.f;
-        }
-        if (b1) {
-            pull_one<Q, S>(fin, stride, cell1, sy, sz, m1, l1, p, t);
-#pragma unroll
-            for (int q = 0; q < Q; q++) g[q].y = t[q];
-        } else {
-#pragma unroll
-            for (int q = 0; q < Q; q++) g[q].y = 0.f;
-        }
-    }
-    bgk_shifted<Q, float2>(g, p.omega);
-    S* D0 = fout + cell0;
-    S* D1 = fout + cell1;
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        const float w = float(L::w(q));
-        if (b0) PairIO<S>::store1(D0 + q * stride, g[q].x, w);
-        if (b1) PairIO<S>::store1(D1 + q * stride, g[q].y, w);
-    }
-}
-
-// One cell per thread (odd nx or unaligned buffers): same arithmetic as the pair kernel.
+// One cell per thread.
 template <int Q, typename S>
 __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* __restrict__ fin, S* __restrict__ fout,
                                                                      const uint32_t* __restrict__ flags, DenseParams<float> p)
@@ -356,7 +228,7 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* _
     uint32_t      mask, lidbits;
     const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
     if (cls == NGB_CELL_OUTLET) {
-        outlet_copy<Q>(fin, fout, stride, cell, x);
+        outlet_copy<Q>(fin, fout, stride, cell, x, flags);
         return;
     }
     if (cls != NGB_CELL_BULK) return;

@@ -64,6 +64,9 @@ def lib():
         L.orc_bgrid_build.restype = c_int64
         L.orc_laplace_i64.argtypes = [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]
         L.orc_masked_values_i64.argtypes = [c_int, c_int, c_int, c_int64, c_int, c_void_p]
+        L.orc_sphere_tube.argtypes = [c_int, c_int, c_int, c_int, c_void_p, c_double, c_double, c_void_p, c_double,
+                                      c_double, c_double, c_uint64, c_void_p, c_void_p]
+        L.orc_flags_from_classes.argtypes = [c_int, c_int, c_int, c_int, c_void_p, c_void_p]
         L.orc_box_boundary.argtypes = [c_int, c_int, c_int, c_void_p]
         L.orc_gaussian_sources.argtypes = [c_int, c_int, c_int, c_uint64, c_void_p, c_void_p]
         L.orc_laplacian_f64.argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]

@@ -63,7 +63,9 @@ inline double w27(int q)
 
 // ---------------------------------------------------------------- cell type
 // CellType.h:3-35: {uint32 wallNghBitflag; classification}.
-enum Classification : int { bounceBack = 0, movingWall = 1, bulk = 2, undefined = 3 };
+// outlet (zero-gradient outflow: copies the x-1 neighbour) is the project's own addition.
+enum Classification : int { bounceBack = 0, movingWall = 1, bulk = 2, undefined = 3, outlet = 4 };
+inline bool is_fluid(int c) { return c == bulk || c == outlet; }
 struct CellType {
     uint32_t wallNghBitflag = 0;
     int      classification = bulk;
@@ -217,7 +219,7 @@ inline void compute_wall_mask(int nx, int ny, int nz, int Q, CellType* flag)
                     const int sx = x - cx, sy = y - cy, sz = z - cz;
                     int       cls = undefined;
                     if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = in[lin(sx, sy, sz, nx, ny)].classification;
-                    if (cls != bulk) c.wallNghBitflag |= (uint32_t(1) << q);
+                    if (!is_fluid(cls)) c.wallNghBitflag |= (uint32_t(1) << q);
                 }
                 flag[lin(x, y, z, nx, ny)] = c;
             }
@@ -237,6 +239,11 @@ void d3q19_step(int nx, int ny, int nz, const S* fin, S* fout, const CellType* f
         for (int y = 0; y < ny; y++)
             for (int x = 0; x < nx; x++) {
                 const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (cell.classification == outlet) {
+                    if (x > 0 && flag[lin(x - 1, y, z, nx, ny)].classification != undefined)
+                        for (int q = 0; q < 19; q++) fout[size_t(q) * V + lin(x, y, z, nx, ny)] = at(x - 1, y, z, q);
+                    continue;
+                }
                 if (cell.classification != bulk) continue;
                 const uint32_t m = cell.wallNghBitflag;
                 S              pop[19];
@@ -321,6 +328,11 @@ void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Loa
         for (int y = 0; y < ny; y++)
             for (int x = 0; x < nx; x++) {
                 const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (cell.classification == outlet) {
+                    if (x > 0 && flag[lin(x - 1, y, z, nx, ny)].classification != undefined)
+                        for (int q = 0; q < Q; q++) store(x, y, z, q, load(x - 1, y, z, q));
+                    continue;
+                }
                 if (cell.classification != bulk) continue;
                 C f[Q];
                 for (int q = 0; q < Q; q++) {
@@ -379,6 +391,11 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
         for (int y = 0; y < ny; y++)
             for (int x = 0; x < nx; x++) {
                 const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (cell.classification == outlet) {
+                    if (x > 0 && flag[lin(x - 1, y, z, nx, ny)].classification != undefined)
+                        for (int q = 0; q < Q; q++) storeg(x, y, z, q, loadg(x - 1, y, z, q));
+                    continue;
+                }
                 if (cell.classification != bulk) continue;
                 float g[Q];
                 for (int q = 0; q < Q; q++) {

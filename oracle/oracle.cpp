@@ -50,7 +50,7 @@ void generic_run(int nx, int ny, int nz, const CellType* flag, double omega, S* 
         S*       fout = (t % 2 == 0) ? b : a;
         auto     load = [&](int x, int y, int z, int q) -> C { return toC(fin[size_t(q) * V + lin(x, y, z, nx, ny)], q); };
         auto     store = [&](int x, int y, int z, int q, C v) { fout[size_t(q) * V + lin(x, y, z, nx, ny)] = fromC(v, q); };
-        auto     wall = [&](int cls, int q) -> C { return (cls >= 0 && cls < 4) ? C(g_wall[cls][q]) : C(0); };
+        auto     wall = [&](int cls, int q) -> C { return C(cls == movingWall ? g_wall[1][q] : g_wall[0][q]); };
 #pragma omp parallel for schedule(static) num_threads(threads)
         for (int z = 0; z < nz; z++) bgk_step_generic<C, Q>(nx, ny, nz, flag, C(omega), load, store, wall, z, z + 1);
     }
@@ -65,7 +65,7 @@ void shifted_run(int nx, int ny, int nz, const CellType* flag, float omega, S* a
         S*       fout = (t % 2 == 0) ? b : a;
         auto     loadg = [&](int x, int y, int z, int q) -> float { return toG(fin[size_t(q) * V + lin(x, y, z, nx, ny)], q); };
         auto     storeg = [&](int x, int y, int z, int q, float g) { fout[size_t(q) * V + lin(x, y, z, nx, ny)] = fromG(g, q); };
-        auto     wall = [&](int cls, int q) -> double { return (cls >= 0 && cls < 4) ? g_wall[cls][q] : 0.0; };
+        auto     wall = [&](int cls, int q) -> double { return cls == movingWall ? g_wall[1][q] : g_wall[0][q]; };
 #pragma omp parallel for schedule(static) num_threads(threads)
         for (int z = 0; z < nz; z++) bgk_step_shifted<Q>(nx, ny, nz, flag, omega, loadg, storeg, wall, z, z + 1);
     }
@@ -229,7 +229,7 @@ int orc_velocity(int nx, int ny, int nz, int Q, int storage, const double* wall,
     const size_t          V = size_t(nx) * ny * nz;
     std::vector<CellType> flag(V);
     for (size_t i = 0; i < V; i++) flag[i] = unpack(packed[i]);
-    auto wt = [&](int cls, int q) -> double { return (wall && cls >= 0 && cls < 4) ? wall[cls * 27 + q] : 0.0; };
+    auto wt = [&](int cls, int q) -> double { return wall ? wall[(cls == movingWall ? 1 : 0) * 27 + q] : 0.0; };
     auto load = [&](int x, int y, int z, int q) -> double {
         const size_t i = size_t(q) * V + lin(x, y, z, nx, ny);
         switch (storage) {
@@ -302,6 +302,54 @@ void orc_masked_values_i64(int nx, int ny, int nz, int64_t offset, int digit, in
     for (int z = 0; z < nz; z++)
         for (int y = 0; y < ny; y++)
             for (int x = 0; x < nx; x++) out[plin(x, y, z, nx, ny)] = masked_value<int64_t>(x, y, z, 0, offset, digit);
+}
+
+// ------------------------------------------------------------------ flow-over-sphere geometry
+// Restatement of the geometry of ngb_geometry_sphere_tube (a project case,
+// no reference counterpart): same double-precision expressions, same
+// std::mt19937_64 stream and 53-bit uniforms.
+int orc_sphere_tube(int nx, int ny, int nz, int ctrl_dx, const double* sc, double r, double band, const double* tc, double tr,
+                    double tband, double amplitude, uint64_t seed, uint8_t* active, uint8_t* cls)
+{
+    const int           n_ctrl = nx / ctrl_dx + 2;
+    std::vector<double> cy(n_ctrl), cz(n_ctrl);
+    std::mt19937_64     rng(seed);
+    for (int c = 0; c < n_ctrl; c++) {
+        cy[c] = tc[0] + amplitude * (2.0 * u01(rng) - 1.0);
+        cz[c] = tc[1] + amplitude * (2.0 * u01(rng) - 1.0);
+    }
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const double dx = double(x) - sc[0], dy = double(y) - sc[1], dz = double(z) - sc[2];
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                const double rs = r + band;
+                bool         act = d2 <= rs * rs;
+                const int    seg = x / ctrl_dx;
+                const double t = double(x - seg * ctrl_dx) / double(ctrl_dx);
+                const double ay = cy[seg] + t * (cy[seg + 1] - cy[seg]);
+                const double az = cz[seg] + t * (cz[seg + 1] - cz[seg]);
+                const double ty = double(y) - ay, tz = double(z) - az;
+                const double rt = tr + tband;
+                act = act || (ty * ty + tz * tz <= rt * rt);
+                int c = undefined;
+                if (act) c = d2 <= r * r ? bounceBack : (x == 0 ? movingWall : (x == nx - 1 ? outlet : bulk));
+                const size_t i = lin(x, y, z, nx, ny);
+                active[i] = act ? 1 : 0;
+                cls[i] = uint8_t(c);
+            }
+    return 0;
+}
+
+// Packed flags (mask computed) from a dense uint8 class map.
+int orc_flags_from_classes(int nx, int ny, int nz, int Q, const uint8_t* cls, uint32_t* packed)
+{
+    const size_t          V = size_t(nx) * ny * nz;
+    std::vector<CellType> f(V);
+    for (size_t i = 0; i < V; i++) f[i].classification = cls[i], f[i].wallNghBitflag = 0;
+    compute_wall_mask(nx, ny, nz, Q, f.data());
+    for (size_t i = 0; i < V; i++) packed[i] = pack(f[i]);
+    return 0;
 }
 
 // ------------------------------------------------------------------ Poisson
