@@ -223,6 +223,79 @@ int ngb_bgrid_laplace_i64(const ngb_bgrid_desc* desc, const int64_t* a, int64_t*
  * dPartition.h:228-263). */
 int ngb_dense_laplace_i64(int32_t nx, int32_t ny, int32_t nz, const int64_t* a, int64_t* b, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Poisson: 7-point Laplacian and (Jacobi-preconditioned) CG
+ * ---------------------------------------------------------------------- */
+
+/* Dense single-partition scalar field (x fastest). `field` is NGB_STORE_F32
+ * or NGB_STORE_F64. `bd` marks each cell Fixed (0, Dirichlet) or Free (1)
+ * as libNeonSolver's BoundaryCondition (IterativeLinearSolver.h:17-21);
+ * NULL means every box-face cell is Fixed and every other cell Free. */
+typedef struct ngb_poisson_desc {
+    int32_t       nx, ny, nz;
+    int32_t       field;
+    double        h; /* grid spacing */
+    const int8_t* bd;
+} ngb_poisson_desc;
+
+/* out = A u: Fixed rows copy u; Free rows (n_valid u - sum of valid
+ * neighbours) / h^2 with neighbours valid inside the box. Replaces
+ * LaplacianMatVec::matVec (libNeonSolver/src/linear/matvecs/LaplacianMatVec.cu:9-99). */
+int ngb_laplacian_apply(const ngb_poisson_desc* desc, const void* u, void* out, void* stream);
+
+/* Doubles of scratch a dot product of n elements needs (per-CTA partials
+ * and a ticket word). */
+size_t ngb_dot_scratch_doubles(int64_t n);
+
+/* *result (device double) = sum_i a_i b_i accumulated in FP64 with a fixed
+ * reduction tree (run-to-run deterministic): warp shuffles, per-CTA partials
+ * in `scratch`, the last CTA to finish sums the partials in CTA order.
+ * `field` selects float or double inputs. Replaces the stubbed grid dot
+ * (dGrid::dot, dGrid_imp.h:254-281; ReduceKernels.cuh:7-76 compiled out). */
+int ngb_dot(int64_t n, int32_t field, const void* a, const void* b, double* result, double* scratch, void* stream);
+
+typedef struct ngb_cg_params {
+    double  tol;           /* stop when |b - A x| / |b| <= tol (true residual, FP64) */
+    int32_t max_iter;
+    int32_t refresh_every; /* true-residual recompute period (iterative refinement), >= 1 */
+    int32_t check_every;   /* iterations per captured CUDA graph between host polls, >= 1 */
+    int32_t jacobi;        /* 1: Jacobi preconditioner z = r / diag(A); 0: plain CG */
+} ngb_cg_params;
+
+typedef struct ngb_cg_result {
+    int32_t iterations;
+    int32_t converged;
+    int32_t refreshes;
+    int32_t pad;
+    double  rel_residual; /* last true relative residual */
+    double  seconds;      /* wall time of the iteration loop */
+} ngb_cg_result;
+
+/* Bytes of device workspace ngb_cg_solve needs for this desc. */
+size_t ngb_cg_workspace_bytes(const ngb_poisson_desc* desc);
+
+/* Solves A x = b (A as ngb_laplacian_apply). Fields r, p, s and the
+ * increment of x are in `desc->field` precision; every reduction, the
+ * solution x (double, device, in: initial guess, out: solution) and the
+ * periodic true residual b - A x are FP64 (iterative refinement). alpha,
+ * beta and the stopping decision stay on the device; the iteration is
+ * captured once as a CUDA graph of `check_every` iterations and the host
+ * polls a 4-byte flag between graph launches. Synchronous.
+ * Replaces CG_t::solve (libNeonSolver/src/linear/krylov/CG.cpp:55-156) with
+ * the containers of CGContainers.cu:11-149. */
+int ngb_cg_solve(const ngb_poisson_desc* desc, const void* b, double* x, void* workspace, size_t workspace_bytes,
+                 const ngb_cg_params* params, ngb_cg_result* result, void* stream);
+
+/* Right-hand side of the Poisson case: f = sum of 8 Gaussians
+ * A_k exp(-|x - c_k|^2 / (2 sigma^2)), centres (8x3) and amplitudes from the
+ * caller (see ngb_gaussian_sources), written in `field` precision. */
+int ngb_poisson_rhs(const ngb_poisson_desc* desc, const double* centres, const double* amps, double sigma, void* f,
+                    void* stream);
+
+/* Deterministic sources: centres uniform in [n/8, 7n/8) per axis, amplitudes
+ * uniform in [-1, 1), from std::mt19937_64(seed) 53-bit uniforms (host). */
+int ngb_gaussian_sources(int32_t nx, int32_t ny, int32_t nz, uint64_t seed, double* centres, double* amps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,34 @@ _EXTRA_SIGNATURES = {
 }
 
 
+class PoissonDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32), ("field", ctypes.c_int32),
+                ("h", ctypes.c_double), ("bd", ctypes.c_void_p)]
+
+
+class CgParams(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("refresh_every", ctypes.c_int32),
+                ("check_every", ctypes.c_int32), ("jacobi", ctypes.c_int32)]
+
+
+class CgResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("converged", ctypes.c_int32), ("refreshes", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+_pd = ctypes.POINTER(PoissonDesc)
+_EXTRA_SIGNATURES.update({
+    "ngb_laplacian_apply": ([_pd, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_dot_scratch_doubles": ([ctypes.c_int64], ctypes.c_size_t),
+    "ngb_dot": ([ctypes.c_int64, _i32, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_cg_workspace_bytes": ([_pd], ctypes.c_size_t),
+    "ngb_cg_solve": ([_pd, _vp, _vp, _vp, ctypes.c_size_t, ctypes.POINTER(CgParams), ctypes.POINTER(CgResult), _vp],
+                     ctypes.c_int),
+    "ngb_poisson_rhs": ([_pd, _vp, _vp, _dbl, _vp, _vp], ctypes.c_int),
+    "ngb_gaussian_sources": ([_i32, _i32, _i32, ctypes.c_uint64, _vp, _vp], ctypes.c_int),
+})
+
+
 def check(rc):
     if rc != NGB_OK:
         raise NeonError("neon_gb300 error %d: %s" % (rc, lib().ngb_last_error().decode()))
@@ -277,3 +305,60 @@ def sphere_config(scale=1):
     s = scale
     return sphere_tube(512 // s, 256 // s, 256 // s, (128 / s, 128 / s, 128 / s), 32 / s, 48 / s, (128 / s, 128 / s),
                        40 / s, 48 / s, 24 / s, max(1, 64 // s), 2024)
+
+
+# ----------------------------------------------------------------------------- Poisson
+def poisson_desc(nx, ny, nz, field="f32", h=1.0, bd=None):
+    d = PoissonDesc()
+    d.nx, d.ny, d.nz = nx, ny, nz
+    d.field = STORAGE_NAMES[field] if isinstance(field, str) else field
+    d.h = h
+    d.bd = bd.data_ptr() if bd is not None else None
+    return d
+
+
+def laplacian_apply(desc, u, out, stream=None):
+    return check(lib().ngb_laplacian_apply(ctypes.byref(desc), _ptr(u), _ptr(out), _stream(stream)))
+
+
+def dot(a, b, result, scratch=None, stream=None):
+    """result (1-element float64 cuda tensor) = <a, b> accumulated in FP64."""
+    import torch
+    n = a.numel()
+    if scratch is None:
+        scratch = torch.empty(lib().ngb_dot_scratch_doubles(n), dtype=torch.float64, device=a.device)
+    field = STORE_F64 if a.dtype == torch.float64 else STORE_F32
+    return check(lib().ngb_dot(n, field, _ptr(a), _ptr(b), _ptr(result), _ptr(scratch), _stream(stream)))
+
+
+def cg_workspace(desc, device):
+    import torch
+    nbytes = lib().ngb_cg_workspace_bytes(ctypes.byref(desc))
+    return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+
+def cg_solve(desc, b, x, workspace, tol=1e-8, max_iter=10000, refresh_every=50, check_every=50, jacobi=True,
+             stream=None):
+    """Jacobi-PCG / CG on the device; x (float64 cuda tensor) is the initial guess and the solution."""
+    p = CgParams()
+    p.tol, p.max_iter, p.refresh_every, p.check_every, p.jacobi = tol, max_iter, refresh_every, check_every, int(jacobi)
+    r = CgResult()
+    check(lib().ngb_cg_solve(ctypes.byref(desc), _ptr(b), _ptr(x), _ptr(workspace), workspace.numel(),
+                             ctypes.byref(p), ctypes.byref(r), _stream(stream)))
+    return {"iterations": r.iterations, "converged": bool(r.converged), "refreshes": r.refreshes,
+            "rel_residual": r.rel_residual, "seconds": r.seconds}
+
+
+def gaussian_sources(nx, ny, nz, seed):
+    import numpy as np
+    c = np.zeros(24)
+    a = np.zeros(8)
+    check(lib().ngb_gaussian_sources(nx, ny, nz, seed, c.ctypes.data_as(ctypes.c_void_p),
+                                     a.ctypes.data_as(ctypes.c_void_p)))
+    return c, a
+
+
+def poisson_rhs(desc, centres, amps, sigma, f, stream=None):
+    """centres/amps: float64 cuda tensors (24 and 8 values)."""
+    return check(lib().ngb_poisson_rhs(ctypes.byref(desc), _ptr(centres), _ptr(amps), float(sigma), _ptr(f),
+                                       _stream(stream)))

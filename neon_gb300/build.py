@@ -23,7 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr",
           "-I", INCLUDE, "-I", CSRC]
 # FP64 reference-arithmetic units: no contraction into FMA.
-NO_FMAD = {"lbm_dense_f64.cu", "lbm_shifted.cu", "bgrid_lbm.cu", "poisson_f64.cu"}
+NO_FMAD = {"lbm_dense_f64.cu", "lbm_shifted.cu", "bgrid_lbm.cu", "poisson.cu"}
 
 
 def nvcc():

@@ -1,0 +1,626 @@
+// Poisson path: 7-point Laplacian, FP64-accumulated deterministic reductions
+// and a mixed-precision (Jacobi-)PCG whose scalars stay on the device.
+//
+// Compiled with --fmad=false: field updates are the IEEE operation sequence
+//   z = T(invdiag * r); p' = z + T(beta) * p; s = (-sum + n p'_c) * (1/h^2)
+//   x_lo += T(alpha) p'; r -= T(alpha) s
+// that the CPU oracle restates; reductions accumulate in double.
+//
+// Reductions: every CTA reduces its FP64 partial with warp shuffles and
+// shared memory and writes it to a per-CTA slot; the last CTA to take a
+// ticket (atomicAdd) sums the slots in CTA order and finalises the scalars.
+// No CTA ever waits on another (no spin loops), and the result does not
+// depend on which CTA finishes last.
+#include "common.cuh"
+#include <chrono>
+#include <random>
+#include <mutex>
+#include <vector>
+
+namespace ngb {
+namespace {
+
+constexpr int kBX = 256;  // threads per CTA (one row segment)
+
+int sm_count()
+{
+    static int sms = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    });
+    return sms;
+}
+
+struct Dom {
+    int32_t       nx, ny, nz, xchunks;
+    int64_t       segs;  // ny * nz * xchunks
+    double        h;
+    const int8_t* bd;
+};
+
+Dom make_dom(const ngb_poisson_desc* d)
+{
+    Dom g{};
+    g.nx = d->nx, g.ny = d->ny, g.nz = d->nz;
+    g.xchunks = (d->nx + kBX - 1) / kBX;
+    g.segs = int64_t(d->ny) * d->nz * g.xchunks;
+    g.h = d->h;
+    g.bd = d->bd;
+    return g;
+}
+
+int grid_for(int64_t segs) { return int(std::min<int64_t>(segs, int64_t(sm_count()) * 4)); }
+
+struct Cell {
+    int     x, y, z;
+    int64_t i;
+};
+
+// Segment -> cell of this thread (x = -1 when past the row end).
+__device__ __forceinline__ Cell seg_cell(const Dom& d, int64_t seg)
+{
+    const int64_t row = seg / d.xchunks;
+    const int     xc = int(seg - row * d.xchunks);
+    Cell          c;
+    c.x = xc * kBX + threadIdx.x;
+    c.y = int(row % d.ny);
+    c.z = int(row / d.ny);
+    c.i = c.x + int64_t(d.nx) * (c.y + int64_t(d.ny) * c.z);
+    if (c.x >= d.nx) c.x = -1;
+    return c;
+}
+
+__device__ __forceinline__ bool is_fixed(const Dom& d, int x, int y, int z, int64_t i)
+{
+    if (d.bd) return d.bd[i] == 0;
+    return x == 0 || y == 0 || z == 0 || x == d.nx - 1 || y == d.ny - 1 || z == d.nz - 1;
+}
+
+__device__ __forceinline__ int n_valid(const Dom& d, int x, int y, int z)
+{
+    return (x + 1 < d.nx) + (x > 0) + (y + 1 < d.ny) + (y > 0) + (z + 1 < d.nz) + (z > 0);
+}
+
+template <typename T>
+__device__ __forceinline__ T invdiag_of(const Dom& d, int x, int y, int z, int64_t i, int jacobi)
+{
+    if (!jacobi || is_fixed(d, x, y, z, i)) return T(1);
+    return T(d.h * d.h / double(n_valid(d, x, y, z)));
+}
+
+// Neighbour visitor in the oracle's order +x, -x, +y, -y, +z, -z.
+template <typename F>
+__device__ __forceinline__ void for_each_ngh(const Dom& d, int x, int y, int z, int64_t i, F f)
+{
+    const int64_t sy = d.nx, sz = int64_t(d.nx) * d.ny;
+    if (x + 1 < d.nx) f(x + 1, y, z, i + 1);
+    if (x > 0) f(x - 1, y, z, i - 1);
+    if (y + 1 < d.ny) f(x, y + 1, z, i + sy);
+    if (y > 0) f(x, y - 1, z, i - sy);
+    if (z + 1 < d.nz) f(x, y, z + 1, i + sz);
+    if (z > 0) f(x, y, z - 1, i - sz);
+}
+
+// ---------------------------------------------------------------- reductions
+template <int NS>
+__device__ __forceinline__ void cta_sum(double (&v)[NS], double (*sh)[kBX / 32])
+{
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        double a = v[k];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+            double a = threadIdx.x < kBX / 32 ? sh[k][threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            v[k] = a;  // valid in thread 0
+        }
+    }
+}
+
+// Writes this CTA's NS sums; returns true in the last CTA, whose thread 0
+// then holds in `out` the sums over all CTAs in CTA order.
+template <int NS>
+__device__ __forceinline__ bool grid_sum(double (&v)[NS], double* partials, unsigned int* ticket, double (&out)[NS])
+{
+    __shared__ double       sh[NS][kBX / 32];
+    __shared__ unsigned int t;
+    __shared__ double       fin[NS][kBX];
+    cta_sum<NS>(v, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NS; k++) partials[size_t(blockIdx.x) * NS + k] = v[k];
+        __threadfence();
+        t = atomicAdd(ticket, 1u);
+    }
+    __syncthreads();
+    if (t != gridDim.x - 1) return false;
+    __threadfence();
+    double acc[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) acc[k] = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += kBX)
+#pragma unroll
+        for (int k = 0; k < NS; k++) acc[k] += __ldcg(partials + size_t(b) * NS + k);
+#pragma unroll
+    for (int k = 0; k < NS; k++) fin[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int w = kBX / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+#pragma unroll
+            for (int k = 0; k < NS; k++) fin[k][threadIdx.x] += fin[k][threadIdx.x + w];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < NS; k++) out[k] = fin[k][0];
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+// ---------------------------------------------------------------- state
+struct CgState {
+    double       rz, rz_prev, pAp, alpha, rr, bnorm, rel, tol;
+    int32_t      iter, converged, refresh, refresh_every, max_iter, refreshes, last, jacobi;
+    unsigned int ticket;
+    unsigned int pad;
+};
+
+// ---------------------------------------------------------------- kernels
+template <typename T>
+__global__ void __launch_bounds__(kBX) laplacian_kernel(Dom d, const T* __restrict__ u, T* __restrict__ out)
+{
+    const T invh2 = T(1.0) / (T(d.h) * T(d.h));
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        const T uc = u[c.i];
+        if (is_fixed(d, c.x, c.y, c.z, c.i)) {
+            out[c.i] = uc;
+            continue;
+        }
+        T   sum = T(0);
+        int n = 0;
+        for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int, int, int, int64_t j) {
+            sum = sum + u[j];
+            n++;
+        });
+        out[c.i] = (-sum + T(n) * uc) * invh2;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBX) dot_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b, double* result,
+                                                  double* partials, unsigned int* ticket)
+{
+    double v[1] = {0.0};
+    for (int64_t i = int64_t(blockIdx.x) * kBX + threadIdx.x; i < n; i += int64_t(gridDim.x) * kBX)
+        v[0] += double(a[i]) * double(b[i]);
+    double out[1];
+    if (grid_sum<1>(v, partials, ticket, out) && threadIdx.x == 0) *result = out[0];
+}
+
+// r = T(b - A x_hi) (0 on Fixed rows); sums: |b|^2 over Free rows, r.z, |b - A x|^2.
+template <typename T>
+__global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const T* __restrict__ bvec, const double* __restrict__ xh,
+                                                      T* __restrict__ r, T* __restrict__ p, T* __restrict__ xlo,
+                                                      double* partials)
+{
+    const double invh2 = 1.0 / (d.h * d.h);
+    double       v[3] = {0.0, 0.0, 0.0};
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        double rt = 0.0;
+        if (!is_fixed(d, c.x, c.y, c.z, c.i)) {
+            double sum = 0.0;
+            int    n = 0;
+            for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int, int, int, int64_t j) {
+                sum = sum + xh[j];
+                n++;
+            });
+            const double ax = (-sum + double(n) * xh[c.i]) * invh2;
+            const double bb = double(bvec[c.i]);
+            rt = bb - ax;
+            v[0] += bb * bb;
+        }
+        const T rc = T(rt);
+        r[c.i] = rc;
+        p[c.i] = T(0);
+        xlo[c.i] = T(0);
+        v[1] += double(rc) * double(T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, st->jacobi) * rc));
+        v[2] += rt * rt;
+    }
+    double out[3];
+    if (grid_sum<3>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
+        st->bnorm = sqrt(out[0]);
+        st->rz = out[1];
+        st->rz_prev = 0.0;
+        st->rel = st->bnorm > 0 ? sqrt(out[2]) / st->bnorm : 0.0;
+        st->iter = 0;
+        st->refreshes = 0;
+        st->refresh = 0;
+        st->last = 0;
+        st->converged = (st->bnorm == 0.0 || st->rel <= st->tol) ? 1 : 0;
+    }
+}
+
+// pass A: beta from device scalars; p' = z + beta p at the cell and its
+// neighbours; s = A p'; pAp = <p', s>; alpha = rz / pAp.
+template <typename T>
+__global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, const T* __restrict__ r, const T* __restrict__ p_old,
+                                                        T* __restrict__ p_new, T* __restrict__ s, double* partials)
+{
+    if (st->converged) return;
+    const int    jac = st->jacobi;
+    const double beta = st->rz_prev == 0.0 ? 0.0 : st->rz / st->rz_prev;
+    const T      tb = T(beta);
+    const T      invh2 = T(1.0) / (T(d.h) * T(d.h));
+    double       v[1] = {0.0};
+    auto         pn = [&](int x, int y, int z, int64_t j) -> T { return T(invdiag_of<T>(d, x, y, z, j, jac) * r[j]) + tb * p_old[j]; };
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        const T pc = pn(c.x, c.y, c.z, c.i);
+        T       sc;
+        if (is_fixed(d, c.x, c.y, c.z, c.i)) {
+            sc = pc;
+        } else {
+            T   sum = T(0);
+            int n = 0;
+            for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int x, int y, int z, int64_t j) {
+                sum = sum + pn(x, y, z, j);
+                n++;
+            });
+            sc = (-sum + T(n) * pc) * invh2;
+        }
+        p_new[c.i] = pc;
+        s[c.i] = sc;
+        v[0] += double(pc) * double(sc);
+    }
+    double out[1];
+    if (grid_sum<1>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
+        st->pAp = out[0];
+        st->alpha = st->rz / out[0];
+    }
+}
+
+// pass B: x_lo += alpha p; r -= alpha s; rz' = <r, z>; rr = <r, r>.
+template <typename T>
+__global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* __restrict__ xlo, const T* __restrict__ p,
+                                                        T* __restrict__ r, const T* __restrict__ s, double* partials)
+{
+    if (st->converged) return;
+    const int jac = st->jacobi;
+    const T   ta = T(st->alpha);
+    double    v[2] = {0.0, 0.0};
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        xlo[c.i] = xlo[c.i] + ta * p[c.i];
+        const T rn = r[c.i] - ta * s[c.i];
+        r[c.i] = rn;
+        const T z = T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, jac) * rn);
+        v[0] += double(rn) * double(z);
+        v[1] += double(rn) * double(rn);
+    }
+    double out[2];
+    if (grid_sum<2>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
+        st->rz_prev = st->rz;
+        st->rz = out[0];
+        st->rr = out[1];
+        st->iter += 1;
+        const bool want = (st->iter % st->refresh_every == 0) || (sqrt(out[1]) / st->bnorm <= st->tol);
+        st->last = st->iter >= st->max_iter ? 1 : 0;
+        st->refresh = (want || st->last) ? 1 : 0;
+    }
+}
+
+// refresh, part 1: x_hi += x_lo; x_lo = 0.
+template <typename T>
+__global__ void __launch_bounds__(kBX) cg_refresh1_kernel(Dom d, const CgState* st, double* __restrict__ xh, T* __restrict__ xlo)
+{
+    if (st->converged || !st->refresh) return;
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        xh[c.i] = xh[c.i] + double(xlo[c.i]);
+        xlo[c.i] = T(0);
+    }
+}
+
+// refresh, part 2: r = T(b - A x_hi); rz = <r, z>; true relative residual.
+template <typename T>
+__global__ void __launch_bounds__(kBX) cg_refresh2_kernel(Dom d, CgState* st, const T* __restrict__ bvec,
+                                                          const double* __restrict__ xh, T* __restrict__ r, double* partials)
+{
+    if (st->converged || !st->refresh) return;
+    const double invh2 = 1.0 / (d.h * d.h);
+    const int    jac = st->jacobi;
+    double       v[2] = {0.0, 0.0};
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        double rt = 0.0;
+        if (!is_fixed(d, c.x, c.y, c.z, c.i)) {
+            double sum = 0.0;
+            int    n = 0;
+            for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int, int, int, int64_t j) {
+                sum = sum + xh[j];
+                n++;
+            });
+            rt = double(bvec[c.i]) - (-sum + double(n) * xh[c.i]) * invh2;
+        }
+        const T rc = T(rt);
+        r[c.i] = rc;
+        v[0] += double(rc) * double(T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, jac) * rc));
+        v[1] += rt * rt;
+    }
+    double out[2];
+    if (grid_sum<2>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
+        st->rz = out[0];
+        st->rel = sqrt(out[1]) / st->bnorm;
+        st->refreshes += 1;
+        st->refresh = 0;
+        if (st->rel <= st->tol)
+            st->converged = 1;
+        else if (st->last)
+            st->converged = 2;
+    }
+}
+
+__global__ void rhs_kernel(Dom d, int field, const double* __restrict__ centres, const double* __restrict__ amps, double sigma,
+                           void* f)
+{
+    const double inv2s2 = 1.0 / (2.0 * sigma * sigma);
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        double v = 0.0;
+        for (int k = 0; k < 8; k++) {
+            const double dx = c.x - centres[3 * k], dy = c.y - centres[3 * k + 1], dz = c.z - centres[3 * k + 2];
+            v += amps[k] * exp(-(dx * dx + dy * dy + dz * dz) * inv2s2);
+        }
+        if (field == NGB_STORE_F64)
+            static_cast<double*>(f)[c.i] = v;
+        else
+            static_cast<float*>(f)[c.i] = float(v);
+    }
+}
+
+// ---------------------------------------------------------------- host helpers
+int validate(const ngb_poisson_desc* d)
+{
+    NGB_CHECK_ARG(d, "desc is NULL");
+    NGB_CHECK_ARG(d->nx >= 1 && d->ny >= 1 && d->nz >= 1, "dims must be positive");
+    NGB_CHECK_ARG(d->field == NGB_STORE_F32 || d->field == NGB_STORE_F64, "field must be NGB_STORE_F32 or NGB_STORE_F64");
+    NGB_CHECK_ARG(d->h > 0, "h must be positive");
+    return NGB_OK;
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct Workspace {
+    CgState* st;
+    double*  partials;
+    void *   r, *p0, *p1, *s, *xlo;
+    size_t   bytes;
+};
+
+Workspace layout(const ngb_poisson_desc* d, void* base)
+{
+    const size_t V = size_t(d->nx) * d->ny * d->nz;
+    const size_t esz = d->field == NGB_STORE_F64 ? 8 : 4;
+    const int    grid = grid_for(make_dom(d).segs);
+    Workspace    w{};
+    char*        p = static_cast<char*>(base);
+    size_t       off = 0;
+    w.st = reinterpret_cast<CgState*>(p + off);
+    off += align256(sizeof(CgState));
+    w.partials = reinterpret_cast<double*>(p + off);
+    off += align256(size_t(grid) * 3 * sizeof(double));
+    void** fields[5] = {&w.r, &w.p0, &w.p1, &w.s, &w.xlo};
+    for (auto f : fields) {
+        *f = p + off;
+        off += align256(V * esz);
+    }
+    w.bytes = off;
+    return w;
+}
+
+template <typename T>
+int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace& w, const ngb_cg_params* prm,
+            ngb_cg_result* res, cudaStream_t s)
+{
+    const Dom d = make_dom(desc);
+    const int grid = grid_for(d.segs);
+    CgState   init{};
+    init.tol = prm->tol;
+    init.refresh_every = prm->refresh_every;
+    init.max_iter = prm->max_iter;
+    init.jacobi = prm->jacobi ? 1 : 0;
+    NGB_CUDA_TRY(cudaMemcpyAsync(w.st, &init, sizeof(CgState), cudaMemcpyHostToDevice, s));
+    T *r = static_cast<T*>(w.r), *p0 = static_cast<T*>(w.p0), *p1 = static_cast<T*>(w.p1), *sv = static_cast<T*>(w.s),
+      *xlo = static_cast<T*>(w.xlo);
+    const auto t0 = std::chrono::steady_clock::now();
+    cg_init_kernel<T><<<grid, kBX, 0, s>>>(d, w.st, b, x, r, p0, xlo, w.partials);
+    NGB_LAUNCH_CHECK("cg_init_kernel");
+    NGB_CUDA_TRY(cudaMemsetAsync(p1, 0, size_t(desc->nx) * desc->ny * desc->nz * sizeof(T), s));
+
+    // Capture `check_every` iterations (rounded up to even: p ping-pongs) once.
+    const int    per = std::max(2, (prm->check_every + 1) / 2 * 2);
+    cudaStream_t cs;
+    NGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int it = 0; it < per; it++) {
+            T* pa = (it % 2 == 0) ? p0 : p1;
+            T* pb = (it % 2 == 0) ? p1 : p0;
+            cg_pass_a_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
+            cg_pass_b_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
+            cg_refresh1_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, x, xlo);
+            cg_refresh2_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, b, x, r, w.partials);
+        }
+        e = cudaStreamEndCapture(cs, &graph);
+    }
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        set_error("CG graph capture failed: %s", cudaGetErrorString(e));
+        return NGB_ERR_CUDA;
+    }
+    cudaGraphExec_t exec;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_error("CG graph instantiate failed: %s", cudaGetErrorString(e));
+        return NGB_ERR_CUDA;
+    }
+    int32_t* flag = nullptr;
+    e = cudaMallocHost(&flag, sizeof(int32_t));
+    if (e != cudaSuccess) {
+        cudaGraphExecDestroy(exec);
+        set_error("cudaMallocHost failed: %s", cudaGetErrorString(e));
+        return NGB_ERR_CUDA;
+    }
+    int rc = NGB_OK;
+    const int max_launches = (prm->max_iter + per - 1) / per + 1;
+    for (int l = 0; l <= max_launches; l++) {
+        e = cudaMemcpyAsync(flag, &w.st->converged, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("CG poll failed: %s", cudaGetErrorString(e));
+            rc = NGB_ERR_CUDA;
+            break;
+        }
+        if (*flag) break;
+        e = cudaGraphLaunch(exec, s);
+        if (e != cudaSuccess) {
+            set_error("CG graph launch failed: %s", cudaGetErrorString(e));
+            rc = NGB_ERR_CUDA;
+            break;
+        }
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    cudaFreeHost(flag);
+    cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    CgState out;
+    NGB_CUDA_TRY(cudaMemcpyAsync(&out, w.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+    NGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (res) {
+        res->iterations = out.iter;
+        res->converged = out.converged == 1;
+        res->refreshes = out.refreshes;
+        res->rel_residual = out.rel;
+        res->seconds = std::chrono::duration<double>(t1 - t0).count();
+    }
+    return NGB_OK;
+}
+
+}  // namespace
+}  // namespace ngb
+
+using namespace ngb;
+
+extern "C" {
+
+int ngb_laplacian_apply(const ngb_poisson_desc* d, const void* u, void* out, void* stream)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(u && out && u != out, "u/out must be distinct non-NULL device pointers");
+    const Dom dom = make_dom(d);
+    const int grid = grid_for(dom.segs);
+    if (d->field == NGB_STORE_F64)
+        laplacian_kernel<double><<<grid, kBX, 0, as_stream(stream)>>>(dom, static_cast<const double*>(u), static_cast<double*>(out));
+    else
+        laplacian_kernel<float><<<grid, kBX, 0, as_stream(stream)>>>(dom, static_cast<const float*>(u), static_cast<float*>(out));
+    NGB_LAUNCH_CHECK("laplacian_kernel");
+    return NGB_OK;
+}
+
+size_t ngb_dot_scratch_doubles(int64_t n)
+{
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + kBX - 1) / kBX, int64_t(sm_count()) * 4));
+    return size_t(blocks) + 1;  // partials + one slot for the ticket
+}
+
+int ngb_dot(int64_t n, int32_t field, const void* a, const void* b, double* result, double* scratch, void* stream)
+{
+    NGB_CHECK_ARG(n >= 0, "n < 0");
+    NGB_CHECK_ARG(field == NGB_STORE_F32 || field == NGB_STORE_F64, "field must be F32 or F64");
+    NGB_CHECK_ARG(result && scratch && (n == 0 || (a && b)), "NULL argument");
+    cudaStream_t s = as_stream(stream);
+    if (n == 0) {
+        NGB_CUDA_TRY(cudaMemsetAsync(result, 0, sizeof(double), s));
+        return NGB_OK;
+    }
+    const int     blocks = int(ngb_dot_scratch_doubles(n) - 1);
+    unsigned int* ticket = reinterpret_cast<unsigned int*>(scratch + blocks);
+    NGB_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
+    if (field == NGB_STORE_F64)
+        dot_kernel<double><<<blocks, kBX, 0, s>>>(n, static_cast<const double*>(a), static_cast<const double*>(b), result, scratch,
+                                                  ticket);
+    else
+        dot_kernel<float><<<blocks, kBX, 0, s>>>(n, static_cast<const float*>(a), static_cast<const float*>(b), result, scratch,
+                                                 ticket);
+    NGB_LAUNCH_CHECK("dot_kernel");
+    return NGB_OK;
+}
+
+size_t ngb_cg_workspace_bytes(const ngb_poisson_desc* d)
+{
+    if (validate(d)) return 0;
+    return layout(d, nullptr).bytes;
+}
+
+int ngb_cg_solve(const ngb_poisson_desc* d, const void* b, double* x, void* workspace, size_t workspace_bytes,
+                 const ngb_cg_params* prm, ngb_cg_result* res, void* stream)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(b && x && workspace && prm, "NULL argument");
+    NGB_CHECK_ARG(prm->refresh_every >= 1 && prm->check_every >= 1 && prm->max_iter >= 0, "bad CG params");
+    NGB_CHECK_ARG(prm->tol >= 0, "tol < 0");
+    NGB_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, "workspace must be 256-byte aligned");
+    const Workspace w = layout(d, workspace);
+    NGB_CHECK_ARG(workspace_bytes >= w.bytes, "workspace too small (%zu < %zu)", workspace_bytes, w.bytes);
+    NGB_CUDA_TRY(cudaMemsetAsync(&w.st->ticket, 0, sizeof(unsigned int), as_stream(stream)));
+    if (d->field == NGB_STORE_F64) return solve_t<double>(d, static_cast<const double*>(b), x, w, prm, res, as_stream(stream));
+    return solve_t<float>(d, static_cast<const float*>(b), x, w, prm, res, as_stream(stream));
+}
+
+int ngb_poisson_rhs(const ngb_poisson_desc* d, const double* centres, const double* amps, double sigma, void* f, void* stream)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(centres && amps && f && sigma > 0, "bad argument");
+    const Dom dom = make_dom(d);
+    rhs_kernel<<<grid_for(dom.segs), kBX, 0, as_stream(stream)>>>(dom, d->field, centres, amps, sigma, f);
+    NGB_LAUNCH_CHECK("rhs_kernel");
+    return NGB_OK;
+}
+
+int ngb_gaussian_sources(int32_t nx, int32_t ny, int32_t nz, uint64_t seed, double* centres, double* amps)
+{
+    NGB_CHECK_ARG(centres && amps && nx > 0 && ny > 0 && nz > 0, "bad argument");
+    std::mt19937_64 g(seed);
+    auto            u01 = [&]() { return double(g() >> 11) * (1.0 / 9007199254740992.0); };
+    for (int k = 0; k < 8; k++) {
+        centres[3 * k + 0] = nx / 8.0 + u01() * (0.75 * nx);
+        centres[3 * k + 1] = ny / 8.0 + u01() * (0.75 * ny);
+        centres[3 * k + 2] = nz / 8.0 + u01() * (0.75 * nz);
+        amps[k] = 2.0 * u01() - 1.0;
+    }
+    return NGB_OK;
+}
+
+}  // extern "C"

@@ -73,7 +73,7 @@ def lib():
         L.orc_laplacian_f32.argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]
         for f in ("orc_pcg_f32", "orc_pcg_f64"):
             getattr(L, f).argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p, c_double,
-                                      c_int, c_int, c_void_p]
+                                      c_int, c_int, c_void_p, c_int]
         L.orc_reference_cg_f64.argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p, c_int]
         L.orc_reference_cg_f64.restype = c_double
         L.orc_reference_cg_f32.argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p, c_int]

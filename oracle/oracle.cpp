@@ -374,9 +374,9 @@ int orc_laplacian_f32(int nx, int ny, int nz, double h, const float* u, const in
 // Mixed-precision Jacobi-PCG (the GPU algorithm). result[0] = iterations,
 // result[1] = converged, result[2] = relative true residual, result[3] = refreshes.
 int orc_pcg_f32(int nx, int ny, int nz, double h, const int8_t* bd, const float* b, double* x, double tol, int max_iter,
-                int refresh_every, double* result)
+                int refresh_every, double* result, int jacobi)
 {
-    PcgOracle<float> s(nx, ny, nz, h, bd);
+    PcgOracle<float> s(nx, ny, nz, h, bd, jacobi != 0);
     PcgResult        r = s.solve(b, x, tol, max_iter, refresh_every);
     result[0] = r.iterations;
     result[1] = r.converged;
@@ -385,9 +385,9 @@ int orc_pcg_f32(int nx, int ny, int nz, double h, const int8_t* bd, const float*
     return 0;
 }
 int orc_pcg_f64(int nx, int ny, int nz, double h, const int8_t* bd, const double* b, double* x, double tol, int max_iter,
-                int refresh_every, double* result)
+                int refresh_every, double* result, int jacobi)
 {
-    PcgOracle<double> s(nx, ny, nz, h, bd);
+    PcgOracle<double> s(nx, ny, nz, h, bd, jacobi != 0);
     PcgResult         r = s.solve(b, x, tol, max_iter, refresh_every);
     result[0] = r.iterations;
     result[1] = r.converged;

@@ -137,7 +137,7 @@ struct PcgOracle {
     std::vector<int8_t> bd;
     std::vector<T>      invdiag;
 
-    PcgOracle(int nx_, int ny_, int nz_, double h_, const int8_t* bd_) : nx(nx_), ny(ny_), nz(nz_), h(h_), bd(bd_, bd_ + size_t(nx_) * ny_ * nz_)
+    PcgOracle(int nx_, int ny_, int nz_, double h_, const int8_t* bd_, bool jacobi = true) : nx(nx_), ny(ny_), nz(nz_), h(h_), bd(bd_, bd_ + size_t(nx_) * ny_ * nz_)
     {
         invdiag.resize(bd.size());
         static const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
@@ -145,7 +145,7 @@ struct PcgOracle {
             for (int y = 0; y < ny; y++)
                 for (int x = 0; x < nx; x++) {
                     const size_t i = plin(x, y, z, nx, ny);
-                    if (bd[i] == Fixed) {
+                    if (bd[i] == Fixed || !jacobi) {
                         invdiag[i] = T(1);
                         continue;
                     }
@@ -211,7 +211,8 @@ struct PcgOracle {
             rz_prev = rz;
             rz = rz_new;
             res.iterations = it + 1;
-            const bool want = ((it + 1) % refresh_every == 0) || (std::sqrt(rr) / bnorm <= tol);
+            const bool last = (it + 1) >= max_iter;
+            const bool want = ((it + 1) % refresh_every == 0) || (std::sqrt(rr) / bnorm <= tol) || last;
             if (want) {
                 res.refreshes++;
                 for (size_t i = 0; i < V; i++) {

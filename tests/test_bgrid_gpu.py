@@ -148,7 +148,7 @@ def test_bgrid_lbm_sphere_bit_exact(ngb, orc, cuda, q, storage):
         dense = np.zeros((q, V), np.uint16)  # g = 0
         dt = np.uint16
     steps = 40
-    a = np.ascontiguousarray(dense.ravel())
+    a = dense.ravel().copy()  # the oracle runs in place: keep `dense` as the initial state
     b = a.copy()
     wall = np.zeros((4, 27))
     wall[1, :q] = [float(np.float32(t)) if storage else t for t in terms]
