@@ -254,6 +254,20 @@ size_t ngb_dot_scratch_doubles(int64_t n);
  * (dGrid::dot, dGrid_imp.h:254-281; ReduceKernels.cuh:7-76 compiled out). */
 int ngb_dot(int64_t n, int32_t field, const void* a, const void* b, double* result, double* scratch, void* stream);
 
+/* Allocation-free form of ngb_dot (no counterpart in the reference): for
+ * callers that cannot allocate device memory where they need the reduction
+ * (between launches of a stream-ordered pipeline, where cudaMalloc would
+ * synchronise the device, or in a host plug-in whose device memory the host
+ * application owns). Same FP64-accumulated, run-to-run deterministic result
+ * as ngb_dot up to summation order; the per-CTA partials live in a fixed
+ * 256 KiB array inside this library (held on every GPU that loads it until
+ * exit), so n is limited to 2^28 elements (NGB_ERR_RANGE beyond). Calls no
+ * cudaMalloc/cudaFree. The first call on a device looks up the array's
+ * device address (make it before any stream capture on that device). All
+ * calls share the array: calls whose kernels overlap on the GPU race. */
+#define NGB_DOT_NOALLOC_MAX_N (268435456LL)
+int ngb_dot_noalloc(int64_t n, int32_t field, const void* a, const void* b, double* result, void* stream);
+
 typedef struct ngb_cg_params {
     double  tol;           /* stop when |b - A x| / |b| <= tol (true residual, FP64) */
     int32_t max_iter;
