@@ -1,0 +1,4 @@
+// All grids of the GB300 Neon API (one partition, one GPU).
+#pragma once
+#include "Neon/domain/bGrid.h"
+#include "Neon/domain/dGrid.h"
