@@ -33,6 +33,24 @@ __device__ __forceinline__ uint32_t bgrid_ngh(const uint32_t* __restrict__ conn,
     return nb;
 }
 
+// As bgrid_ngh, with this block's 27 connectivity entries already in `sconn`
+// (shared memory): no dependent global load on the neighbour path.
+__device__ __forceinline__ uint32_t bgrid_ngh_local(const uint32_t* sconn, uint32_t b, int i, int j, int k, int ox, int oy, int oz,
+                                                    int& v)
+{
+    int       ni = i + ox, nj = j + oy, nk = k + oz;
+    const int fx = ni < 0 ? -1 : (ni >= 8 ? 1 : 0);
+    const int fy = nj < 0 ? -1 : (nj >= 8 ? 1 : 0);
+    const int fz = nk < 0 ? -1 : (nk >= 8 ? 1 : 0);
+    uint32_t  nb = b;
+    if (fx | fy | fz) {
+        ni -= 8 * fx, nj -= 8 * fy, nk -= 8 * fz;
+        nb = sconn[(fx + 1) + 3 * (fy + 1) + 9 * (fz + 1)];
+    }
+    v = ni + 8 * nj + 64 * nk;
+    return nb;
+}
+
 // Valid neighbour = block exists and voxel active (bPartition_imp.h:109-124).
 __device__ __forceinline__ bool bgrid_valid_ngh(const uint32_t* __restrict__ mask, const uint32_t* __restrict__ conn, uint32_t b,
                                                 int i, int j, int k, int ox, int oy, int oz, uint32_t& nb, int& v)

@@ -55,11 +55,14 @@ __global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __rest
                                                                  BParams<typename std::conditional<F64, double, float>::type> p)
 {
     using L = Lattice<Q>;
-    const uint32_t b = blockIdx.x;
-    const int      v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
+    const uint32_t      b = blockIdx.x;
+    const int           v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
+    __shared__ uint32_t sconn[27];  // this block's neighbour blocks
+    if (v < 27) sconn[v] = __ldg(p.conn + size_t(b) * 27 + v);
     const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
-    const int      cls = flag_class(f);
-    const size_t   bq = size_t(b) * Q;
+    __syncthreads();
+    const int    cls = flag_class(f);
+    const size_t bq = size_t(b) * Q;
     if (cls == NGB_CELL_OUTLET) {  // zero-gradient outflow: copy the x-1 neighbour
         uint32_t nb;
         int      nv;
@@ -85,7 +88,7 @@ __global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __rest
                 pop[q] = __ldg(fin + (bq + q) * kBlockVoxels + v - L::cx(q) - 8 * L::cy(q) - 64 * L::cz(q));
             } else {
                 int            nv;
-                const uint32_t nb = bgrid_ngh(p.conn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
+                const uint32_t nb = bgrid_ngh_local(sconn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
                 pop[q] = __ldg(fin + (size_t(nb) * Q + q) * kBlockVoxels + nv);
             }
         }
@@ -106,7 +109,7 @@ __global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __rest
                                         float(L::w(q)));
             } else {
                 int            nv;
-                const uint32_t nb = bgrid_ngh(p.conn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
+                const uint32_t nb = bgrid_ngh_local(sconn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
                 g[q] = PairIO<S>::to_g1(__ldg(fin + (size_t(nb) * Q + q) * kBlockVoxels + nv), float(L::w(q)));
             }
         }

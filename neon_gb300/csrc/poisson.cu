@@ -39,6 +39,35 @@ struct Dom {
     int64_t       segs;  // ny * nz * xchunks
     double        h;
     const int8_t* bd;
+    double        invd[7];  // h^2 / n for n valid neighbours (host-computed: no division on the device)
+};
+
+// Dot-product accumulator of one thread. For FP32 operands the exact product
+// (Dekker's TwoProduct via fma) is accumulated with Knuth's TwoSum in a float
+// pair, about 48 significant bits, without occupying GB300's FP64 pipe; the
+// pair becomes a double at the CTA reduction. FP64 operands accumulate in FP64.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<float> {
+    float                      s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float a, float b)
+    {
+        const float p = a * b;
+        const float e = __fmaf_rn(a, b, -p);
+        const float t = s + p;
+        const float bp = t - s;
+        const float err = (s - (t - bp)) + (p - bp);
+        s = t;
+        c = c + (err + e);
+    }
+    __device__ __forceinline__ double value() const { return double(s) + double(c); }
+};
+template <>
+struct DotAcc<double> {
+    double                     s = 0.0;
+    __device__ __forceinline__ void   add(double a, double b) { s += a * b; }
+    __device__ __forceinline__ double value() const { return s; }
 };
 
 Dom make_dom(const ngb_poisson_desc* d)
@@ -49,6 +78,8 @@ Dom make_dom(const ngb_poisson_desc* d)
     g.segs = int64_t(d->ny) * d->nz * g.xchunks;
     g.h = d->h;
     g.bd = d->bd;
+    g.invd[0] = 1.0;
+    for (int n = 1; n <= 6; n++) g.invd[n] = d->h * d->h / double(n);
     return g;
 }
 
@@ -88,7 +119,7 @@ template <typename T>
 __device__ __forceinline__ T invdiag_of(const Dom& d, int x, int y, int z, int64_t i, int jacobi)
 {
     if (!jacobi || is_fixed(d, x, y, z, i)) return T(1);
-    return T(d.h * d.h / double(n_valid(d, x, y, z)));
+    return T(d.invd[n_valid(d, x, y, z)]);
 }
 
 // Neighbour visitor in the oracle's order +x, -x, +y, -y, +z, -z.
@@ -199,9 +230,9 @@ template <typename T>
 __global__ void __launch_bounds__(kBX) dot_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b, double* result,
                                                   double* partials, unsigned int* ticket)
 {
-    double v[1] = {0.0};
-    for (int64_t i = int64_t(blockIdx.x) * kBX + threadIdx.x; i < n; i += int64_t(gridDim.x) * kBX)
-        v[0] += double(a[i]) * double(b[i]);
+    DotAcc<T> acc;
+    for (int64_t i = int64_t(blockIdx.x) * kBX + threadIdx.x; i < n; i += int64_t(gridDim.x) * kBX) acc.add(a[i], b[i]);
+    double v[1] = {acc.value()};
     double out[1];
     if (grid_sum<1>(v, partials, ticket, out) && threadIdx.x == 0) *result = out[0];
 }
@@ -214,6 +245,7 @@ __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const 
 {
     const double invh2 = 1.0 / (d.h * d.h);
     double       v[3] = {0.0, 0.0, 0.0};
+    DotAcc<T>    bacc, rzacc;
     for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
         const Cell c = seg_cell(d, seg);
         if (c.x < 0) continue;
@@ -226,17 +258,18 @@ __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const 
                 n++;
             });
             const double ax = (-sum + double(n) * xh[c.i]) * invh2;
-            const double bb = double(bvec[c.i]);
-            rt = bb - ax;
-            v[0] += bb * bb;
+            rt = double(bvec[c.i]) - ax;
+            bacc.add(bvec[c.i], bvec[c.i]);
         }
         const T rc = T(rt);
         r[c.i] = rc;
         p[c.i] = T(0);
         xlo[c.i] = T(0);
-        v[1] += double(rc) * double(T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, st->jacobi) * rc));
+        rzacc.add(rc, T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, st->jacobi) * rc));
         v[2] += rt * rt;
     }
+    v[0] = bacc.value();
+    v[1] = rzacc.value();
     double out[3];
     if (grid_sum<3>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
         st->bnorm = sqrt(out[0]);
@@ -262,7 +295,7 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     const double beta = st->rz_prev == 0.0 ? 0.0 : st->rz / st->rz_prev;
     const T      tb = T(beta);
     const T      invh2 = T(1.0) / (T(d.h) * T(d.h));
-    double       v[1] = {0.0};
+    DotAcc<T>    acc;
     auto         pn = [&](int x, int y, int z, int64_t j) -> T { return T(invdiag_of<T>(d, x, y, z, j, jac) * r[j]) + tb * p_old[j]; };
     for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
         const Cell c = seg_cell(d, seg);
@@ -282,8 +315,9 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
         }
         p_new[c.i] = pc;
         s[c.i] = sc;
-        v[0] += double(pc) * double(sc);
+        acc.add(pc, sc);
     }
+    double v[1] = {acc.value()};
     double out[1];
     if (grid_sum<1>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
         st->pAp = out[0];
@@ -299,7 +333,7 @@ __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* _
     if (st->converged) return;
     const int jac = st->jacobi;
     const T   ta = T(st->alpha);
-    double    v[2] = {0.0, 0.0};
+    DotAcc<T> a0, a1;
     for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
         const Cell c = seg_cell(d, seg);
         if (c.x < 0) continue;
@@ -307,9 +341,10 @@ __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* _
         const T rn = r[c.i] - ta * s[c.i];
         r[c.i] = rn;
         const T z = T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, jac) * rn);
-        v[0] += double(rn) * double(z);
-        v[1] += double(rn) * double(rn);
+        a0.add(rn, z);
+        a1.add(rn, rn);
     }
+    double v[2] = {a0.value(), a1.value()};
     double out[2];
     if (grid_sum<2>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
         st->rz_prev = st->rz;
@@ -344,6 +379,7 @@ __global__ void __launch_bounds__(kBX) cg_refresh2_kernel(Dom d, CgState* st, co
     const double invh2 = 1.0 / (d.h * d.h);
     const int    jac = st->jacobi;
     double       v[2] = {0.0, 0.0};
+    DotAcc<T>    rzacc;
     for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
         const Cell c = seg_cell(d, seg);
         if (c.x < 0) continue;
@@ -359,9 +395,10 @@ __global__ void __launch_bounds__(kBX) cg_refresh2_kernel(Dom d, CgState* st, co
         }
         const T rc = T(rt);
         r[c.i] = rc;
-        v[0] += double(rc) * double(T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, jac) * rc));
+        rzacc.add(rc, T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, jac) * rc));
         v[1] += rt * rt;
     }
+    v[0] = rzacc.value();
     double out[2];
     if (grid_sum<2>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
         st->rz = out[0];
