@@ -310,6 +310,44 @@ int ngb_poisson_rhs(const ngb_poisson_desc* desc, const double* centres, const d
  * uniform in [-1, 1), from std::mt19937_64(seed) 53-bit uniforms (host). */
 int ngb_gaussian_sources(int32_t nx, int32_t ny, int32_t nz, uint64_t seed, double* centres, double* amps);
 
+/* ------------------------------------------------------------------------
+ * Learned preconditioner: kernels of a small 3-D U-Net (no reference
+ * counterpart; the reference has no learned solver). Tensors are BF16 or FP32,
+ * channels-last on an nx*ny*nz grid: element (voxel v, channel c) at v*ld + c.
+ * ---------------------------------------------------------------------- */
+
+/* 3x3x3 convolution with zero padding as an implicit GEMM on the tensor cores
+ * (BF16 operands, FP32 accumulation): y[v][co] = act(sum_{t,ci} x[v+t][ci] w[co][t][ci] + bias[co]).
+ * cin % 16 == 0; cout in {8, 16, 32, 48, 64}; w is [cout][27][cin] BF16
+ * (t = 9(dz+1) + 3(dy+1) + (dx+1)); bias FP32 or NULL. out_f32 = 0: BF16
+ * output with optional ReLU; 1: FP32 output, optionally added to y. */
+int ngb_conv3d(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* w, const float* bias,
+               void* y, int32_t ldy, int32_t cout, int32_t out_f32, int32_t relu, int32_t accumulate, void* stream);
+
+/* dw[co][t][ci] += sum_v dy[v][co] x[v+t][ci] (BF16 inputs, FP32 dw). */
+int ngb_conv3d_bwd_weight(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy, int32_t lddy,
+                          int32_t cout, float* dw, void* stream);
+
+/* out = BF16(dy * (y > 0)) (ReLU backward; y NULL: no mask). */
+int ngb_relu_bwd(int64_t V, int32_t C, const float* dy, int32_t lddy, const void* y, int32_t ldy, void* out, int32_t ldo, void* stream);
+
+/* 2x2x2 average pooling (BF16) of an even fine grid and its adjoint (FP32, optionally accumulated). */
+int ngb_pool2(int32_t nx, int32_t ny, int32_t nz, int32_t C, const void* x, int32_t ldx, void* y, int32_t ldy, void* stream);
+int ngb_pool2_bwd(int32_t nx, int32_t ny, int32_t nz, int32_t C, const float* dy, int32_t lddy, float* dx, int32_t lddx,
+                  int32_t accumulate, void* stream);
+
+/* Nearest 2x upsampling to the fine grid (BF16) and its adjoint (FP32). */
+int ngb_up2(int32_t nx, int32_t ny, int32_t nz, int32_t C, const void* x, int32_t ldx, void* y, int32_t ldy, void* stream);
+int ngb_up2_bwd(int32_t nx, int32_t ny, int32_t nz, int32_t C, const float* dy, int32_t lddy, float* dx, int32_t lddx, void* stream);
+
+/* Adam step on FP32 master weights (bias-corrected with `step`), writing the
+ * BF16 copy `pb` if non-NULL. */
+int ngb_adam(int64_t n, float* p, const float* g, float* m, float* s, float lr, float b1, float b2, float eps, int32_t step, void* pb,
+             void* stream);
+
+/* wt[ci][26 - t][co] = BF16(w[co][t][ci]): weights of the backward-data convolution. */
+int ngb_flip_weights(int32_t cout, int32_t cin, const float* w, void* wt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

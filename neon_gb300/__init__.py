@@ -122,6 +122,17 @@ _EXTRA_SIGNATURES.update({
                      ctypes.c_int),
     "ngb_poisson_rhs": ([_pd, _vp, _vp, _dbl, _vp, _vp], ctypes.c_int),
     "ngb_gaussian_sources": ([_i32, _i32, _i32, ctypes.c_uint64, _vp, _vp], ctypes.c_int),
+    "ngb_dot_noalloc": ([ctypes.c_int64, _i32, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_conv3d": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
+    "ngb_conv3d_bwd_weight": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp, _i32, _i32, _vp, _vp], ctypes.c_int),
+    "ngb_relu_bwd": ([ctypes.c_int64, _i32, _vp, _i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
+    "ngb_pool2": ([_i32, _i32, _i32, _i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
+    "ngb_pool2_bwd": ([_i32, _i32, _i32, _i32, _vp, _i32, _vp, _i32, _i32, _vp], ctypes.c_int),
+    "ngb_up2": ([_i32, _i32, _i32, _i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
+    "ngb_up2_bwd": ([_i32, _i32, _i32, _i32, _vp, _i32, _vp, _i32, _vp], ctypes.c_int),
+    "ngb_adam": ([ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                  _i32, _vp, _vp], ctypes.c_int),
+    "ngb_flip_weights": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
 })
 
 

@@ -40,6 +40,7 @@ struct Dom {
     double        h;
     const int8_t* bd;
     double        invd[7];  // h^2 / n for n valid neighbours (host-computed: no division on the device)
+    float         invf[7];  // the same, rounded to float (no FP64 conversion on the device)
 };
 
 // Dot-product accumulator of one thread. For FP32 operands the exact product
@@ -80,6 +81,7 @@ Dom make_dom(const ngb_poisson_desc* d)
     g.bd = d->bd;
     g.invd[0] = 1.0;
     for (int n = 1; n <= 6; n++) g.invd[n] = d->h * d->h / double(n);
+    for (int n = 0; n <= 6; n++) g.invf[n] = float(g.invd[n]);
     return g;
 }
 
@@ -93,12 +95,15 @@ struct Cell {
 // Segment -> cell of this thread (x = -1 when past the row end).
 __device__ __forceinline__ Cell seg_cell(const Dom& d, int64_t seg)
 {
-    const int64_t row = seg / d.xchunks;
-    const int     xc = int(seg - row * d.xchunks);
-    Cell          c;
+    // 32-bit index arithmetic (segments < 2^31, checked on the host): 64-bit
+    // division is a long emulated sequence on the GPU.
+    const uint32_t s32 = uint32_t(seg);
+    const uint32_t row = s32 / uint32_t(d.xchunks);
+    const int      xc = int(s32 - row * uint32_t(d.xchunks));
+    Cell           c;
     c.x = xc * kBX + threadIdx.x;
-    c.y = int(row % d.ny);
-    c.z = int(row / d.ny);
+    c.y = int(row % uint32_t(d.ny));
+    c.z = int(row / uint32_t(d.ny));
     c.i = c.x + int64_t(d.nx) * (c.y + int64_t(d.ny) * c.z);
     if (c.x >= d.nx) c.x = -1;
     return c;
@@ -119,7 +124,10 @@ template <typename T>
 __device__ __forceinline__ T invdiag_of(const Dom& d, int x, int y, int z, int64_t i, int jacobi)
 {
     if (!jacobi || is_fixed(d, x, y, z, i)) return T(1);
-    return T(d.invd[n_valid(d, x, y, z)]);
+    if constexpr (std::is_same<T, float>::value)
+        return d.invf[n_valid(d, x, y, z)];
+    else
+        return d.invd[n_valid(d, x, y, z)];
 }
 
 // Neighbour visitor in the oracle's order +x, -x, +y, -y, +z, -z.
@@ -438,6 +446,7 @@ int validate(const ngb_poisson_desc* d)
     NGB_CHECK_ARG(d->nx >= 1 && d->ny >= 1 && d->nz >= 1, "dims must be positive");
     NGB_CHECK_ARG(d->field == NGB_STORE_F32 || d->field == NGB_STORE_F64, "field must be NGB_STORE_F32 or NGB_STORE_F64");
     NGB_CHECK_ARG(d->h > 0, "h must be positive");
+    NGB_CHECK_ARG(make_dom(d).segs < (int64_t(1) << 31), "grid too large (ny * nz * ceil(nx / 256) >= 2^31)");
     return NGB_OK;
 }
 

@@ -20,7 +20,8 @@ PROGRAMS = ["api_stencil", "api_lbm", "api_poisson"]
 
 
 def _compile(name):
-    import neon_gb300.build as b
+    import importlib
+    b = importlib.import_module("neon_gb300.build")
     exe = os.path.join(BUILD, name)
     src = os.path.join(CPP, name + ".cu")
     libdir = os.path.dirname(b.LIB_PATH)
