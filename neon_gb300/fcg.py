@@ -1,0 +1,173 @@
+"""Flexible CG with the learned U-Net preconditioner, its training data and
+training loop (the learned-preconditioner case of the Poisson benchmark).
+
+* Training data are residual/error pairs the solver itself produces: for
+  seeded Gaussian random right-hand sides with a k^-2 power spectrum (zero on
+  the Dirichlet faces), plain CG runs to convergence and the pairs
+  (r_k, x_final - x_k) are kept at a fixed set of iterations k.
+* Training minimises |M(r) - e|^2 / |e|^2 with Adam on the U-Net's FP32
+  master weights (forward/backward on the tensor-core kernels).
+* The solver is FCG(1) (flexible CG with one-step A-orthogonalisation, which
+  tolerates a nonlinear preconditioner): z = M(r) masked to the Free rows,
+  p = z - (z.q_prev / p_prev.q_prev) p_prev, q = A p, alpha = p.r / p.q;
+  x accumulates in FP64 and the true residual b - A x is recomputed in FP64
+  every `refresh` iterations. If the true residual fails to halve over
+  `stall` iterations the solve continues with Jacobi-PCG (ngb_cg_solve) from
+  the current x.
+"""
+import time
+
+import torch
+
+from . import (STORE_F32, STORE_F64, _ptr, cg_solve, cg_workspace, check, dot, laplacian_apply, lib, poisson_desc)
+
+
+def free_mask(n, device):
+    m = torch.zeros(n, n, n, dtype=torch.float32, device=device)
+    m[1:-1, 1:-1, 1:-1] = 1.0
+    return m.reshape(-1)
+
+
+def grf_k2(n, seed, device):
+    """Gaussian random field with power spectrum |k|^-2 (amplitude |k|^-1), zero on the box faces, unit RMS."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    white = torch.randn(n, n, n, generator=g).to(device)
+    F = torch.fft.rfftn(white)
+    kz = torch.fft.fftfreq(n, device=device).reshape(n, 1, 1)
+    ky = torch.fft.fftfreq(n, device=device).reshape(1, n, 1)
+    kx = torch.fft.rfftfreq(n, device=device).reshape(1, 1, n // 2 + 1)
+    k = torch.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    k[0, 0, 0] = 1.0
+    field = torch.fft.irfftn(F / k, s=(n, n, n)).reshape(-1)
+    field = field * free_mask(n, device)
+    return (field / field.pow(2).mean().sqrt()).float()
+
+
+class _Ops:
+    """A, dot on the device through the C ABI (FP32 and FP64 fields)."""
+
+    def __init__(self, n, device):
+        self.n = n
+        self.dev = device
+        self.d32 = poisson_desc(n, n, n, "f32", 1.0)
+        self.d64 = poisson_desc(n, n, n, "f64", 1.0)
+        self.res = torch.zeros(1, dtype=torch.float64, device=device)
+        self.scratch = torch.empty(lib().ngb_dot_scratch_doubles(n ** 3), dtype=torch.float64, device=device)
+
+    def A(self, u, out):
+        laplacian_apply(self.d64 if u.dtype == torch.float64 else self.d32, u, out)
+        return out
+
+    def dot(self, a, b):
+        dot(a, b, self.res, self.scratch)
+        return float(self.res.item())
+
+
+def cg_pairs(n, seed, captures, device, tol=1e-7, max_iter=5000):
+    """Plain CG on A x = b (b = k^-2 field); returns [(r_k, x_final - x_k)] at iterations `captures`."""
+    ops = _Ops(n, device)
+    b = grf_k2(n, seed, device)
+    x = torch.zeros_like(b)
+    r = b.clone()
+    p = r.clone()
+    q = torch.empty_like(b)
+    rr = ops.dot(r, r)
+    bb = rr
+    saved = {}
+    for k in range(max_iter):
+        if k in captures:
+            saved[k] = (r.clone(), x.clone())
+        ops.A(p, q)
+        alpha = rr / ops.dot(p, q)
+        x.add_(p, alpha=alpha)
+        r.add_(q, alpha=-alpha)
+        rr_new = ops.dot(r, r)
+        if rr_new <= tol * tol * bb:
+            break
+        p.mul_(rr_new / rr).add_(r)
+        rr = rr_new
+    return [(rk, x - xk) for rk, xk in saved.values()]
+
+
+def make_training_set(n=128, systems=200, captures=(2, 5, 10, 20, 40, 80, 120, 160, 200, 250), seed=2024,
+                      device="cuda"):
+    pairs = []
+    for s in range(systems):
+        pairs += cg_pairs(n, seed + s, set(captures), device)
+    return pairs
+
+
+def train(net, pairs, epochs=2, lr=1e-3, log=None, seed=0):
+    g = torch.Generator().manual_seed(seed)
+    losses = []
+    for ep in range(epochs):
+        order = torch.randperm(len(pairs), generator=g).tolist()
+        for i in order:
+            r, e = pairs[i]
+            z = net.forward(r)
+            ee = float((e.double() ** 2).sum())
+            diff = z - e
+            losses.append(float((diff.double() ** 2).sum()) / ee)
+            net.zero_grad()
+            net.backward((2.0 / ee) * diff)
+            net.adam_step(lr=lr)
+        if log:
+            log("epoch %d: mean relative loss %.4f" % (ep, sum(losses[-len(pairs):]) / len(pairs)))
+    return losses
+
+
+def fcg_solve(net, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=20, fallback=True, ws=None):
+    """FCG(1) with z = M(r). b: float32 n^3 field (zero on the faces); x: float64 n^3 initial guess / result."""
+    n = round(b.numel() ** (1.0 / 3.0))
+    dev = b.device
+    ops = _Ops(n, dev)
+    mask = free_mask(n, dev)
+    t0 = time.perf_counter()
+    bn = ops.dot(b, b) ** 0.5
+    ax = torch.empty_like(x)
+
+    def true_residual():
+        ops.A(x, ax)
+        rt = (b.double() - ax) * mask.double()
+        return rt.float(), ops.dot(rt, rt) ** 0.5 / bn
+
+    r, rel = true_residual()
+    history = [rel]
+    q = torch.empty_like(b)
+    p_prev = q_prev = None
+    pq_prev = None
+    it = 0
+    used_fallback = False
+    while rel > tol and it < max_iter:
+        z = net.forward(r) * mask
+        az = ops.A(z, torch.empty_like(z))
+        if p_prev is not None:
+            coef = ops.dot(z, q_prev) / pq_prev
+            p = z - coef * p_prev
+            q = az - coef * q_prev
+        else:
+            p, q = z, az
+        pq = ops.dot(p, q)
+        alpha = ops.dot(p, r) / pq
+        x.add_(p.double(), alpha=alpha)
+        r = r - alpha * q
+        p_prev, q_prev, pq_prev = p, q, pq
+        it += 1
+        if it % refresh == 0:
+            r, rel = true_residual()
+            history.append(rel)
+            if fallback and len(history) > stall // refresh and history[-1] > 0.5 * history[-1 - stall // refresh]:
+                used_fallback = True
+                break
+        else:
+            rel = ops.dot(r, r) ** 0.5 / bn
+    torch.cuda.synchronize()
+    extra = {"iterations": 0}
+    if used_fallback and rel > tol:
+        d = poisson_desc(n, n, n, "f32", 1.0)
+        ws = ws if ws is not None else cg_workspace(d, dev)
+        extra = cg_solve(d, b, x, ws, tol=tol, max_iter=20000, refresh_every=50, check_every=50, jacobi=True)
+        r, rel = true_residual()
+    torch.cuda.synchronize()
+    return {"iterations": it, "fallback_iterations": extra["iterations"], "fallback": used_fallback,
+            "rel_residual": rel, "converged": rel <= tol, "seconds": time.perf_counter() - t0, "history": history}

@@ -1,0 +1,127 @@
+"""GPU checks of the learned preconditioner's kernels against the numpy oracle
+(oracle/unet_oracle.py): tensor-core convolution forward / backward-data /
+backward-weight, pooling, upsampling, the whole U-Net forward pass and its
+gradients."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_tensor(a, dev):
+    import torch
+    return torch.from_numpy(np.asarray(a, np.float32)).to(torch.bfloat16).to(dev)
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 64), (96, 32), (48, 16), (16, 8)])
+def test_conv_forward_matches_oracle(ngb, cuda, cin, cout):
+    import torch
+    rng = np.random.default_rng(cin * 100 + cout)
+    n = (6, 5, 7)  # nz, ny, nx
+    x = U.bf16(rng.standard_normal(n + (cin,)))
+    w = U.bf16(rng.standard_normal((cout, 27, cin)) / np.sqrt(27 * cin))
+    ref = U.conv(x, w)
+    X = _bf16_tensor(x.reshape(-1, cin), cuda)
+    Wt = _bf16_tensor(w, cuda)
+    Y = torch.zeros(X.shape[0], cout, dtype=torch.float32, device=cuda)
+    ngb.check(ngb.lib().ngb_conv3d(7, 5, 6, ngb._ptr(X), cin, cin, ngb._ptr(Wt), None, ngb._ptr(Y), cout, cout, 1, 0, 0, None))
+    got = Y.cpu().numpy().reshape(ref.shape)
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+    # BF16 output with ReLU
+    Yb = torch.zeros(X.shape[0], cout, dtype=torch.bfloat16, device=cuda)
+    ngb.check(ngb.lib().ngb_conv3d(7, 5, 6, ngb._ptr(X), cin, cin, ngb._ptr(Wt), None, ngb._ptr(Yb), cout, cout, 0, 1, 0, None))
+    gotb = Yb.float().cpu().numpy().reshape(ref.shape)
+    assert np.abs(gotb - U.bf16(np.maximum(ref, 0))).max() <= 2 ** -7 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (32, 64), (96, 32)])
+def test_conv_backward_weight_and_data(ngb, cuda, cin, cout):
+    import torch
+    rng = np.random.default_rng(7 + cin + cout)
+    nz, ny, nx = 6, 8, 5
+    x = U.bf16(rng.standard_normal((nz, ny, nx, cin)))
+    dy = U.bf16(rng.standard_normal((nz, ny, nx, cout)))
+    w = U.bf16(rng.standard_normal((cout, 27, cin)) / np.sqrt(27 * cin))
+    dw_ref = U.conv_bwd_weight(x, dy)
+    dx_ref = U.conv_bwd_data(dy, w)
+    X = _bf16_tensor(x.reshape(-1, cin), cuda)
+    D = _bf16_tensor(dy.reshape(-1, cout), cuda)
+    dW = torch.zeros(cout, 27, cin, dtype=torch.float32, device=cuda)
+    L = ngb.lib()
+    ngb.check(L.ngb_conv3d_bwd_weight(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dW), None))
+    assert np.abs(dW.cpu().numpy() - dw_ref).max() <= 1e-5 * np.abs(dw_ref).max()
+    Wf = torch.from_numpy(w.astype(np.float32)).to(cuda)
+    Wt = torch.empty(cin, 27, cout, dtype=torch.bfloat16, device=cuda)
+    ngb.check(L.ngb_flip_weights(cout, cin, ngb._ptr(Wf), ngb._ptr(Wt), None))
+    dX = torch.zeros(X.shape[0], cin, dtype=torch.float32, device=cuda)
+    if cin <= 64:
+        ngb.check(L.ngb_conv3d(nx, ny, nz, ngb._ptr(D), cout, cout, ngb._ptr(Wt), None, ngb._ptr(dX), cin, cin, 1, 0, 0, None))
+    else:  # 96 output channels in two calls of 64 and 32 (the U-Net's c1c)
+        for lo, hi in ((0, 64), (64, 96)):
+            ptr = ctypes.c_void_p(dX.data_ptr() + lo * 4)
+            ngb.check(L.ngb_conv3d(nx, ny, nz, ngb._ptr(D), cout, cout, ngb._ptr(Wt[lo:hi]), None, ptr, cin, hi - lo, 1, 0, 0,
+                                   None))
+    assert np.abs(dX.cpu().numpy().reshape(dx_ref.shape) - dx_ref).max() <= 1e-5 * np.abs(dx_ref).max()
+
+
+def test_pool_and_upsample(ngb, cuda):
+    import torch
+    rng = np.random.default_rng(5)
+    x = U.bf16(rng.standard_normal((4, 6, 8, 16)))
+    X = _bf16_tensor(x.reshape(-1, 16), cuda)
+    P = torch.zeros(2 * 3 * 4, 16, dtype=torch.bfloat16, device=cuda)
+    L = ngb.lib()
+    ngb.check(L.ngb_pool2(8, 6, 4, 16, ngb._ptr(X), 16, ngb._ptr(P), 16, None))
+    assert np.allclose(P.float().cpu().numpy().reshape(2, 3, 4, 16), U.bf16(U.pool(x)), rtol=0, atol=1e-6)
+    Up = torch.zeros_like(X)
+    ngb.check(L.ngb_up2(8, 6, 4, 16, ngb._ptr(P), 16, ngb._ptr(Up), 16, None))
+    assert np.array_equal(Up.float().cpu().numpy().reshape(x.shape), U.up(P.float().cpu().numpy().reshape(2, 3, 4, 16)))
+
+
+def test_unet_forward_and_gradients_match_oracle(ngb, cuda):
+    import torch
+    from neon_gb300.learned import UNet
+    n = 12
+    net = UNet(seed=4, device=cuda)
+    # non-trivial last layer so gradients reach every layer
+    net.w["c0d"] = net.w["c0d"] * 0 + torch.randn(net.w["c0d"].shape, generator=torch.Generator().manual_seed(9)).to(cuda) * 0.05
+    net.load_state_dict({k: v.cpu() for k, v in net.w.items()})
+    rng = np.random.default_rng(11)
+    r = rng.standard_normal(n ** 3).astype(np.float32)
+    e = rng.standard_normal(n ** 3).astype(np.float32)
+    z = net.forward(torch.from_numpy(r).to(cuda))
+    W = {k: v.cpu().numpy().astype(np.float64) for k, v in net.w.items()}
+    zo, cache = U.forward(W, r, n)
+    zg = z.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(zg - zo) <= 2e-3 * np.linalg.norm(zo), np.linalg.norm(zg - zo) / np.linalg.norm(zo)
+    dz = (zg - e).astype(np.float32)
+    net.zero_grad()
+    net.backward(torch.from_numpy(dz).to(cuda))
+    go = U.backward(cache, dz.astype(np.float64))
+    for name in go:
+        gg = net.g[name].cpu().numpy()
+        rel = np.linalg.norm(gg - go[name]) / max(np.linalg.norm(go[name]), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+
+
+def test_training_reduces_loss(ngb, cuda):
+    import torch
+    from neon_gb300.learned import UNet
+    n = 16
+    net = UNet(seed=1, device=cuda)
+    g = torch.Generator().manual_seed(2)
+    r = torch.randn(n ** 3, generator=g).to(cuda)
+    target = torch.roll(r, 1) * 0.5 + r  # a fixed linear map of r
+    losses = []
+    for it in range(60):
+        z = net.forward(r)
+        diff = z - target
+        losses.append(float((diff ** 2).sum() / (target ** 2).sum()))
+        net.zero_grad()
+        net.backward(2 * diff / (target ** 2).sum())
+        net.adam_step(lr=3e-3)
+    assert losses[-1] < 0.5 * losses[0], losses[::10]
