@@ -85,7 +85,7 @@ Dom make_dom(const ngb_poisson_desc* d)
     return g;
 }
 
-int grid_for(int64_t segs) { return int(std::min<int64_t>(segs, int64_t(sm_count()) * 4)); }
+int grid_for(int64_t segs) { return int(std::min<int64_t>(segs, int64_t(sm_count()) * 8)); }
 
 struct Cell {
     int     x, y, z;
@@ -124,10 +124,13 @@ template <typename T>
 __device__ __forceinline__ T invdiag_of(const Dom& d, int x, int y, int z, int64_t i, int jacobi)
 {
     if (!jacobi || is_fixed(d, x, y, z, i)) return T(1);
+    // constant indices only: a runtime index into the parameter array would
+    // copy it to local memory
+    const int n = n_valid(d, x, y, z);
     if constexpr (std::is_same<T, float>::value)
-        return d.invf[n_valid(d, x, y, z)];
+        return n == 6 ? d.invf[6] : n == 5 ? d.invf[5] : n == 4 ? d.invf[4] : n == 3 ? d.invf[3] : n == 2 ? d.invf[2] : n == 1 ? d.invf[1] : d.invf[0];
     else
-        return d.invd[n_valid(d, x, y, z)];
+        return n == 6 ? d.invd[6] : n == 5 ? d.invd[5] : n == 4 ? d.invd[4] : n == 3 ? d.invd[3] : n == 2 ? d.invd[2] : n == 1 ? d.invd[1] : d.invd[0];
 }
 
 // Neighbour visitor in the oracle's order +x, -x, +y, -y, +z, -z.
@@ -305,9 +308,36 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     const T      invh2 = T(1.0) / (T(d.h) * T(d.h));
     DotAcc<T>    acc;
     auto         pn = [&](int x, int y, int z, int64_t j) -> T { return T(invdiag_of<T>(d, x, y, z, j, jac) * r[j]) + tb * p_old[j]; };
+    // diagonal inverse of a Free cell with six valid neighbours (interior fast path)
+    T dg = T(1);
+    if (jac) {
+        if constexpr (std::is_same<T, float>::value)
+            dg = d.invf[6];
+        else
+            dg = d.invd[6];
+    }
     for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
         const Cell c = seg_cell(d, seg);
         if (c.x < 0) continue;
+        // Fast path: in the analytic box, a cell two or more cells from every
+        // face has itself and its six neighbours Free with six valid
+        // neighbours each (the same values as the general path, fewer checks).
+        if (!d.bd && c.x >= 2 && c.y >= 2 && c.z >= 2 && c.x < d.nx - 2 && c.y < d.ny - 2 && c.z < d.nz - 2) {
+            const int64_t sy = d.nx, sz = int64_t(d.nx) * d.ny, i = c.i;
+            const T       pc = T(dg * r[i]) + tb * p_old[i];
+            T             sum = T(0);
+            sum = sum + (T(dg * r[i + 1]) + tb * p_old[i + 1]);
+            sum = sum + (T(dg * r[i - 1]) + tb * p_old[i - 1]);
+            sum = sum + (T(dg * r[i + sy]) + tb * p_old[i + sy]);
+            sum = sum + (T(dg * r[i - sy]) + tb * p_old[i - sy]);
+            sum = sum + (T(dg * r[i + sz]) + tb * p_old[i + sz]);
+            sum = sum + (T(dg * r[i - sz]) + tb * p_old[i - sz]);
+            const T sc = (-sum + T(6) * pc) * invh2;
+            p_new[i] = pc;
+            s[i] = sc;
+            acc.add(pc, sc);
+            continue;
+        }
         const T pc = pn(c.x, c.y, c.z, c.i);
         T       sc;
         if (is_fixed(d, c.x, c.y, c.z, c.i)) {
@@ -342,15 +372,28 @@ __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* _
     const int jac = st->jacobi;
     const T   ta = T(st->alpha);
     DotAcc<T> a0, a1;
-    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
-        const Cell c = seg_cell(d, seg);
-        if (c.x < 0) continue;
-        xlo[c.i] = xlo[c.i] + ta * p[c.i];
-        const T rn = r[c.i] - ta * s[c.i];
-        r[c.i] = rn;
-        const T z = T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, jac) * rn);
-        a0.add(rn, z);
-        a1.add(rn, rn);
+    // two segments per trip: both cells' loads are in flight together
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += 2 * int64_t(gridDim.x)) {
+        Cell      c[2];
+        T         xv[2], pv[2], rv[2], sv[2];
+        const int cnt = (seg + gridDim.x < d.segs) ? 2 : 1;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            c[u] = seg_cell(d, seg + u * int64_t(gridDim.x));
+            if (u >= cnt) c[u].x = -1;
+            if (c[u].x < 0) continue;
+            xv[u] = xlo[c[u].i], pv[u] = p[c[u].i], rv[u] = r[c[u].i], sv[u] = s[c[u].i];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (c[u].x < 0) continue;
+            xlo[c[u].i] = xv[u] + ta * pv[u];
+            const T rn = rv[u] - ta * sv[u];
+            r[c[u].i] = rn;
+            const T z = T(invdiag_of<T>(d, c[u].x, c[u].y, c[u].z, c[u].i, jac) * rn);
+            a0.add(rn, z);
+            a1.add(rn, rn);
+        }
     }
     double v[2] = {a0.value(), a1.value()};
     double out[2];
