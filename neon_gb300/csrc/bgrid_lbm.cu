@@ -31,26 +31,66 @@ __device__ __forceinline__ double as_f<__nv_bfloat16>(__nv_bfloat16 v, double w)
     return double(__bfloat162float(v)) + double(float(w));
 }
 
-// Moving-wall bits of the masked directions (source class == moving wall).
+// Pull source of direction q for voxel (i,j,k): the voxel (i,j,k) - c_q, in
+// this block or one of its 26 neighbours (bPartition::helpGetNghIdx,
+// bPartition_imp.h:135-309). Every thread takes the same arithmetic path: the
+// block offset per axis is -1 / 0 / +1 from the shifted coordinate, the block
+// comes from the connectivity row in shared memory (entry 13 is the block
+// itself), so a warp that mixes block-edge and inner voxels does not diverge.
+template <int Q>
+__device__ __forceinline__ uint32_t bgrid_pull_src(const uint32_t* sconn, int i, int j, int k, int q, int& nv)
+{
+    using L = Lattice<Q>;
+    const int cx = L::cx(q), cy = L::cy(q), cz = L::cz(q);
+    const int ii = i - cx, jj = j - cy, kk = k - cz;
+    const int fx = cx > 0 ? (ii >> 31) : (cx < 0 ? (ii >> 3) : 0);
+    const int fy = cy > 0 ? (jj >> 31) : (cy < 0 ? (jj >> 3) : 0);
+    const int fz = cz > 0 ? (kk >> 31) : (cz < 0 ? (kk >> 3) : 0);
+    nv = (ii & 7) | ((jj & 7) << 3) | ((kk & 7) << 6);
+    return sconn[13 + fx + 3 * fy + 9 * fz];
+}
+
+// Moving-wall bits of the masked directions (source voxel active and of class
+// moving wall). The mask word and the flag of the source are loaded together.
 template <int Q>
 __device__ __forceinline__ uint32_t bgrid_lidbits(const uint32_t* __restrict__ flags, const uint32_t* __restrict__ mask,
-                                                  const uint32_t* __restrict__ conn, uint32_t b, int i, int j, int k, uint32_t m)
+                                                  const uint32_t* sconn, int i, int j, int k, uint32_t m)
 {
     uint32_t lid = 0;
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         if (!(m & (1u << q))) continue;
-        uint32_t nb;
-        int      nv;
-        if (bgrid_valid_ngh(mask, conn, b, i, j, k, -Lattice<Q>::cx(q), -Lattice<Q>::cy(q), -Lattice<Q>::cz(q), nb, nv) &&
-            flag_class(__ldg(flags + size_t(nb) * kBlockVoxels + nv)) == NGB_CELL_MOVINGWALL)
-            lid |= 1u << q;
+        int            nv;
+        const uint32_t nb = bgrid_pull_src<Q>(sconn, i, j, k, q, nv);
+        if (nb == NGB_BGRID_NO_BLOCK) continue;
+        const uint32_t word = __ldg(mask + size_t(nb) * 16 + (nv >> 5));
+        const uint32_t fl = __ldg(flags + size_t(nb) * kBlockVoxels + nv);
+        if (((word >> (nv & 31)) & 1u) && flag_class(fl) == NGB_CELL_MOVINGWALL) lid |= 1u << q;
     }
     return lid;
 }
 
+// Source pointer of direction q for this voxel: the pulled neighbour
+// population, or the voxel's own opposite population when q is masked (the
+// half-way bounce-back rule). A source outside every block is taken as a wall,
+// so no flag word can make the kernel read outside the field.
+template <int Q, typename S>
+__device__ __forceinline__ const S* bgrid_src(const S* __restrict__ fin, const uint32_t* sconn, size_t bq, int v, int i, int j,
+                                              int k, int q, uint32_t m, bool& masked)
+{
+    using L = Lattice<Q>;
+    if (L::cx(q) == 0 && L::cy(q) == 0 && L::cz(q) == 0) {
+        masked = false;
+        return fin + (bq + q) * kBlockVoxels + v;
+    }
+    int            nv;
+    const uint32_t nb = bgrid_pull_src<Q>(sconn, i, j, k, q, nv);
+    masked = ((m >> q) & 1u) || nb == NGB_BGRID_NO_BLOCK;
+    return masked ? fin + (bq + L::opp(q)) * kBlockVoxels + v : fin + (size_t(nb) * Q + q) * kBlockVoxels + nv;
+}
+
 template <int Q, typename S, bool F64>
-__global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+__global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
                                                                  const uint32_t* __restrict__ flags,
                                                                  BParams<typename std::conditional<F64, double, float>::type> p)
 {
@@ -74,23 +114,17 @@ __global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __rest
     }
     if (cls != NGB_CELL_BULK) return;
     const uint32_t m = flag_mask(f);
-    const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, p.conn, b, i, j, k, m) : 0u;
-    const bool     interior = (i >= 1 && i <= 6 && j >= 1 && j <= 6 && k >= 1 && k <= 6);
+    const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m) : 0u;
 
     if constexpr (F64) {
         S pop[Q];
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            if (m & (1u << q)) {
-                const int o = L::opp(q);
-                pop[q] = __ldg(fin + (bq + o) * kBlockVoxels + v) + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
-            } else if (interior) {
-                pop[q] = __ldg(fin + (bq + q) * kBlockVoxels + v - L::cx(q) - 8 * L::cy(q) - 64 * L::cz(q));
-            } else {
-                int            nv;
-                const uint32_t nb = bgrid_ngh_local(sconn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
-                pop[q] = __ldg(fin + (size_t(nb) * Q + q) * kBlockVoxels + nv);
-            }
+            bool      masked;
+            const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
+            const int o = L::opp(q);
+            pop[q] = __ldg(src);
+            if (masked) pop[q] = pop[q] + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
         }
         S out[Q];
         bgk_f64_ref<Q, S>(pop, p.omega, out);
@@ -100,18 +134,12 @@ __global__ void __launch_bounds__(kBlockVoxels) bgrid_lbm_kernel(const S* __rest
         float g[Q];
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            if (m & (1u << q)) {
-                const int o = L::opp(q);
-                g[q] = PairIO<S>::to_g1(__ldg(fin + (bq + o) * kBlockVoxels + v), float(L::w(o))) +
-                       ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
-            } else if (interior) {
-                g[q] = PairIO<S>::to_g1(__ldg(fin + (bq + q) * kBlockVoxels + v - L::cx(q) - 8 * L::cy(q) - 64 * L::cz(q)),
-                                        float(L::w(q)));
-            } else {
-                int            nv;
-                const uint32_t nb = bgrid_ngh_local(sconn, b, i, j, k, -L::cx(q), -L::cy(q), -L::cz(q), nv);
-                g[q] = PairIO<S>::to_g1(__ldg(fin + (size_t(nb) * Q + q) * kBlockVoxels + nv), float(L::w(q)));
-            }
+            bool      masked;
+            const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
+            const int o = L::opp(q);
+            // w(opp q) == w(q), so one conversion serves both cases
+            g[q] = PairIO<S>::to_g1(__ldg(src), float(L::w(q)));
+            if (masked) g[q] = g[q] + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
         }
         bgk_shifted<Q, float>(g, p.omega);
 #pragma unroll
