@@ -324,6 +324,23 @@ int ngb_gaussian_sources(int32_t nx, int32_t ny, int32_t nz, uint64_t seed, doub
 int ngb_conv3d(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* w, const float* bias,
                void* y, int32_t ldy, int32_t cout, int32_t out_f32, int32_t relu, int32_t accumulate, void* stream);
 
+/* The same convolution on the 5th-generation tensor cores (tcgen05.mma with
+ * the accumulator in TMEM, operands staged by TMA; no reference counterpart).
+ * Shapes it takes (ngb_conv3d_tc_supported returns 1): cin % 16 == 0,
+ * cout in {16, 32, 48, 64, 96}, ldx and ldy multiples of 8, and either
+ * nx % 128 == 0 or nx a divisor of 128 with ny % (128 / nx) == 0; x, y, the
+ * packed weights and bias 16-byte aligned. `wpacked` is the operand image
+ * written by ngb_conv3d_pack from [cout][27][cin] BF16 weights (same size).
+ * Asynchronous; ngb_conv3d_tc_check(stream) synchronises the stream and
+ * returns NGB_ERR_TIMEOUT if a pipeline wait of any earlier launch ran out
+ * (results of that launch are then invalid). */
+int ngb_conv3d_tc_supported(int32_t nx, int32_t ny, int32_t nz, int32_t ldx, int32_t cin, int32_t ldy, int32_t cout);
+int ngb_conv3d_pack(int32_t cout, int32_t cin, const void* w, void* wpacked, void* stream);
+int ngb_conv3d_tc(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* wpacked,
+                  const float* bias, void* y, int32_t ldy, int32_t cout, int32_t out_f32, int32_t relu, int32_t accumulate,
+                  void* stream);
+int ngb_conv3d_tc_check(void* stream);
+
 /* dw[co][t][ci] += sum_v dy[v][co] x[v+t][ci] (BF16 inputs, FP32 dw). */
 int ngb_conv3d_bwd_weight(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy, int32_t lddy,
                           int32_t cout, float* dw, void* stream);

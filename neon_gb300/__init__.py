@@ -133,6 +133,10 @@ _EXTRA_SIGNATURES.update({
     "ngb_adam": ([ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                   _i32, _vp, _vp], ctypes.c_int),
     "ngb_flip_weights": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_conv3d_tc_supported": ([_i32, _i32, _i32, _i32, _i32, _i32, _i32], ctypes.c_int),
+    "ngb_conv3d_pack": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_conv3d_tc": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
+    "ngb_conv3d_tc_check": ([_vp], ctypes.c_int),
 })
 
 

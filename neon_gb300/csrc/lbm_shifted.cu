@@ -8,8 +8,17 @@ int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const 
                          cudaStream_t s)
 {
     const dim3 grid((p.nx + kLbmBlockX - 1) / kLbmBlockX, p.ny, p.nz), block(kLbmBlockX);
+    const int64_t esz = storage == NGB_STORE_F32 ? 4 : 2, sy = p.nx, sz = int64_t(p.nx) * p.ny;
+    DirOffsets    o{};
+    for (int q = 0; q < Q; q++) {
+        const int cx = Q == 19 ? Lattice<19>::cx(q) : Lattice<27>::cx(q);
+        const int cy = Q == 19 ? Lattice<19>::cy(q) : Lattice<27>::cy(q);
+        const int cz = Q == 19 ? Lattice<19>::cz(q) : Lattice<27>::cz(q);
+        o.own[q] = q * p.stride * esz;
+        o.pull[q] = (q * p.stride - cx - cy * sy - cz * sz) * esz;
+    }
 #define NGB_ONE(QQ, T) \
-    lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)
+    lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p, o)
     const bool q19 = Q == 19;
     switch (storage) {
         case NGB_STORE_F32:

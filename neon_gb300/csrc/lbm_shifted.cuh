@@ -91,32 +91,37 @@ struct PairIO<__nv_bfloat16> {
     __device__ __forceinline__ static void store1(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
 };
 
-// Scalar pull of one cell's populations as g (wall rule included). Addresses
-// are the cell's own pointer plus a per-direction offset that depends only on
-// kernel parameters (warp-uniform), so each load costs one address add.
+// Byte offsets, relative to a cell's own element of plane 0, of each
+// direction's pull source (q * stride - c_q . (1, nx, nx ny)) and of each of
+// the cell's own planes (q * stride). They depend only on the grid, so the
+// host computes them once: recomputing them per thread in 64-bit integer
+// arithmetic was the largest instruction class of the 16-bit kernels.
+struct DirOffsets {
+    int64_t pull[27];
+    int64_t own[27];
+};
+
+// Scalar pull of one cell's populations as g (wall rule included): one 64-bit
+// address add per load.
 template <int Q, typename S>
-__device__ __forceinline__ void pull_one(const S* __restrict__ fin, int64_t stride, int64_t cell, int64_t sy, int64_t sz,
-                                         uint32_t mask, uint32_t lidbits, const DenseParams<float>& p, float* g)
+__device__ __forceinline__ void pull_one(const S* __restrict__ fin, int64_t cell, uint32_t mask, uint32_t lidbits,
+                                         const DenseParams<float>& p, const DirOffsets& o, float* g)
 {
     using L = Lattice<Q>;
-    const S* P = fin + cell;
+    const char* P = reinterpret_cast<const char*>(fin + cell);
     if (mask == 0) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const int64_t off = q * stride - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-            g[q] = PairIO<S>::to_g1(__ldg(P + off), float(L::w(q)));
-        }
+        for (int q = 0; q < Q; q++) g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
         return;
     }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         if (mask & (1u << q)) {
-            const int   o = L::opp(q);
-            const float wt = (lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o];
-            g[q] = PairIO<S>::to_g1(__ldg(P + o * stride), float(L::w(o))) + wt;
+            const int   oq = L::opp(q);
+            const float wt = (lidbits & (1u << q)) ? p.wall[1][oq] : p.wall[0][oq];
+            g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.own[oq])), float(L::w(oq))) + wt;
         } else {
-            const int64_t off = q * stride - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz;
-            g[q] = PairIO<S>::to_g1(__ldg(P + off), float(L::w(q)));
+            g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
         }
     }
 }
@@ -217,27 +222,27 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
 // One cell per thread.
 template <int Q, typename S>
 __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                     const uint32_t* __restrict__ flags, DenseParams<float> p)
+                                                                     const uint32_t* __restrict__ flags, DenseParams<float> p,
+                                                                     const __grid_constant__ DirOffsets o)
 {
     using L = Lattice<Q>;
     const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= p.nx) return;
-    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
-    const int64_t cell = x + sy * y + sz * z;
+    const int64_t cell = x + int64_t(p.nx) * (y + int64_t(p.ny) * z);
     uint32_t      mask, lidbits;
     const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
     if (cls == NGB_CELL_OUTLET) {
-        outlet_copy<Q>(fin, fout, stride, cell, x, flags);
+        outlet_copy<Q>(fin, fout, p.stride, cell, x, flags);
         return;
     }
     if (cls != NGB_CELL_BULK) return;
     float g[Q];
-    pull_one<Q, S>(fin, stride, cell, sy, sz, mask, lidbits, p, g);
+    pull_one<Q, S>(fin, cell, mask, lidbits, p, o, g);
     bgk_shifted<Q, float>(g, p.omega);
-    S* D = fout + cell;
+    char* D = reinterpret_cast<char*>(fout + cell);
 #pragma unroll
-    for (int q = 0; q < Q; q++) PairIO<S>::store1(D + q * stride, g[q], float(L::w(q)));
+    for (int q = 0; q < Q; q++) PairIO<S>::store1(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)));
 }
 
 }  // namespace ngb

@@ -53,6 +53,10 @@ class UNet:
             self.s[name] = torch.zeros_like(self.w[name])
         self.step_count = 0
         self.shape = None
+        # tcgen05 convolutions where the grid shape allows (ngb_conv3d_tc),
+        # the mma.sync kernel elsewhere
+        self.tensor_cores = True
+        self._pk = {}
         self._refresh_flipped()
 
     # ------------------------------------------------------------------ buffers
@@ -83,14 +87,39 @@ class UNet:
                           g2=E(V2, 64, f), gp1=E(V2, 32, f), dyb2=E(V2, 64, bf))
 
     def _refresh_flipped(self):
+        self._pk = {}
         for name, cin, cout in LAYERS:
             check(lib().ngb_flip_weights(cout, cin, _ptr(self.w[name]), _ptr(self.wt[name]), None))
+
+    def _packed(self, w):
+        """Tensor-core operand image of BF16 weights [cout, 27, cin] (cached until the weights change)."""
+        key = (w.data_ptr(), tuple(w.shape))
+        pk = self._pk.get(key)
+        if pk is None:
+            pk = torch.empty_like(w)
+            check(lib().ngb_conv3d_pack(w.shape[0], w.shape[2], _ptr(w), _ptr(pk), None))
+            self._pk[key] = pk
+        return pk
 
     # ------------------------------------------------------------------ primitives
     def _conv(self, lvl, x, xoff, cin, w, y, yoff, cout, out_f32=False, relu=False, acc=False):
         n = self.shape >> lvl
-        check(lib().ngb_conv3d(n, n, n, _p(x, xoff), x.shape[1], cin, _ptr(w), None, _p(y, yoff), y.shape[1], cout,
-                               int(out_f32), int(relu), int(acc), None))
+        L = lib()
+        if self.tensor_cores and L.ngb_conv3d_tc_supported(n, n, n, x.shape[1], cin, y.shape[1], cout):
+            check(L.ngb_conv3d_tc(n, n, n, _p(x, xoff), x.shape[1], cin, _ptr(self._packed(w)), None, _p(y, yoff), y.shape[1],
+                                  cout, int(out_f32), int(relu), int(acc), None))
+            self._tc_used = True
+            return
+        for lo in range(0, cout, 64):  # the mma.sync kernel takes at most 64 output channels
+            hi = min(cout, lo + 64)
+            check(L.ngb_conv3d(n, n, n, _p(x, xoff), x.shape[1], cin, _ptr(w[lo:hi]), None, _p(y, yoff + lo), y.shape[1],
+                               hi - lo, int(out_f32), int(relu), int(acc), None))
+
+    def _tc_check(self):
+        """Raise if a tensor-core convolution of the last pass reported a pipeline time-out (synchronises)."""
+        if getattr(self, "_tc_used", False):
+            self._tc_used = False
+            check(lib().ngb_conv3d_tc_check(None))
 
     def _bwdw(self, lvl, x, xoff, cin, dy, cout, dw):
         n = self.shape >> lvl
@@ -141,6 +170,7 @@ class UNet:
         self._up(0, self.d1b, 32, self.cat0, 0)
         self._conv(0, self.cat0, 0, 48, W["c0c"], self.d0a, 0, 16, relu=True)
         self._conv(0, self.d0a, 0, 16, W["c0d"], self.out, 0, 16, out_f32=True)
+        self._tc_check()
         return self.out[:, 0] * sigma
 
     def backward(self, dz):
@@ -167,9 +197,7 @@ class UNet:
         # c1c (96 input channels: two backward-data calls of 64 and 32 channels)
         self._relu_bwd(g1, 0, 32, self.d1a, 0, G["dyb1"])
         self._bwdw(1, self.cat1, 0, 96, G["dyb1"], 32, self.g["c1c"])
-        wt = Wt["c1c"]
-        self._conv(1, G["dyb1"], 0, 32, wt[:64], G["gcat1"], 0, 64, out_f32=True)
-        self._conv(1, G["dyb1"], 0, 32, wt[64:], G["gcat1"], 64, 32, out_f32=True)
+        self._conv(1, G["dyb1"], 0, 32, Wt["c1c"], G["gcat1"], 0, 96, out_f32=True)
         # up to level 1 <- b2
         g2 = G["g2"]
         self._up_bwd(1, G["gcat1"], 0, 64, g2)
@@ -200,6 +228,7 @@ class UNet:
         # c0a
         self._relu_bwd(G["g16"], 0, 16, self.a0, 0, G["dyb0"])
         self._bwdw(0, self.in0, 0, 16, G["dyb0"], 16, self.g["c0a"])
+        self._tc_check()
 
     def zero_grad(self):
         for k in self.g:

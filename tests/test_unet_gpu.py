@@ -125,3 +125,83 @@ def test_training_reduces_loss(ngb, cuda):
         net.backward(2 * diff / (target ** 2).sum())
         net.adam_step(lr=3e-3)
     assert losses[-1] < 0.5 * losses[0], losses[::10]
+
+
+@pytest.mark.parametrize("dims", [(3, 4, 32), (2, 3, 128), (2, 2, 256)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 64), (96, 32), (48, 16), (16, 48), (32, 96), (64, 64)])
+def test_conv_tensor_cores_match_oracle(ngb, cuda, dims, cin, cout):
+    """tcgen05 convolution (TMA-staged operands, TMEM accumulators) against the
+    float64 oracle on the same BF16 inputs: FP32 output with and without
+    accumulation, BF16 output with ReLU; tile edges at the x, y and z faces."""
+    import torch
+    nz, ny, nx = dims
+    L = ngb.lib()
+    assert L.ngb_conv3d_tc_supported(nx, ny, nz, cin, cin, cout, cout) == 1
+    rng = np.random.default_rng(cin * 1000 + cout + nx)
+    x = U.bf16(rng.standard_normal((nz, ny, nx, cin)))
+    w = U.bf16(rng.standard_normal((cout, 27, cin)) / np.sqrt(27 * cin))
+    ref = U.conv(x, w)
+    X = _bf16_tensor(x.reshape(-1, cin), cuda)
+    Wt = _bf16_tensor(w, cuda)
+    Wp = torch.empty_like(Wt)
+    ngb.check(L.ngb_conv3d_pack(cout, cin, ngb._ptr(Wt), ngb._ptr(Wp), None))
+    Y = torch.zeros(X.shape[0], cout, dtype=torch.float32, device=cuda)
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), None, ngb._ptr(Y), cout, cout, 1, 0, 0, None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    got = Y.cpu().numpy().reshape(ref.shape)
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= 1e-5 * scale, np.abs(got - ref).max() / scale
+    # accumulate into the existing FP32 output: 2 x ref
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), None, ngb._ptr(Y), cout, cout, 1, 0, 1, None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    assert np.abs(Y.cpu().numpy().reshape(ref.shape) - 2 * ref).max() <= 2e-5 * scale
+    # BF16 output with ReLU, written into a channel range of a wider buffer
+    wide = cout + 16
+    Yb = torch.zeros(X.shape[0], wide, dtype=torch.bfloat16, device=cuda)
+    ptr = ctypes.c_void_p(Yb.data_ptr() + 16 * 2)
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), None, ptr, wide, cout, 0, 1, 0, None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    gotb = Yb[:, 16:].float().cpu().numpy().reshape(ref.shape)
+    assert np.abs(gotb - U.bf16(np.maximum(ref, 0))).max() <= 2 ** -7 * scale
+    assert float(Yb[:, :16].abs().max()) == 0.0
+
+
+def test_conv_tensor_cores_reject_unsupported_shapes(ngb):
+    L = ngb.lib()
+    assert L.ngb_conv3d_tc_supported(12, 12, 12, 16, 16, 16, 16) == 0  # 12 does not divide 128
+    assert L.ngb_conv3d_tc_supported(32, 6, 4, 16, 16, 16, 16) == 0  # 128 / 32 rows do not tile ny = 6
+    assert L.ngb_conv3d_tc_supported(128, 1, 1, 16, 16, 8, 8) == 0  # cout 8 (N must be a multiple of 16)
+    assert L.ngb_conv3d_tc_supported(128, 1, 1, 16, 16, 16, 16) == 1
+    rc = L.ngb_conv3d_tc(12, 12, 12, None, 16, 16, None, None, None, 16, 16, 0, 0, 0, None)
+    assert rc != 0
+
+
+def test_unet_tensor_cores_match_oracle_and_mma_path(ngb, cuda):
+    """At 32^3 levels 0 and 1 run on tcgen05 (level 2, 8^3, on mma.sync): the
+    forward pass and all gradients against the numpy oracle, and the forward
+    pass against the all-mma.sync network."""
+    import torch
+    from neon_gb300.learned import UNet
+    n = 32
+    net = UNet(seed=4, device=cuda)
+    net.w["c0d"] = net.w["c0d"] * 0 + torch.randn(net.w["c0d"].shape, generator=torch.Generator().manual_seed(9)).to(cuda) * 0.05
+    net.load_state_dict({k: v.cpu() for k, v in net.w.items()})
+    rng = np.random.default_rng(12)
+    r = rng.standard_normal(n ** 3).astype(np.float32)
+    e = rng.standard_normal(n ** 3).astype(np.float32)
+    z = net.forward(torch.from_numpy(r).to(cuda)).clone()
+    W = {k: v.cpu().numpy().astype(np.float64) for k, v in net.w.items()}
+    zo, cache = U.forward(W, r, n)
+    zg = z.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(zg - zo) <= 2e-3 * np.linalg.norm(zo), np.linalg.norm(zg - zo) / np.linalg.norm(zo)
+    dz = (zg - e).astype(np.float32)
+    net.zero_grad()
+    net.backward(torch.from_numpy(dz).to(cuda))
+    go = U.backward(cache, dz.astype(np.float64))
+    for name in go:
+        gg = net.g[name].cpu().numpy()
+        rel = np.linalg.norm(gg - go[name]) / max(np.linalg.norm(go[name]), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+    net.tensor_cores = False
+    z2 = net.forward(torch.from_numpy(r).to(cuda)).clone()
+    assert float((z - z2).norm() / z2.norm()) <= 2e-3
