@@ -1,23 +1,31 @@
 // 3x3x3 BF16 convolution of the learned preconditioner on Blackwell's
 // 5th-generation tensor cores (tcgen05), as an implicit GEMM:
 //   D[v][co] = sum_{tap t, channel c} x[ngh(v, t)][c] * w[co][t][c]
-// M = 128 consecutive voxels (one tile), N = Cout, K = 27 taps x Cin, one
-// tcgen05.mma (M 128, N Cout, K 16) per (tap, 16-channel chunk).
+// M = 128 consecutive voxels (one tile), N = Cout, K = 27 taps x Cin, in
+// tcgen05.mma steps of M 128, N Cout, K 16.
+//
+// Operand staging (TMA, one 5-D box per stage: 8 channels x voxels x all
+// Cin / 8 channel groups, so the shared-memory image is already the
+// no-swizzle K-major layout: 8-row x 16-byte core matrices, 8-row groups
+// 128 B apart (SBO), 8-channel groups one voxel strip apart (LBO)):
+//   strip mode (nx % 128 == 0): a stage is one (dy, dz) strip of 130 voxels
+//     (x0 - 1 .. x0 + 128) with all channels; the three dx taps are the same
+//     image read from rows 0, 1, 2 (start address + 16 B per row), so a tile
+//     takes 9 stages and each input voxel is staged 9 times, not 27;
+//   tap mode (nx a divisor of 128): a stage is one tap's box of 128 voxels
+//     (by = 128 / nx rows of the grid), 27 stages per tile.
+// The tensor map's zero fill at the grid faces is the convolution's zero
+// padding. The weights of a stage's taps (pre-packed into the B operand
+// image) arrive by one bulk copy on the same barrier.
 //
 // Per CTA (persistent over tiles, 6 warps):
-//   warp 0     one thread issues TMA loads: per (tap, chunk) two boxes of
-//              8 channels x 128 voxels at the tap-shifted coordinates (the
-//              tensor map's zero fill is the convolution's zero padding) and
-//              one bulk copy of the packed weight slice;
+//   warp 0     one thread issues the TMA and bulk copies;
 //   warp 1     owns the TMEM accumulators (two buffers of N FP32 columns at
-//              column offsets 0 and kCols / 2);
-//              one thread issues the MMAs and commits each stage back to the
-//              producer and each finished tile to the epilogue;
+//              column offsets 0 and kCols / 2); one thread issues the MMAs and
+//              commits each stage back to the producer and each finished tile
+//              to the epilogue;
 //   warps 2-5  epilogue: tcgen05.ld of their 32-lane quarter, optional bias /
 //              ReLU / accumulation, BF16 or FP32 stores (channels-last rows).
-// Shared-memory operands use the no-swizzle K-major layout: 8-row x 16-byte
-// core matrices, 8-row groups 128 B apart (SBO), the two 8-channel halves of
-// a 16-channel chunk 2048 B (A) or N * 16 B (B) apart (LBO).
 //
 // Every wait is bounded: on time-out the kernel raises a device error flag
 // (read by ngb_conv3d_tc_check), waits for its own copies and MMAs with the
@@ -33,9 +41,9 @@ namespace ngb {
 namespace {
 
 constexpr int      kTcM = 128;           // voxels per tile (MMA M)
-constexpr int      kTcStages = 8;        // shared-memory pipeline depth
+constexpr int      kTcMaxStages = 8;     // shared-memory pipeline depth (at most)
 constexpr int      kTcThreads = 192;     // 6 warps
-constexpr uint32_t kTcGuard = 32 * 1024;  // slack after the stages (see launch)
+constexpr int      kStripRows = kTcM + 2;  // voxels x0 - 1 .. x0 + 128
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;
@@ -86,12 +94,12 @@ __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity)
     atomicExch(&g_tc_error, 1);
 }
 
-__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint64_t* bar)
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c1, int c2, int c3, uint64_t* bar)
 {
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(
-            smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
+        "[%7];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3), "r"(0), "r"(smem_u32(bar))
         : "memory");
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
@@ -153,8 +161,12 @@ struct TmemCols {
 
 struct TcParams {
     int                  nx, ny, nz, kc;  // kc = Cin / 16
+    int                  strip;           // 1: strip mode, 0: tap mode
+    int                  nstages;         // pipeline depth
+    uint32_t             a_bytes, b_bytes, stage_bytes;  // per stage (stage_bytes: 128-aligned stride)
+    uint32_t             a_lbo;           // bytes between 8-channel groups in the A image (rows * 16)
     int64_t              tiles;
-    const __nv_bfloat16* wpk;  // packed weights, 27 * kc slices of N x 16 BF16
+    const __nv_bfloat16* wpk;  // packed weights: per tap Cin / 8 groups of N x 8 BF16
     const float*         bias;
     void*                y;
     int                  ldy, relu, accumulate;
@@ -163,22 +175,20 @@ struct TcParams {
 template <int N, bool F32OUT>
 __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_constant__ CUtensorMap xmap, TcParams p)
 {
-    constexpr uint32_t kABytes = kTcM * 32;  // 128 rows x 16 channels
-    constexpr uint32_t kBBytes = N * 32;     // N rows x 16 channels
-    constexpr uint32_t kStageBytes = kABytes + kBBytes;
     constexpr uint32_t kCols = TmemCols<N>::value;
     constexpr uint32_t kIdesc = idesc_bf16_f32(kTcM, N);
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t* stages = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
 
-    __shared__ uint64_t     full_bar[kTcStages], empty_bar[kTcStages], tfull_bar[2], tempty_bar[2], drain_bar;
+    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[2], tempty_bar[2], drain_bar;
     __shared__ uint32_t     tmem_base_sh;
     __shared__ volatile int abort_sh;
 
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int      warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ns = uint32_t(p.nstages);
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kTcStages; s++) {
+        for (uint32_t s = 0; s < ns; s++) {
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
@@ -199,7 +209,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
-    const int      nst = 27 * p.kc;  // pipeline stages per tile
+    const int      nst = p.strip ? 9 : 27;  // stages per tile
+    const int      ntap = p.strip ? 3 : 1;  // taps per stage
+    const uint32_t tap_b = uint32_t(N) * uint32_t(p.kc) * 32u;  // B bytes of one tap
 
     if (warp == 0 && lane == 0) {
         // ------------------------------------------------ TMA producer
@@ -210,22 +222,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
             const int     x0 = int(v0 % p.nx);
             const int64_t row = v0 / p.nx;
             const int     y0 = int(row % p.ny), z0 = int(row / p.ny);
-            for (int i = 0; i < nst && ok; i++, k++) {
-                const int t = i / p.kc, kc = i - t * p.kc;
-                const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-                const int s = int(k % kTcStages);
-                if (!(ok = mbar_wait(&empty_bar[s], ((k / kTcStages) & 1u) ^ 1u, &abort_sh))) break;
-                uint8_t* st = stages + size_t(s) * kStageBytes;
-                mbar_expect_tx(&full_bar[s], kStageBytes);
-                tma_load_4d(st, &xmap, kc * 16, x0 + dx, y0 + dy, z0 + dz, &full_bar[s]);
-                tma_load_4d(st + kABytes / 2, &xmap, kc * 16 + 8, x0 + dx, y0 + dy, z0 + dz, &full_bar[s]);
-                bulk_load(st + kABytes, p.wpk + size_t(i) * N * 16, kBBytes, &full_bar[s]);
+            for (int i = 0; i < nst; i++, k++) {
+                // strip g = 3 (dz + 1) + (dy + 1); tap t = 9 (dz + 1) + 3 (dy + 1) + (dx + 1)
+                const int dx = p.strip ? -1 : i % 3 - 1;
+                const int dy = (p.strip ? i : i / 3) % 3 - 1, dz = (p.strip ? i / 3 : i / 9) - 1;
+                const uint32_t s = k % ns;
+                if (!(ok = mbar_wait(&empty_bar[s], ((k / ns) & 1u) ^ 1u, &abort_sh))) break;
+                uint8_t* st = stages + size_t(s) * p.stage_bytes;
+                mbar_expect_tx(&full_bar[s], p.a_bytes + p.b_bytes);
+                tma_load_5d(st, &xmap, x0 + dx, y0 + dy, z0 + dz, &full_bar[s]);
+                bulk_load(st + p.stage_bytes - ((p.b_bytes + 127u) & ~127u), reinterpret_cast<const uint8_t*>(p.wpk) + size_t(i) * ntap * tap_b,
+                          p.b_bytes, &full_bar[s]);
             }
         }
         // copies still in flight land before the CTA leaves: the latest phase of
         // each stage used is complete once its bytes have arrived
-        const uint32_t used = k < uint32_t(kTcStages) ? k : uint32_t(kTcStages);
-        for (uint32_t j = k - used; j < k; j++) mbar_drain(&full_bar[j % kTcStages], (j / kTcStages) & 1u);
+        const uint32_t used = k < ns ? k : ns;
+        for (uint32_t j = k - used; j < k; j++) mbar_drain(&full_bar[j % ns], (j / ns) & 1u);
     } else if (warp == 1 && lane == 0) {
         // ------------------------------------------------ MMA issuer
         uint32_t k = 0, j = 0;
@@ -235,12 +248,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
             if (!(ok = mbar_wait(&tempty_bar[a], u ^ 1u, &abort_sh))) break;
             tc_fence_after();
             const uint32_t d = tmem + a * (kCols / 2);  // buffers at power-of-two column offsets
+            uint32_t       acc = 0;
             for (int i = 0; i < nst; i++, k++) {
-                const int s = int(k % kTcStages);
-                if (!(ok = mbar_wait(&full_bar[s], (k / kTcStages) & 1u, &abort_sh))) break;
+                const uint32_t s = k % ns;
+                if (!(ok = mbar_wait(&full_bar[s], (k / ns) & 1u, &abort_sh))) break;
                 tc_fence_after();
-                const uint32_t sa = smem_u32(stages + size_t(s) * kStageBytes);
-                mma_bf16(d, smem_desc(sa, kABytes / 2, 128), smem_desc(sa + kABytes, N * 16, 128), kIdesc, i > 0 ? 1u : 0u);
+                const uint32_t sa = smem_u32(stages + size_t(s) * p.stage_bytes);
+                const uint32_t sb = sa + p.stage_bytes - ((p.b_bytes + 127u) & ~127u);
+                for (int t = 0; t < ntap; t++) {
+                    for (int kc = 0; kc < p.kc; kc++) {
+                        // A: rows from t (the dx shift of strip mode), channel groups 2kc, 2kc + 1
+                        const uint64_t ad = smem_desc(sa + uint32_t(t) * 16u + uint32_t(kc) * 2u * p.a_lbo, p.a_lbo, 128);
+                        const uint64_t bd = smem_desc(sb + uint32_t(t) * tap_b + uint32_t(kc) * 2u * N * 16u, N * 16, 128);
+                        mma_bf16(d, ad, bd, kIdesc, acc);
+                        acc = 1;
+                    }
+                }
                 mma_commit(&empty_bar[s]);
             }
             if (ok) mma_commit(&tfull_bar[a]);
@@ -339,10 +362,7 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 template <int N, bool F32OUT>
 int launch_tc(const CUtensorMap& map, const TcParams& p, cudaStream_t s)
 {
-    constexpr uint32_t kStageBytes = kTcM * 32 + N * 32;
-    // The guard keeps every operand read of a stage inside this CTA's shared
-    // memory even for the largest stride a descriptor of this kernel encodes.
-    constexpr size_t smem = size_t(kTcStages) * kStageBytes + kTcGuard + 1024;
+    const size_t smem = size_t(p.nstages) * p.stage_bytes + 1024;  // + alignment slack
     NGB_CUDA_TRY(cudaFuncSetAttribute(conv3d_tc_kernel<N, F32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int dev = 0, sms = 0, per_sm = 0;
     NGB_CUDA_TRY(cudaGetDevice(&dev));
@@ -400,13 +420,16 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
         set_error("cuTensorMapEncodeTiled is not available from the driver");
         return NGB_ERR_CUDA;
     }
-    const int  bx = nx >= kTcM ? kTcM : nx, by = kTcM / bx;
+    // 5-D view (8 channels, x, y, z, channel group): one box per stage holds
+    // every channel, laid out group-major (the K-major core-matrix image)
+    const bool strip = nx % kTcM == 0;
+    const int  bx = strip ? kStripRows : nx, by = strip ? 1 : kTcM / nx, rows = bx * by;
     CUtensorMap map;
-    cuuint64_t dims[4] = {cuuint64_t(cin), cuuint64_t(nx), cuuint64_t(ny), cuuint64_t(nz)};
-    cuuint64_t strides[3] = {cuuint64_t(ldx) * 2, cuuint64_t(ldx) * 2 * nx, cuuint64_t(ldx) * 2 * nx * ny};
-    cuuint32_t box[4] = {8, cuuint32_t(bx), cuuint32_t(by), 1};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+    cuuint64_t  dims[5] = {8, cuuint64_t(nx), cuuint64_t(ny), cuuint64_t(nz), cuuint64_t(cin / 8)};
+    cuuint64_t  strides[4] = {cuuint64_t(ldx) * 2, cuuint64_t(ldx) * 2 * nx, cuuint64_t(ldx) * 2 * nx * ny, 16};
+    cuuint32_t  box[5] = {8, cuuint32_t(bx), cuuint32_t(by), 1, cuuint32_t(cin / 8)};
+    cuuint32_t  estr[5] = {1, 1, 1, 1, 1};
+    const CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(x), dims, strides, box, estr,
                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS) {
@@ -415,6 +438,13 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
     }
     TcParams p{};
     p.nx = nx, p.ny = ny, p.nz = nz, p.kc = cin / 16;
+    p.strip = strip ? 1 : 0;
+    p.a_lbo = uint32_t(rows) * 16u;
+    p.a_bytes = p.a_lbo * uint32_t(cin / 8);
+    p.b_bytes = uint32_t(strip ? 3 : 1) * uint32_t(cout) * uint32_t(cin) * 2u;
+    p.stage_bytes = ((p.a_bytes + 127u) & ~127u) + ((p.b_bytes + 127u) & ~127u);
+    // depth: as many stages as fit in ~108 KB (two CTAs per SM), 2 to 8
+    p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, (108u * 1024u) / p.stage_bytes)));
     p.tiles = int64_t(nx) * ny * nz / kTcM;
     p.wpk = static_cast<const __nv_bfloat16*>(wpacked);
     p.bias = bias, p.y = y, p.ldy = ldy, p.relu = relu, p.accumulate = accumulate;
