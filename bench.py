@@ -47,9 +47,15 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--extra", action="store_true", help="also time the other storage/lattice forms")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson", "learned", "accuracy"],
                     help="cavity: dense LBM (default, the headline); sphere: bGrid flow over a sphere; "
-                         "poisson: Jacobi-PCG to 1e-8")
+                         "poisson: Jacobi-PCG to 1e-8; learned: U-Net-preconditioned FCG vs Jacobi-PCG to 1e-8; "
+                         "accuracy: cavity velocity error of every storage form against FP64 after --sim-steps")
+    ap.add_argument("--train-n", type=int, default=128, help="learned: training grid size")
+    ap.add_argument("--train-pairs", type=int, default=2000, help="learned: solver-generated training pairs")
+    ap.add_argument("--epochs", type=int, default=2, help="learned: training epochs")
+    ap.add_argument("--weights", default="", help="learned: load U-Net weights from this file instead of training")
+    ap.add_argument("--save-weights", default="", help="learned: save the trained weights here")
     ap.add_argument("--scale", type=int, default=1, help="sphere case size divisor")
     ap.add_argument("--sim-steps", type=int, default=0, help="sphere: steps of the drag comparison run")
     return ap.parse_args()
@@ -423,6 +429,126 @@ def run_poisson(args):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args):
+    """Learned preconditioner: a 3-level U-Net (16/32/64 channels, BF16 tensor-core
+    convolutions) trained on residual/error pairs that CG itself produces on
+    seeded k^-2 Gaussian random fields at --train-n, then used inside flexible
+    CG (with Jacobi-PCG fallback on stagnation) on the Gaussian-source Poisson
+    problem at --n, against device Jacobi-PCG on the same problem; both to a
+    1e-8 relative true residual. `value` is the FCG solve time (seconds)."""
+    import torch
+    import neon_gb300 as ngb
+    from neon_gb300 import fcg
+    from neon_gb300.learned import UNet
+    dev = torch.device("cuda", 0)
+    ngb.lib()
+    n = args.n
+    # --- training (or loading) the network
+    net = UNet(seed=0, device=dev)
+    train = {"pairs": 0, "seconds": 0.0, "loss_first": None, "loss_last": None}
+    if args.weights:
+        net.load_state_dict(torch.load(args.weights))
+        train["weights"] = os.path.basename(args.weights)
+    else:
+        captures = (2, 5, 10, 20, 40, 80, 120, 160, 200, 250)
+        systems = max(1, args.train_pairs // len(captures))
+        t0 = time.perf_counter()
+        pairs = fcg.make_training_set(args.train_n, systems, captures, seed=2024, device=dev)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        losses = fcg.train(net, pairs, epochs=args.epochs, lr=1e-3)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        k = max(1, len(losses) // 10)
+        train.update(pairs=len(pairs), seconds=round(t2 - t0, 1), data_seconds=round(t1 - t0, 1),
+                     loss_first=round(sum(losses[:k]) / k, 4), loss_last=round(sum(losses[-k:]) / k, 4))
+        del pairs
+        torch.cuda.empty_cache()
+        if args.save_weights:
+            torch.save({k2: v.cpu() for k2, v in net.w.items()}, args.save_weights)
+    # --- the Poisson problem of the Jacobi-PCG benchmark
+    d = ngb.poisson_desc(n, n, n, "f32", 1.0)
+    c, a = ngb.gaussian_sources(n, n, n, 2024)
+    b = torch.empty(n ** 3, dtype=torch.float32, device=dev)
+    ngb.poisson_rhs(d, torch.from_numpy(c).to(dev), torch.from_numpy(a).to(dev), 8.0, b)
+    ws = ngb.cg_workspace(d, dev)
+    x = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
+    pcg = ngb.cg_solve(d, b, x, ws, tol=1e-8, max_iter=20000, refresh_every=50, check_every=50, jacobi=True)
+    # FCG: one warm-up application of the network, then the timed solve
+    net.forward(b)
+    torch.cuda.synchronize()
+    x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
+    res = fcg.fcg_solve(net, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
+    agree = float((x2 - x).norm() / x.norm())
+    # U-Net forward cost at n (device time)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        net.forward(b)
+    e1.record()
+    e1.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / 3
+    line = {"metric": "Poisson seconds to 1e-8: learned FCG vs Jacobi-PCG", "value": round(res["seconds"], 4), "unit": "s",
+            "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "dtype": "bf16",
+            "data": "synthetic (8 seeded Gaussians, sigma 8; training on seeded k^-2 fields)",
+            "config": {"workload": "Poisson 7-point, zero Dirichlet, %d^3; U-Net 16/32/64 trained at %d^3" % (n, args.train_n),
+                       "fcg_iterations": res["iterations"], "fcg_fallback": res["fallback"],
+                       "fallback_iterations": res["fallback_iterations"], "fcg_rel_residual": res["rel_residual"],
+                       "converged": res["converged"], "pcg_seconds": round(pcg["seconds"], 4),
+                       "pcg_iterations": pcg["iterations"], "speedup_vs_pcg": round(pcg["seconds"] / res["seconds"], 3),
+                       "solution_rel_diff": agree, "unet_forward_ms": round(fwd_ms, 2),
+                       "unet_forward_tflops": round(net.flops_forward(n) / fwd_ms / 1e9, 1), "training": train}}
+    print(json.dumps(line), flush=True)
+
+
+def run_accuracy(args):
+    """Lid-driven cavity at --n for --sim-steps steps (default 2000) in every
+    storage form of the lattice: MLUPS of each run and the relative L2 error of
+    its velocity field (bulk cells) against the FP64 run."""
+    import torch
+    import neon_gb300 as ngb
+    dev = torch.device("cuda", 0)
+    ngb.lib()
+    n, q = args.n, 19 if args.lattice == "d3q19" else 27
+    steps = args.sim_steps or 2000
+    ulb, re_ = 0.1, 100.0
+    V = n ** 3
+    tdts = {"f64": torch.float64, "f32": torch.float32, "f16off": torch.float16, "bf16off": torch.bfloat16}
+    u_ref, out = None, {}
+    for st in ("f64", "f32", "f16off", "bf16off"):
+        desc = ngb.lbm_dense_desc(n, n, n, q, st, ngb.cavity_omega(n, ulb, re_), ngb.lid_wall_terms(q, ulb))
+        fa = torch.empty(q * V, dtype=tdts[st], device=dev)
+        fb = torch.empty_like(fa)
+        ngb.lbm_cavity_init(desc, ulb, fa, fb)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ngb.lbm_dense_run(desc, fa, fb, steps)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        fin = fa if steps % 2 == 0 else fb
+        u = torch.zeros(3 * V, dtype=torch.float64, device=dev)
+        ngb.lbm_dense_macroscopic(desc, fin, None, u)
+        del fa, fb
+        torch.cuda.empty_cache()
+        if st == "f64":
+            u_ref = u
+            out[st] = {"mlups": round(V / (ms * 1e3), 1)}
+        else:
+            # bulk cells only (the interior; lid and wall cells carry identical set values)
+            du = (u - u_ref).view(3, n, n, n)[:, 1:-1, 1:-1, 1:-1]
+            err = float(du.norm() / u_ref.view(3, n, n, n)[:, 1:-1, 1:-1, 1:-1].norm())
+            out[st] = {"mlups": round(V / (ms * 1e3), 1), "velocity_l2_rel_err_vs_f64": err}
+            del u
+    line = {"metric": "%s cavity velocity L2 error vs FP64" % args.lattice.upper(), "value": out["f16off"]["velocity_l2_rel_err_vs_f64"],
+            "unit": "relative L2", "n_gpus": 1, "steps": steps, "warmup": 0, "higher_is_better": False, "dtype": "f32",
+            "data": "synthetic (lid-driven cavity set-up, equilibrium start)",
+            "config": {"workload": "%s BGK lid-driven cavity, dense %d^3, %d steps" % (args.lattice.upper(), n, steps),
+                       "lid_u": ulb, "Re": re_, "forms": out,
+                       "f16_speedup_vs_f32": round(out["f16off"]["mlups"] / out["f32"]["mlups"], 3)}}
+    print(json.dumps(line), flush=True)
+
+
 def time_variant(ngb, torch, dev, n, lat, st, args):
     q = 19 if lat == "d3q19" else 27
     ulb = 0.1
@@ -456,6 +582,10 @@ def main():
         run_sphere(args)
     elif args.workload == "poisson":
         run_poisson(args)
+    elif args.workload == "learned":
+        run_learned(args)
+    elif args.workload == "accuracy":
+        run_accuracy(args)
     else:
         run_ours(args)
 

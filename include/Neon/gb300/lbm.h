@@ -4,7 +4,7 @@
 // benchmarks/lbm-lid-driven-cavity-flow/src/LbmTools.h: an application keeps
 // its grids, fields and Skeleton and swaps LbmContainers<...>::iteration /
 // computeWallNghMask for these. Population fields hold `double` or `float`
-// (f), or `__half` / `__nv_bfloat16` (g = f - w); the cell-type field holds
+// (f), or `__nv_bfloat16` (g = f - w) / `__half` (2^14 (f - w), NGB_F16OFF_SCALE); the cell-type field holds
 // one uint32 per cell in the packed form NGB_MAKE_FLAG(mask, classification)
 // (CellType.h:3-35 values for the classification).
 #pragma once

@@ -37,7 +37,11 @@ int ngb_version(void);
  * Lattice-Boltzmann populations
  * ---------------------------------------------------------------------- */
 
-/* How populations are held in HBM. The *_OFF forms hold g_q = f_q - w_q. */
+/* How populations are held in HBM. The *_OFF forms hold g_q = f_q - w_q:
+ * BF16OFF as bf16(g_q); F16OFF as fp16(2^14 g_q) (NGB_F16OFF_SCALE), which
+ * keeps the small offsets of slow flow regions out of FP16's subnormal range
+ * (2^14 is exact, so the FP32 collision computes the same values either way). */
+#define NGB_F16OFF_SCALE 16384.0f
 typedef enum {
     NGB_STORE_F64 = 0,
     NGB_STORE_F32 = 1,

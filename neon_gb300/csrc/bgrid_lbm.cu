@@ -24,7 +24,10 @@ __device__ __forceinline__ double as_f<double>(double v, double) { return v; }
 template <>
 __device__ __forceinline__ double as_f<float>(float v, double) { return v; }
 template <>
-__device__ __forceinline__ double as_f<__half>(__half v, double w) { return double(__half2float(v)) + double(float(w)); }
+__device__ __forceinline__ double as_f<__half>(__half v, double w)
+{
+    return double(__half2float(v) * (1.0f / NGB_F16OFF_SCALE)) + double(float(w));
+}
 template <>
 __device__ __forceinline__ double as_f<__nv_bfloat16>(__nv_bfloat16 v, double w)
 {
@@ -70,6 +73,39 @@ __device__ __forceinline__ uint32_t bgrid_lidbits(const uint32_t* __restrict__ f
     return lid;
 }
 
+// Thread -> voxel of the block. Threads 0..215 take the 6^3 inner voxels
+// (i, j, k in 1..6), whose 19 or 27 pull sources all lie in the block itself;
+// threads 216..511 take the 296 voxels on the block's faces, in k-major order:
+// the k = 0 face (64), the rings of k = 1..6 (28 each: row j = 0, row j = 7,
+// then i = 0 / 7 of rows 1..6), the k = 7 face (64). Warps of inner voxels
+// then never run the neighbour-block arithmetic.
+constexpr int kInnerVoxels = 216;
+__device__ __forceinline__ void bgrid_thread_voxel(int t, int& i, int& j, int& k)
+{
+    if (t < kInnerVoxels) {
+        i = 1 + t % 6, j = 1 + (t / 6) % 6, k = 1 + t / 36;
+        return;
+    }
+    const int r = t - kInnerVoxels;
+    if (r < 64) {
+        i = r & 7, j = r >> 3, k = 0;
+    } else if (r < 64 + 6 * 28) {
+        const int u = r - 64, ring = u % 28;
+        k = 1 + u / 28;
+        if (ring < 8) {
+            i = ring, j = 0;
+        } else if (ring < 16) {
+            i = ring - 8, j = 7;
+        } else {
+            const int w = ring - 16;
+            j = 1 + (w >> 1), i = (w & 1) ? 7 : 0;
+        }
+    } else {
+        const int w = r - 64 - 6 * 28;
+        i = w & 7, j = w >> 3, k = 7;
+    }
+}
+
 // Source pointer of direction q for this voxel: the pulled neighbour
 // population, or the voxel's own opposite population when q is masked (the
 // half-way bounce-back rule). A source outside every block is taken as a wall,
@@ -90,15 +126,26 @@ __device__ __forceinline__ const S* bgrid_src(const S* __restrict__ fin, const u
 }
 
 template <int Q, typename S, bool F64>
-__global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+__global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 27 ? (sizeof(S) == 2 ? 2 : 3) : (sizeof(S) == 2 ? 3 : 4)))
+    bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
                                                                  const uint32_t* __restrict__ flags,
                                                                  BParams<typename std::conditional<F64, double, float>::type> p)
 {
     using L = Lattice<Q>;
     const uint32_t      b = blockIdx.x;
-    const int           v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
+    // 16-bit storage is issue-bound: inner voxels first (see bgrid_thread_voxel);
+    // FP32 is bandwidth-bound and keeps the natural order (whole 32-byte rows per access)
+    constexpr bool      kPermute = sizeof(S) == 2;
+    const int           t = threadIdx.x;
+    const bool          inner = kPermute && t < kInnerVoxels;
+    int                 i, j, k;
+    if (kPermute)
+        bgrid_thread_voxel(t, i, j, k);
+    else
+        i = t & 7, j = (t >> 3) & 7, k = t >> 6;
+    const int           v = i + 8 * j + 64 * k;
     __shared__ uint32_t sconn[27];  // this block's neighbour blocks
-    if (v < 27) sconn[v] = __ldg(p.conn + size_t(b) * 27 + v);
+    if (t < 27) sconn[t] = __ldg(p.conn + size_t(b) * 27 + t);
     const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
     __syncthreads();
     const int    cls = flag_class(f);
@@ -116,15 +163,23 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgr
     const uint32_t m = flag_mask(f);
     const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m) : 0u;
 
+    // own voxel of plane 0: inner voxels without walls read every source at a
+    // fixed offset from it (no neighbour-block arithmetic)
+    const S* own = fin + bq * kBlockVoxels + v;
     if constexpr (F64) {
         S pop[Q];
+        if (inner && m == 0) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            bool      masked;
-            const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
-            const int o = L::opp(q);
-            pop[q] = __ldg(src);
-            if (masked) pop[q] = pop[q] + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            for (int q = 0; q < Q; q++) pop[q] = __ldg(own + q * kBlockVoxels - (L::cx(q) + 8 * L::cy(q) + 64 * L::cz(q)));
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                bool      masked;
+                const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
+                const int o = L::opp(q);
+                pop[q] = __ldg(src);
+                if (masked) pop[q] = pop[q] + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            }
         }
         S out[Q];
         bgk_f64_ref<Q, S>(pop, p.omega, out);
@@ -132,16 +187,22 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgr
         for (int q = 0; q < Q; q++) fout[(bq + q) * kBlockVoxels + v] = out[q];
     } else {
         float g[Q];
+        if (inner && m == 0) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            bool      masked;
-            const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
-            const int o = L::opp(q);
-            // w(opp q) == w(q), so one conversion serves both cases
-            g[q] = PairIO<S>::to_g1(__ldg(src), float(L::w(q)));
-            if (masked) g[q] = g[q] + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            for (int q = 0; q < Q; q++)
+                g[q] = PairIO<S>::to_g1(__ldg(own + q * kBlockVoxels - (L::cx(q) + 8 * L::cy(q) + 64 * L::cz(q))), float(L::w(q)));
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                bool      masked;
+                const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
+                const int o = L::opp(q);
+                // w(opp q) == w(q), so one conversion serves both cases
+                g[q] = PairIO<S>::to_g1(__ldg(src), float(L::w(q)));
+                if (masked) g[q] = g[q] + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            }
         }
-        bgk_shifted<Q, float>(g, p.omega);
+        bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
 #pragma unroll
         for (int q = 0; q < Q; q++) PairIO<S>::store1(fout + (bq + q) * kBlockVoxels + v, g[q], float(L::w(q)));
     }
@@ -279,8 +340,10 @@ int launch_bgrid_lbm(const ngb_bgrid_desc* d, const void* fin, void* fout, const
     } else {
         BParams<float> p{};
         p.omega = float(d->omega);
+        // FP16 values are 2^14 g: the wall terms added to them scale alike
+        const float up = d->storage == NGB_STORE_F16OFF ? NGB_F16OFF_SCALE : 1.0f;
         for (int c = 0; c < 2; c++)
-            for (int q = 0; q < 27; q++) p.wall[c][q] = float(d->wall_term[c][q]);
+            for (int q = 0; q < 27; q++) p.wall[c][q] = float(d->wall_term[c][q]) * up;
         p.mask = d->mask, p.conn = d->conn;
 #define NGB_B(QQ, T) \
     bgrid_lbm_kernel<QQ, T, false><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)

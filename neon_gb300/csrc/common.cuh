@@ -108,32 +108,17 @@ __host__ __device__ inline uint32_t make_flag(uint32_t mask, int cls) { return (
 __host__ __device__ inline bool is_fluid_class(int c) { return c == NGB_CELL_BULK || c == NGB_CELL_OUTLET; }
 
 // ------------------------------------------------------------------ storage
-// Storage policies: how a population value is held in HBM and turned into the
-// compute type. The "off" forms hold g = f - w_q in 16 bits.
-struct StoreF64 {
-    using T = double;
-    static constexpr int id = NGB_STORE_F64;
+// The 16-bit "off" forms hold g = f - w_q; FP16 holds it scaled by 2^14
+// (NGB_F16OFF_SCALE). log2 of the scale of each stored type:
+template <typename S>
+struct StoreScale {
+    static constexpr int log2 = 0;
 };
-struct StoreF32 {
-    using T = float;
-    static constexpr int id = NGB_STORE_F32;
+template <>
+struct StoreScale<__half> {
+    static constexpr int log2 = 14;
 };
-struct StoreF16Off {
-    using T = __half;
-    static constexpr int id = NGB_STORE_F16OFF;
-};
-struct StoreBF16Off {
-    using T = __nv_bfloat16;
-    static constexpr int id = NGB_STORE_BF16OFF;
-};
-
-// g = f - w (compute type float) from the stored value.
-__device__ __forceinline__ float load_g(const float* p, float w) { return __ldg(p) - w; }
-__device__ __forceinline__ float load_g(const __half* p, float) { return __half2float(__ldg(p)); }
-__device__ __forceinline__ float load_g(const __nv_bfloat16* p, float) { return __bfloat162float(__ldg(p)); }
-__device__ __forceinline__ void  store_g(float* p, float g, float w) { *p = w + g; }
-__device__ __forceinline__ void  store_g(__half* p, float g, float) { *p = __float2half_rn(g); }
-__device__ __forceinline__ void  store_g(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
+static_assert(float(1 << StoreScale<__half>::log2) == NGB_F16OFF_SCALE, "FP16 storage scale");
 
 inline size_t storage_bytes(int storage)
 {

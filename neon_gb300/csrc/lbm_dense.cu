@@ -165,7 +165,7 @@ __device__ __forceinline__ double pop_value(const S* p, double w, int off)
     if constexpr (std::is_same<S, double>::value || std::is_same<S, float>::value) {
         return double(*p);
     } else if constexpr (std::is_same<S, __half>::value) {
-        return double(__half2float(*p)) + double(float(w));
+        return double(__half2float(*p) * (1.0f / NGB_F16OFF_SCALE)) + double(float(w));
     } else {
         return double(__bfloat162float(*p)) + double(float(w));
     }

@@ -17,8 +17,13 @@ int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const 
         o.own[q] = q * p.stride * esz;
         o.pull[q] = (q * p.stride - cx - cy * sy - cz * sz) * esz;
     }
+    // FP16 values are 2^14 g: the wall terms added to them scale alike
+    DenseParams<float> ps = p;
+    if (storage == NGB_STORE_F16OFF)
+        for (int c = 0; c < 2; c++)
+            for (int q = 0; q < 27; q++) ps.wall[c][q] = p.wall[c][q] * NGB_F16OFF_SCALE;
 #define NGB_ONE(QQ, T) \
-    lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p, o)
+    lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, ps, o)
     const bool q19 = Q == 19;
     switch (storage) {
         case NGB_STORE_F32:

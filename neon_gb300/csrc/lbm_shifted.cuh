@@ -170,9 +170,15 @@ __device__ __forceinline__ V cdot(int q, V u3x, V u3y, V u3z)
 }
 
 // Shifted BGK on V = float (one cell) or float2 (a cell pair): g -> g' in place.
-template <int Q, typename V>
+// SH: the values are G = 2^SH g (FP16 storage). Every quantity of the
+// sequence below is then exactly 2^SH times its unscaled value (power-of-two
+// scaling commutes with rounding) once drho and 1/rho are taken back by
+// 2^-SH and the weights enter as 2^SH w: the stored result is the same
+// rounding of the same number.
+template <int Q, typename V, int SH = 0>
 __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
 {
+    constexpr float kUp = float(1u << SH), kDown = 1.0f / kUp;
     using L = Lattice<Q>;
     V drho = g[0];
 #pragma unroll
@@ -194,8 +200,10 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
         }
     }
     const V jx = sub2(jp[0], jm[0]), jy = sub2(jp[1], jm[1]), jz = sub2(jp[2], jm[2]);
+    if constexpr (SH != 0) drho = mul2(drho, splat<V>(kDown));
     const V rho = add2(splat<V>(1.f), drho);
-    const V inv = recip(rho);
+    V       inv = recip(rho);
+    if constexpr (SH != 0) inv = mul2(inv, splat<V>(kDown));
     const V ux = mul2(jx, inv), uy = mul2(jy, inv), uz = mul2(jz, inv);
     const V usq = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
     const V rus = mul2(rho, mul2(splat<V>(1.5f), usq));
@@ -204,7 +212,7 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
     V       wr[WeightClass<Q>::n], wb[WeightClass<Q>::n];
 #pragma unroll
     for (int k = 0; k < WeightClass<Q>::n; k++) {
-        const float wk = float(WeightClass<Q>::w(k));
+        const float wk = float(WeightClass<Q>::w(k)) * kUp;  // exact
         wr[k] = mul2(splat<V>(wk), rho);
         wb[k] = mul2(splat<V>(wk), base);
     }
@@ -239,7 +247,7 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* _
     if (cls != NGB_CELL_BULK) return;
     float g[Q];
     pull_one<Q, S>(fin, cell, mask, lidbits, p, o, g);
-    bgk_shifted<Q, float>(g, p.omega);
+    bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
     char* D = reinterpret_cast<char*>(fout + cell);
 #pragma unroll
     for (int q = 0; q < Q; q++) PairIO<S>::store1(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)));

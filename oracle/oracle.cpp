@@ -24,6 +24,8 @@ using namespace oracle;
 namespace {
 
 enum Storage { ST_F64 = 0, ST_F32 = 1, ST_F16OFF = 2, ST_BF16OFF = 3 };
+// FP16 offset storage holds fp16(2^14 g) (the library's NGB_F16OFF_SCALE); both factors are exact
+constexpr float kF16Up = 16384.0f, kF16Down = 1.0f / 16384.0f;
 enum ComputeMode { CM_REFERENCE = 0, CM_GENERIC = 1, CM_SHIFTED = 2 };
 
 // Flags are exchanged with the tests in the packed form used by the GPU
@@ -172,7 +174,8 @@ int orc_lbm_run(int nx, int ny, int nz, int Q, int storage, int mode, int comput
                                 [](float g, int q) { return float(weight(QQ, q)) + g; }, threads);
             } else if (storage == ST_F16OFF) {
                 shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
-                                [](uint16_t v, int) { return f16_to_f32(v); }, [](float g, int) { return f32_to_f16(g); },
+                                [](uint16_t v, int) { return f16_to_f32(v) * kF16Down; },
+                                [](float g, int) { return f32_to_f16(g * kF16Up); },
                                 threads);
             } else if (storage == ST_BF16OFF) {
                 shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
@@ -200,8 +203,8 @@ int orc_lbm_run(int nx, int ny, int nz, int Q, int storage, int mode, int comput
                                    [](float v, int) { return C(v); }, [](C v, int) { return float(v); }, threads);
             } else if (storage == ST_F16OFF) {
                 generic_run<C, QQ>(nx, ny, nz, flag.data(), omega, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
-                                   [](uint16_t v, int q) { return C(f16_to_f32(v)) + C(float(weight(QQ, q))); },
-                                   [](C v, int q) { return f32_to_f16(float(v - C(float(weight(QQ, q))))); }, threads);
+                                   [](uint16_t v, int q) { return C(f16_to_f32(v) * kF16Down) + C(float(weight(QQ, q))); },
+                                   [](C v, int q) { return f32_to_f16(float(v - C(float(weight(QQ, q)))) * kF16Up); }, threads);
             } else {
                 generic_run<C, QQ>(nx, ny, nz, flag.data(), omega, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
                                    [](uint16_t v, int q) { return C(bf16_to_f32(v)) + C(float(weight(QQ, q))); },
@@ -235,7 +238,8 @@ int orc_velocity(int nx, int ny, int nz, int Q, int storage, const double* wall,
         switch (storage) {
             case ST_F64: return static_cast<const double*>(pop)[i];
             case ST_F32: return static_cast<const float*>(pop)[i];
-            case ST_F16OFF: return double(f16_to_f32(static_cast<const uint16_t*>(pop)[i])) + double(float(weight(Q, q)));
+            case ST_F16OFF:
+                return double(f16_to_f32(static_cast<const uint16_t*>(pop)[i]) * kF16Down) + double(float(weight(Q, q)));
             default: return double(bf16_to_f32(static_cast<const uint16_t*>(pop)[i])) + double(float(weight(Q, q)));
         }
     };

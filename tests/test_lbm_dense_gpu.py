@@ -129,6 +129,8 @@ def test_single_step_from_developed_state(ngb, orc, cuda, q, storage):
         tsrc = torch.from_numpy(src.copy())
     else:
         g = (f.astype(np.float32) - w[:, None].astype(np.float32))
+        if storage == 2:  # FP16 offsets are stored scaled by 2^14 (NGB_F16OFF_SCALE)
+            g = g * np.float32(16384.0)
         tsrc = torch.from_numpy(g.ravel()).to(torch.float16 if storage == 2 else torch.bfloat16)
         src = tsrc.view(torch.int16).numpy().view(np.uint16).copy()
     a = src.copy()
