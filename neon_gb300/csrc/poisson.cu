@@ -123,7 +123,15 @@ __device__ __forceinline__ int n_valid(const Dom& d, int x, int y, int z)
 template <typename T>
 __device__ __forceinline__ T invdiag_of(const Dom& d, int x, int y, int z, int64_t i, int jacobi)
 {
-    if (!jacobi || is_fixed(d, x, y, z, i)) return T(1);
+    if (!jacobi) return T(1);
+    if (!d.bd) {  // analytic box: faces are Fixed, every Free cell has six valid neighbours
+        if (x == 0 || y == 0 || z == 0 || x == d.nx - 1 || y == d.ny - 1 || z == d.nz - 1) return T(1);
+        if constexpr (std::is_same<T, float>::value)
+            return d.invf[6];
+        else
+            return d.invd[6];
+    }
+    if (is_fixed(d, x, y, z, i)) return T(1);
     // constant indices only: a runtime index into the parameter array would
     // copy it to local memory
     const int n = n_valid(d, x, y, z);
@@ -295,9 +303,36 @@ __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const 
     }
 }
 
-// pass A: beta from device scalars; p' = z + beta p at the cell and its
-// neighbours; s = A p'; pAp = <p', s>; alpha = rz / pAp.
+// pass A: beta from device scalars; p' = z + beta p; s = A p'; pAp = <p', s>;
+// alpha = rz / pAp. 2.5-D blocking: a CTA takes a 32 x 8 (x, y) tile and
+// marches along z through a chunk of kZC planes. Each thread computes p' of its
+// own cell once per plane (two loads); 84 threads also compute the in-plane
+// halo into shared memory; the z neighbours stay in registers. So every p'
+// value is formed from r and p once per tile instead of once per stencil use.
+constexpr int kTX = 32, kTY = 8, kZC = 64;
+constexpr int kHalo = 2 * (kTX + 2) + 2 * kTY;  // halo cells of one plane
+static_assert(kTX * kTY == kBX && kHalo <= kBX, "tile shape");
+
+__host__ __device__ inline int pass_a_items(const Dom& d)
+{
+    return ((d.nx + kTX - 1) / kTX) * ((d.ny + kTY - 1) / kTY) * ((d.nz + kZC - 1) / kZC);
+}
+
 template <typename T>
+__device__ __forceinline__ T invdiag6(const Dom& d, int jac)
+{
+    if (!jac) return T(1);
+    if constexpr (std::is_same<T, float>::value)
+        return d.invf[6];
+    else
+        return d.invd[6];
+}
+
+// BOX: the analytic box (no boundary array): faces are Fixed, Free cells have
+// six valid neighbours, so the Jacobi diagonal of a column depends only on
+// whether it lies on an x/y face and on z. Otherwise every value goes through
+// invdiag_of / is_fixed (boundary array, Free cells on faces).
+template <typename T, bool BOX>
 __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, const T* __restrict__ r, const T* __restrict__ p_old,
                                                         T* __restrict__ p_new, T* __restrict__ s, double* partials)
 {
@@ -306,54 +341,111 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     const double beta = st->rz_prev == 0.0 ? 0.0 : st->rz / st->rz_prev;
     const T      tb = T(beta);
     const T      invh2 = T(1.0) / (T(d.h) * T(d.h));
-    DotAcc<T>    acc;
-    auto         pn = [&](int x, int y, int z, int64_t j) -> T { return T(invdiag_of<T>(d, x, y, z, j, jac) * r[j]) + tb * p_old[j]; };
-    // diagonal inverse of a Free cell with six valid neighbours (interior fast path)
-    T dg = T(1);
-    if (jac) {
-        if constexpr (std::is_same<T, float>::value)
-            dg = d.invf[6];
-        else
-            dg = d.invd[6];
+    const T      dg6 = invdiag6<T>(d, jac);
+    __shared__ T planes[2][kTY + 2][kTX + 2];  // double-buffered: one barrier per plane
+    const int    lx = threadIdx.x % kTX, ly = threadIdx.x / kTX;
+    // this thread's halo cell (threads < kHalo), in tile coordinates
+    int        hx = 0, hy = 0;
+    const bool halo = threadIdx.x < kHalo;
+    if (threadIdx.x < kTX + 2) {
+        hx = threadIdx.x - 1, hy = -1;
+    } else if (threadIdx.x < 2 * (kTX + 2)) {
+        hx = threadIdx.x - (kTX + 2) - 1, hy = kTY;
+    } else if (halo) {
+        const int k = threadIdx.x - 2 * (kTX + 2);
+        hx = (k & 1) ? kTX : -1, hy = k >> 1;
     }
-    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
-        const Cell c = seg_cell(d, seg);
-        if (c.x < 0) continue;
-        // Fast path: in the analytic box, a cell two or more cells from every
-        // face has itself and its six neighbours Free with six valid
-        // neighbours each (the same values as the general path, fewer checks).
-        if (!d.bd && c.x >= 2 && c.y >= 2 && c.z >= 2 && c.x < d.nx - 2 && c.y < d.ny - 2 && c.z < d.nz - 2) {
-            const int64_t sy = d.nx, sz = int64_t(d.nx) * d.ny, i = c.i;
-            const T       pc = T(dg * r[i]) + tb * p_old[i];
-            T             sum = T(0);
-            sum = sum + (T(dg * r[i + 1]) + tb * p_old[i + 1]);
-            sum = sum + (T(dg * r[i - 1]) + tb * p_old[i - 1]);
-            sum = sum + (T(dg * r[i + sy]) + tb * p_old[i + sy]);
-            sum = sum + (T(dg * r[i - sy]) + tb * p_old[i - sy]);
-            sum = sum + (T(dg * r[i + sz]) + tb * p_old[i + sz]);
-            sum = sum + (T(dg * r[i - sz]) + tb * p_old[i - sz]);
-            const T sc = (-sum + T(6) * pc) * invh2;
-            p_new[i] = pc;
-            s[i] = sc;
-            acc.add(pc, sc);
-            continue;
+    const int     ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTY - 1) / kTY;
+    const int     items = pass_a_items(d);
+    const int64_t pl = int64_t(d.nx) * d.ny;
+    DotAcc<T>     acc;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int tx = item % ntx, rest = item / ntx, ty = rest % nty, zc = rest / nty;
+        const int x = tx * kTX + lx, y = ty * kTY + ly, z0 = zc * kZC, z1 = min(z0 + kZC, d.nz);
+        const int gx = tx * kTX + hx, gy = ty * kTY + hy;
+        const bool    own = x < d.nx && y < d.ny;
+        const bool    hown = halo && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
+        const int64_t oc = own ? x + int64_t(d.nx) * y : 0, hc = hown ? gx + int64_t(d.nx) * gy : 0;
+        const bool    oface = x == 0 || y == 0 || x == d.nx - 1 || y == d.ny - 1;
+        const bool    hface = gx == 0 || gy == 0 || gx == d.nx - 1 || gy == d.ny - 1;
+        // raw (r, p) of a column at plane zz; zeros outside the grid
+        auto load = [&](bool ok, int64_t col, int zz, T& rv, T& pv) {
+            if (ok && zz >= 0 && zz < d.nz) {
+                rv = r[col + zz * pl];
+                pv = p_old[col + zz * pl];
+            } else {
+                rv = T(0), pv = T(0);
+            }
+        };
+        // p' of a column at plane zz from its raw values; 0 outside the grid
+        auto pn = [&](bool ok, bool face, int64_t col, int xx, int yy, int zz, T rv, T pv) -> T {
+            if (!ok || zz < 0 || zz >= d.nz) return T(0);
+            T dgv;
+            if constexpr (BOX)
+                dgv = (face || zz == 0 || zz == d.nz - 1) ? T(1) : dg6;
+            else
+                dgv = invdiag_of<T>(d, xx, yy, zz, col + zz * pl, jac);
+            return T(dgv * rv) + tb * pv;
+        };
+        T ra, pa, rb, pb, r1, p1, hr, hp;
+        load(own, oc, z0 - 1, ra, pa);
+        load(own, oc, z0, rb, pb);
+        load(own, oc, z0 + 1, r1, p1);
+        load(hown, hc, z0, hr, hp);
+        T pprev = pn(own, oface, oc, x, y, z0 - 1, ra, pa);
+        T pc = pn(own, oface, oc, x, y, z0, rb, pb);
+        // the previous item's last plane may share a buffer with this item's first
+        __syncthreads();
+        int64_t i = oc + int64_t(z0) * pl;  // this thread's cell of plane z
+        for (int z = z0; z < z1; z++, i += pl) {
+            // one plane of lookahead: these loads are used in the next iteration
+            T r2, p2, hr2, hp2;
+            load(own, oc, z + 2, r2, p2);
+            load(hown, hc, z + 1, hr2, hp2);
+            const T pnext = pn(own, oface, oc, x, y, z + 1, r1, p1);
+            const T hv = pn(hown, hface, hc, gx, gy, z, hr, hp);
+            // buffer z & 1 was last read in iteration z - 2, before the barrier of iteration z - 1
+            T (*plane)[kTX + 2] = planes[z & 1];
+            plane[ly + 1][lx + 1] = pc;
+            if (halo) plane[hy + 1][hx + 1] = hv;
+            __syncthreads();
+            if (own) {
+                T             sc;
+                const bool    inner = !oface && z >= 1 && z < d.nz - 1;
+                if (BOX || (!d.bd && inner)) {
+                    if (inner) {
+                        T sum = T(0);
+                        sum = sum + plane[ly + 1][lx + 2];
+                        sum = sum + plane[ly + 1][lx];
+                        sum = sum + plane[ly + 2][lx + 1];
+                        sum = sum + plane[ly][lx + 1];
+                        sum = sum + pnext;
+                        sum = sum + pprev;
+                        sc = (-sum + T(6) * pc) * invh2;
+                    } else {
+                        sc = pc;  // Fixed face row
+                    }
+                } else if (is_fixed(d, x, y, z, i)) {
+                    sc = pc;
+                } else {  // neighbours in the oracle's order +x, -x, +y, -y, +z, -z, valid ones only
+                    T   sum = T(0);
+                    int n = 0;
+                    if (x + 1 < d.nx) sum = sum + plane[ly + 1][lx + 2], n++;
+                    if (x > 0) sum = sum + plane[ly + 1][lx], n++;
+                    if (y + 1 < d.ny) sum = sum + plane[ly + 2][lx + 1], n++;
+                    if (y > 0) sum = sum + plane[ly][lx + 1], n++;
+                    if (z + 1 < d.nz) sum = sum + pnext, n++;
+                    if (z > 0) sum = sum + pprev, n++;
+                    sc = (-sum + T(n) * pc) * invh2;
+                }
+                p_new[i] = pc;
+                s[i] = sc;
+                acc.add(pc, sc);
+            }
+            pprev = pc;
+            pc = pnext;
+            r1 = r2, p1 = p2, hr = hr2, hp = hp2;
         }
-        const T pc = pn(c.x, c.y, c.z, c.i);
-        T       sc;
-        if (is_fixed(d, c.x, c.y, c.z, c.i)) {
-            sc = pc;
-        } else {
-            T   sum = T(0);
-            int n = 0;
-            for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int x, int y, int z, int64_t j) {
-                sum = sum + pn(x, y, z, j);
-                n++;
-            });
-            sc = (-sum + T(n) * pc) * invh2;
-        }
-        p_new[c.i] = pc;
-        s[c.i] = sc;
-        acc.add(pc, sc);
     }
     double v[1] = {acc.value()};
     double out[1];
@@ -363,36 +455,45 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     }
 }
 
-// pass B: x_lo += alpha p; r -= alpha s; rz' = <r, z>; rr = <r, r>.
-template <typename T>
+// pass B: x_lo += alpha p; r -= alpha s; rz' = <r, z>; rr = <r, r>. The
+// work items of pass A (32 x 8 columns, chunks of kZC planes): each thread
+// walks its column with a running index, the loads of the next plane in
+// flight while the current one is updated; BOX as in pass A.
+template <typename T, bool BOX>
 __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* __restrict__ xlo, const T* __restrict__ p,
                                                         T* __restrict__ r, const T* __restrict__ s, double* partials)
 {
     if (st->converged) return;
-    const int jac = st->jacobi;
-    const T   ta = T(st->alpha);
-    DotAcc<T> a0, a1;
-    // two segments per trip: both cells' loads are in flight together
-    for (int64_t seg = blockIdx.x; seg < d.segs; seg += 2 * int64_t(gridDim.x)) {
-        Cell      c[2];
-        T         xv[2], pv[2], rv[2], sv[2];
-        const int cnt = (seg + gridDim.x < d.segs) ? 2 : 1;
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            c[u] = seg_cell(d, seg + u * int64_t(gridDim.x));
-            if (u >= cnt) c[u].x = -1;
-            if (c[u].x < 0) continue;
-            xv[u] = xlo[c[u].i], pv[u] = p[c[u].i], rv[u] = r[c[u].i], sv[u] = s[c[u].i];
-        }
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            if (c[u].x < 0) continue;
-            xlo[c[u].i] = xv[u] + ta * pv[u];
-            const T rn = rv[u] - ta * sv[u];
-            r[c[u].i] = rn;
-            const T z = T(invdiag_of<T>(d, c[u].x, c[u].y, c[u].z, c[u].i, jac) * rn);
-            a0.add(rn, z);
-            a1.add(rn, rn);
+    const int     jac = st->jacobi;
+    const T       ta = T(st->alpha);
+    const T       dg6 = invdiag6<T>(d, jac);
+    const int     lx = threadIdx.x % kTX, ly = threadIdx.x / kTX;
+    const int     ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTY - 1) / kTY;
+    const int     items = pass_a_items(d);
+    const int64_t pl = int64_t(d.nx) * d.ny;
+    DotAcc<T>     a0, a1;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int tx = item % ntx, rest = item / ntx, ty = rest % nty, zc = rest / nty;
+        const int x = tx * kTX + lx, y = ty * kTY + ly, z0 = zc * kZC, z1 = min(z0 + kZC, d.nz);
+        if (x >= d.nx || y >= d.ny) continue;  // no barrier in this kernel
+        const bool oface = x == 0 || y == 0 || x == d.nx - 1 || y == d.ny - 1;
+        int64_t    i = x + int64_t(d.nx) * y + int64_t(z0) * pl;
+        T          xv = xlo[i], pv = p[i], rv = r[i], sv = s[i];
+        for (int z = z0; z < z1; z++, i += pl) {
+            T xn = T(0), pn = T(0), rn = T(0), sn = T(0);
+            if (z + 1 < z1) xn = xlo[i + pl], pn = p[i + pl], rn = r[i + pl], sn = s[i + pl];
+            xlo[i] = xv + ta * pv;
+            const T rnew = rv - ta * sv;
+            r[i] = rnew;
+            T dgv;
+            if constexpr (BOX)
+                dgv = (oface || z == 0 || z == d.nz - 1) ? T(1) : dg6;
+            else
+                dgv = invdiag_of<T>(d, x, y, z, i, jac);
+            const T zz = T(dgv * rnew);
+            a0.add(rnew, zz);
+            a1.add(rnew, rnew);
+            xv = xn, pv = pn, rv = rn, sv = sn;
         }
     }
     double v[2] = {a0.value(), a1.value()};
@@ -490,6 +591,8 @@ int validate(const ngb_poisson_desc* d)
     NGB_CHECK_ARG(d->field == NGB_STORE_F32 || d->field == NGB_STORE_F64, "field must be NGB_STORE_F32 or NGB_STORE_F64");
     NGB_CHECK_ARG(d->h > 0, "h must be positive");
     NGB_CHECK_ARG(make_dom(d).segs < (int64_t(1) << 31), "grid too large (ny * nz * ceil(nx / 256) >= 2^31)");
+    NGB_CHECK_ARG(int64_t((d->nx + kTX - 1) / kTX) * ((d->ny + kTY - 1) / kTY) * ((d->nz + kZC - 1) / kZC) < (int64_t(1) << 31),
+                  "grid too large for the CG tiling");
     return NGB_OK;
 }
 
@@ -552,8 +655,14 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
         for (int it = 0; it < per; it++) {
             T* pa = (it % 2 == 0) ? p0 : p1;
             T* pb = (it % 2 == 0) ? p1 : p0;
-            cg_pass_a_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
-            cg_pass_b_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
+            if (d.bd)
+                cg_pass_a_kernel<T, false><<<grid, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
+            else
+                cg_pass_a_kernel<T, true><<<grid, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
+            if (d.bd)
+                cg_pass_b_kernel<T, false><<<grid, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
+            else
+                cg_pass_b_kernel<T, true><<<grid, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
             cg_refresh1_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, x, xlo);
             cg_refresh2_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, b, x, r, w.partials);
         }
