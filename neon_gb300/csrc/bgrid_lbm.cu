@@ -138,12 +138,13 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 27 ? (sizeof(S) 
     constexpr bool      kPermute = sizeof(S) == 2;
     const int           t = threadIdx.x;
     const bool          inner = kPermute && t < kInnerVoxels;
-    int                 i, j, k;
-    if (kPermute)
+    int                 i, j, k, v;
+    if constexpr (kPermute) {
         bgrid_thread_voxel(t, i, j, k);
-    else
-        i = t & 7, j = (t >> 3) & 7, k = t >> 6;
-    const int           v = i + 8 * j + 64 * k;
+        v = i + 8 * j + 64 * k;
+    } else {
+        v = t, i = t & 7, j = (t >> 3) & 7, k = t >> 6;
+    }
     __shared__ uint32_t sconn[27];  // this block's neighbour blocks
     if (t < 27) sconn[t] = __ldg(p.conn + size_t(b) * 27 + t);
     const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);

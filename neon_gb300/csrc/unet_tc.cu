@@ -2,28 +2,31 @@
 // 5th-generation tensor cores (tcgen05), as an implicit GEMM:
 //   D[v][co] = sum_{tap t, channel c} x[ngh(v, t)][c] * w[co][t][c]
 // M = 128 consecutive voxels (one tile), N = Cout, K = 27 taps x Cin, in
-// tcgen05.mma steps of M 128, N Cout, K 16.
+// tcgen05.mma steps of M 128, N Cout, K 16 (one 16-channel chunk of one tap).
 //
-// Operand staging (TMA, one 5-D box per stage: 8 channels x voxels x all
-// Cin / 8 channel groups, so the shared-memory image is already the
-// no-swizzle K-major layout: 8-row x 16-byte core matrices, 8-row groups
-// 128 B apart (SBO), 8-channel groups one voxel strip apart (LBO)):
-//   strip mode (nx % 128 == 0): a stage is one (dy, dz) strip of 130 voxels
-//     (x0 - 1 .. x0 + 128) with all channels; the three dx taps are the same
-//     image read from rows 0, 1, 2 (start address + 16 B per row), so a tile
-//     takes 9 stages and each input voxel is staged 9 times, not 27;
-//   tap mode (nx a divisor of 128): a stage is one tap's box of 128 voxels
-//     (by = 128 / nx rows of the grid), 27 stages per tile.
-// The tensor map's zero fill at the grid faces is the convolution's zero
-// padding. The weights of a stage's taps (pre-packed into the B operand
-// image) arrive by one bulk copy on the same barrier.
+// Operands sit in shared memory in the no-swizzle K-major layout: 8-row x
+// 16-byte core matrices, 8-row groups 128 B apart (SBO), the two 8-channel
+// groups of a chunk one voxel image apart (LBO). TMA writes that image
+// directly: the input is viewed as a 5-D tensor (8 channels, x, y, z,
+// channel group) and a box's channel groups are its slowest dimension.
 //
-// Per CTA (persistent over tiles, 6 warps):
+// Plane mode (nx % 128 == 0, ny even): a work unit is two tiles on adjacent
+// y rows (x0..x0+127 at y0 and y0 + 1). A pipeline stage is one (dz, chunk):
+// one TMA box of 4 y rows (y0 - 1 .. y0 + 2) x 130 voxels (x0 - 1 ..
+// x0 + 128) x 16 channels, and one bulk copy of the 9 (dy, dx) taps' weight
+// slices. Every (tile, dy, dx) is the same image read from row
+// (tile + dy + 1, dx + 1) through the descriptor's start address, so a stage
+// feeds 18 MMAs and each input row is staged 3 times per two tiles.
+// Tap mode (nx a divisor of 128): a work unit is one tile of 128 / nx rows,
+// a stage one (tap, chunk) box, one MMA per stage.
+// The tensor map's zero fill at the grid faces is the convolution's padding.
+//
+// Per CTA (persistent over work units, 6 warps):
 //   warp 0     one thread issues the TMA and bulk copies;
-//   warp 1     owns the TMEM accumulators (two buffers of N FP32 columns at
-//              column offsets 0 and kCols / 2); one thread issues the MMAs and
-//              commits each stage back to the producer and each finished tile
-//              to the epilogue;
+//   warp 1     owns the TMEM accumulators (two buffers, each holding the
+//              unit's tiles side by side); one thread issues the MMAs and
+//              commits each stage back to the producer and each finished
+//              unit to the epilogue;
 //   warps 2-5  epilogue: tcgen05.ld of their 32-lane quarter, optional bias /
 //              ReLU / accumulation, BF16 or FP32 stores (channels-last rows).
 //
@@ -43,7 +46,7 @@ namespace {
 constexpr int      kTcM = 128;           // voxels per tile (MMA M)
 constexpr int      kTcMaxStages = 8;     // shared-memory pipeline depth (at most)
 constexpr int      kTcThreads = 192;     // 6 warps
-constexpr int      kStripRows = kTcM + 2;  // voxels x0 - 1 .. x0 + 128
+constexpr int      kStripRows = kTcM + 2;  // plane mode: voxels x0 - 1 .. x0 + 128 of an image row
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;
@@ -94,12 +97,12 @@ __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity)
     atomicExch(&g_tc_error, 1);
 }
 
-__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c1, int c2, int c3, uint64_t* bar)
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c1, int c2, int c3, int c4, uint64_t* bar)
 {
     asm volatile(
         "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
         "[%7];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3), "r"(0), "r"(smem_u32(bar))
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
         : "memory");
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
@@ -161,21 +164,47 @@ struct TmemCols {
 
 struct TcParams {
     int                  nx, ny, nz, kc;  // kc = Cin / 16
-    int                  strip;           // 1: strip mode, 0: tap mode
+    int                  plane;           // 1: plane mode, 0: tap mode
+    int                  ntile;           // tiles per work unit (2 / 1)
     int                  nstages;         // pipeline depth
+    uint32_t             tmem_cols;       // allocated TMEM columns (two buffers of ntile * N)
     uint32_t             a_bytes, b_bytes, stage_bytes;  // per stage (stage_bytes: 128-aligned stride)
-    uint32_t             a_lbo;           // bytes between 8-channel groups in the A image (rows * 16)
-    int64_t              tiles;
-    const __nv_bfloat16* wpk;  // packed weights: per tap Cin / 8 groups of N x 8 BF16
+    uint32_t             a_lbo;           // bytes between the two 8-channel groups of the A image
+    int                  a_row;           // plane mode: voxels per image row (130)
+    int64_t              units;
+    const __nv_bfloat16* wpk;  // packed weights (ngb_conv3d_pack)
     const float*         bias;
     void*                y;
     int                  ldy, relu, accumulate;
 };
 
+// First voxel and grid coordinates of work unit u.
+struct Unit {
+    int64_t v0;
+    int     x0, y0, z0;
+};
+__device__ __forceinline__ Unit unit_of(const TcParams& p, int64_t u)
+{
+    Unit t;
+    if (p.plane) {
+        const int64_t xt = p.nx / kTcM, yt = p.ny / 2;
+        t.x0 = int(u % xt) * kTcM;
+        const int64_t r = u / xt;
+        t.y0 = int(r % yt) * 2;
+        t.z0 = int(r / yt);
+        t.v0 = t.x0 + int64_t(p.nx) * (t.y0 + int64_t(p.ny) * t.z0);
+    } else {
+        t.v0 = u * kTcM;
+        t.x0 = int(t.v0 % p.nx);
+        const int64_t r = t.v0 / p.nx;
+        t.y0 = int(r % p.ny), t.z0 = int(r / p.ny);
+    }
+    return t;
+}
+
 template <int N, bool F32OUT>
 __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_constant__ CUtensorMap xmap, TcParams p)
 {
-    constexpr uint32_t kCols = TmemCols<N>::value;
     constexpr uint32_t kIdesc = idesc_bf16_f32(kTcM, N);
 
     extern __shared__ uint8_t smem_raw[];
@@ -201,7 +230,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)), "r"(kCols)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(p.tmem_cols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -209,30 +239,35 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
-    const int      nst = p.strip ? 9 : 27;  // stages per tile
-    const int      ntap = p.strip ? 3 : 1;  // taps per stage
-    const uint32_t tap_b = uint32_t(N) * uint32_t(p.kc) * 32u;  // B bytes of one tap
+    const uint32_t half_cols = p.tmem_cols / 2;           // accumulator buffer 1 starts here
+    const int      nst = (p.plane ? 3 : 27) * p.kc;       // stages per unit
+    const uint32_t slice = uint32_t(N) * 32u;             // B bytes of one (tap, chunk)
+    const uint32_t b_off = p.stage_bytes - ((p.b_bytes + 127u) & ~127u);
 
     if (warp == 0 && lane == 0) {
         // ------------------------------------------------ TMA producer
         uint32_t k = 0;
         bool     ok = true;
-        for (int64_t tile = blockIdx.x; tile < p.tiles && ok; tile += gridDim.x) {
-            const int64_t v0 = tile * kTcM;
-            const int     x0 = int(v0 % p.nx);
-            const int64_t row = v0 / p.nx;
-            const int     y0 = int(row % p.ny), z0 = int(row / p.ny);
+        for (int64_t u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
+            const Unit t = unit_of(p, u);
             for (int i = 0; i < nst; i++, k++) {
-                // strip g = 3 (dz + 1) + (dy + 1); tap t = 9 (dz + 1) + 3 (dy + 1) + (dx + 1)
-                const int dx = p.strip ? -1 : i % 3 - 1;
-                const int dy = (p.strip ? i : i / 3) % 3 - 1, dz = (p.strip ? i / 3 : i / 9) - 1;
+                // plane: i = dz_index * kc + chunk; tap: i = tap * kc + chunk, tap = 9 dz + 3 dy + dx (indices 0..2)
+                const int      chunk = i % p.kc, outer = i / p.kc;
                 const uint32_t s = k % ns;
                 if (!(ok = mbar_wait(&empty_bar[s], ((k / ns) & 1u) ^ 1u, &abort_sh))) break;
                 uint8_t* st = stages + size_t(s) * p.stage_bytes;
                 mbar_expect_tx(&full_bar[s], p.a_bytes + p.b_bytes);
-                tma_load_5d(st, &xmap, x0 + dx, y0 + dy, z0 + dz, &full_bar[s]);
-                bulk_load(st + p.stage_bytes - ((p.b_bytes + 127u) & ~127u), reinterpret_cast<const uint8_t*>(p.wpk) + size_t(i) * ntap * tap_b,
-                          p.b_bytes, &full_bar[s]);
+                size_t boff;
+                if (p.plane) {
+                    const int dzi = outer;
+                    tma_load_5d(st, &xmap, t.x0 - 1, t.y0 - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
+                    boff = (size_t(dzi) * p.kc + chunk) * 9 * slice;
+                } else {
+                    const int dzi = outer / 9, dyi = (outer / 3) % 3, dxi = outer % 3;
+                    tma_load_5d(st, &xmap, t.x0 + dxi - 1, t.y0 + dyi - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
+                    boff = ((size_t(dzi) * p.kc + chunk) * 9 + dyi * 3 + dxi) * slice;
+                }
+                bulk_load(st + b_off, reinterpret_cast<const uint8_t*>(p.wpk) + boff, p.b_bytes, &full_bar[s]);
             }
         }
         // copies still in flight land before the CTA leaves: the latest phase of
@@ -243,26 +278,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         // ------------------------------------------------ MMA issuer
         uint32_t k = 0, j = 0;
         bool     ok = true;
-        for (int64_t tile = blockIdx.x; tile < p.tiles && ok; tile += gridDim.x, j++) {
-            const uint32_t a = j & 1u, u = (j >> 1) & 1u;
-            if (!(ok = mbar_wait(&tempty_bar[a], u ^ 1u, &abort_sh))) break;
+        for (int64_t u = blockIdx.x; u < p.units && ok; u += gridDim.x, j++) {
+            const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
+            if (!(ok = mbar_wait(&tempty_bar[a], ph ^ 1u, &abort_sh))) break;
             tc_fence_after();
-            const uint32_t d = tmem + a * (kCols / 2);  // buffers at power-of-two column offsets
-            uint32_t       acc = 0;
+            const uint32_t d0 = tmem + a * half_cols;
             for (int i = 0; i < nst; i++, k++) {
                 const uint32_t s = k % ns;
                 if (!(ok = mbar_wait(&full_bar[s], (k / ns) & 1u, &abort_sh))) break;
                 tc_fence_after();
                 const uint32_t sa = smem_u32(stages + size_t(s) * p.stage_bytes);
-                const uint32_t sb = sa + p.stage_bytes - ((p.b_bytes + 127u) & ~127u);
-                for (int t = 0; t < ntap; t++) {
-                    for (int kc = 0; kc < p.kc; kc++) {
-                        // A: rows from t (the dx shift of strip mode), channel groups 2kc, 2kc + 1
-                        const uint64_t ad = smem_desc(sa + uint32_t(t) * 16u + uint32_t(kc) * 2u * p.a_lbo, p.a_lbo, 128);
-                        const uint64_t bd = smem_desc(sb + uint32_t(t) * tap_b + uint32_t(kc) * 2u * N * 16u, N * 16, 128);
-                        mma_bf16(d, ad, bd, kIdesc, acc);
-                        acc = 1;
-                    }
+                const uint32_t sb = sa + b_off;
+                if (p.plane) {
+                    // the first stage of a unit overwrites each tile's accumulator with its first MMA
+                    for (int tt = 0; tt < 2; tt++)
+                        for (int tap = 0; tap < 9; tap++) {
+                            const int      dyi = tap / 3, dxi = tap % 3;
+                            const uint32_t arow = uint32_t((tt + dyi) * p.a_row + dxi);
+                            const uint64_t ad = smem_desc(sa + arow * 16u, p.a_lbo, 128);
+                            const uint64_t bd = smem_desc(sb + uint32_t(tap) * slice, N * 16, 128);
+                            mma_bf16(d0 + uint32_t(tt) * N, ad, bd, kIdesc, (i > 0 || tap > 0) ? 1u : 0u);
+                        }
+                } else {
+                    mma_bf16(d0, smem_desc(sa, p.a_lbo, 128), smem_desc(sb, N * 16, 128), kIdesc, i > 0 ? 1u : 0u);
                 }
                 mma_commit(&empty_bar[s]);
             }
@@ -275,45 +313,50 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         // ------------------------------------------------ epilogue
         const uint32_t q = uint32_t(warp & 3);  // the TMEM lane quarter this warp may read
         uint32_t       j = 0;
-        for (int64_t tile = blockIdx.x; tile < p.tiles; tile += gridDim.x, j++) {
-            const uint32_t a = j & 1u, u = (j >> 1) & 1u;
-            if (!mbar_wait(&tfull_bar[a], u, &abort_sh)) break;
+        for (int64_t u = blockIdx.x; u < p.units; u += gridDim.x, j++) {
+            const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
+            if (!mbar_wait(&tfull_bar[a], ph, &abort_sh)) break;
             tc_fence_after();
-            float acc[N];
+            const Unit t = unit_of(p, u);
+            for (int tt = 0; tt < p.ntile; tt++) {
+                float acc[N];
 #pragma unroll
-            for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((q * 32u) << 16) + a * (kCols / 2) + c, acc + c);
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&tempty_bar[a]);
-            const int64_t v = tile * kTcM + q * 32 + lane;
-            if (p.bias) {
-#pragma unroll
-                for (int c = 0; c < N; c++) acc[c] += __ldg(p.bias + c);
-            }
-            if constexpr (F32OUT) {
-                float* yo = static_cast<float*>(p.y) + v * p.ldy;
-#pragma unroll
-                for (int c = 0; c < N; c += 4) {
-                    float4 o = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
-                    if (p.accumulate) {
-                        const float4 old = *reinterpret_cast<const float4*>(yo + c);
-                        o.x += old.x, o.y += old.y, o.z += old.z, o.w += old.w;
-                    }
-                    *reinterpret_cast<float4*>(yo + c) = o;
+                for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((q * 32u) << 16) + a * half_cols + uint32_t(tt) * N + c, acc + c);
+                if (tt == p.ntile - 1) {
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty_bar[a]);
                 }
-            } else {
-                __nv_bfloat16* yo = static_cast<__nv_bfloat16*>(p.y) + v * p.ldy;
+                const int64_t v = t.v0 + int64_t(tt) * p.nx + q * 32 + lane;
+                if (p.bias) {
 #pragma unroll
-                for (int c = 0; c < N; c += 8) {
-                    uint32_t w4[4];
+                    for (int c = 0; c < N; c++) acc[c] += __ldg(p.bias + c);
+                }
+                if constexpr (F32OUT) {
+                    float* yo = static_cast<float*>(p.y) + v * p.ldy;
 #pragma unroll
-                    for (int e = 0; e < 4; e++) {
-                        float lo = acc[c + 2 * e], hi = acc[c + 2 * e + 1];
-                        if (p.relu) lo = fmaxf(lo, 0.f), hi = fmaxf(hi, 0.f);
-                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(lo, hi);
-                        w4[e] = *reinterpret_cast<const uint32_t*>(&h2);
+                    for (int c = 0; c < N; c += 4) {
+                        float4 o = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
+                        if (p.accumulate) {
+                            const float4 old = *reinterpret_cast<const float4*>(yo + c);
+                            o.x += old.x, o.y += old.y, o.z += old.z, o.w += old.w;
+                        }
+                        *reinterpret_cast<float4*>(yo + c) = o;
                     }
-                    *reinterpret_cast<uint4*>(yo + c) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                } else {
+                    __nv_bfloat16* yo = static_cast<__nv_bfloat16*>(p.y) + v * p.ldy;
+#pragma unroll
+                    for (int c = 0; c < N; c += 8) {
+                        uint32_t w4[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            float lo = acc[c + 2 * e], hi = acc[c + 2 * e + 1];
+                            if (p.relu) lo = fmaxf(lo, 0.f), hi = fmaxf(hi, 0.f);
+                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(lo, hi);
+                            w4[e] = *reinterpret_cast<const uint32_t*>(&h2);
+                        }
+                        *reinterpret_cast<uint4*>(yo + c) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                    }
                 }
             }
         }
@@ -323,23 +366,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     if (warp == 1) {
         __syncwarp();
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols) : "memory");
     }
 }
 
-// packed[((t * kc + c16) * 2 + h) * N * 8 + n * 8 + e] = w[n][t][c16 * 16 + h * 8 + e]
+// Operand image of weights w[cout][27][cin] (BF16), ordered so that a plane
+// stage's 9 taps and a tap stage's slice are contiguous:
+// packed[(((((dz * kc + c16) * 3 + dy) * 3 + dx) * 2 + h) * cout + n) * 8 + e] = w[n][9 dz + 3 dy + dx][16 c16 + 8 h + e]
+// (dz, dy, dx the tap indices 0..2).
 __global__ void conv3d_pack_kernel(int cout, int cin, const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __restrict__ out)
 {
     const int64_t total = int64_t(cout) * 27 * cin;
+    const int     kc = cin / 16;
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
-        const int e = int(i % 8);
-        const int n = int((i / 8) % cout);
-        const int64_t rest = i / (8 * int64_t(cout));  // (t * kc + c16) * 2 + h
-        const int h = int(rest % 2);
-        const int64_t tc = rest / 2;
-        const int kc = cin / 16;
-        const int t = int(tc / kc), c16 = int(tc % kc);
-        out[i] = w[(int64_t(n) * 27 + t) * cin + c16 * 16 + h * 8 + e];
+        const int     e = int(i % 8);
+        const int     n = int((i / 8) % cout);
+        int64_t       r = i / (8 * int64_t(cout));
+        const int     h = int(r % 2);
+        r /= 2;
+        const int dx = int(r % 3);
+        r /= 3;
+        const int dy = int(r % 3);
+        r /= 3;
+        const int c16 = int(r % kc), dz = int(r / kc);
+        out[i] = w[(int64_t(n) * 27 + 9 * dz + 3 * dy + dx) * cin + c16 * 16 + h * 8 + e];
     }
 }
 
@@ -368,8 +418,9 @@ int launch_tc(const CUtensorMap& map, const TcParams& p, cudaStream_t s)
     NGB_CUDA_TRY(cudaGetDevice(&dev));
     NGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     NGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3d_tc_kernel<N, F32OUT>, kTcThreads, smem));
-    // persistent CTAs: all resident at once (two per SM hold at most 2 x 256 TMEM columns)
-    const int64_t grid = std::min<int64_t>(p.tiles, int64_t(sms) * std::max(1, std::min(per_sm, 2)));
+    // persistent CTAs, all resident at once: at most 512 / tmem_cols per SM (TMEM), 2 at most
+    const int     by_tmem = int(512u / p.tmem_cols);
+    const int64_t grid = std::min<int64_t>(p.units, int64_t(sms) * std::max(1, std::min(std::min(per_sm, by_tmem), 2)));
     conv3d_tc_kernel<N, F32OUT><<<int(grid), kTcThreads, smem, s>>>(map, p);
     NGB_LAUNCH_CHECK("conv3d_tc_kernel");
     return NGB_OK;
@@ -420,14 +471,15 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
         set_error("cuTensorMapEncodeTiled is not available from the driver");
         return NGB_ERR_CUDA;
     }
-    // 5-D view (8 channels, x, y, z, channel group): one box per stage holds
-    // every channel, laid out group-major (the K-major core-matrix image)
-    const bool strip = nx % kTcM == 0;
-    const int  bx = strip ? kStripRows : nx, by = strip ? 1 : kTcM / nx, rows = bx * by;
+    // 5-D view (8 channels, x, y, z, channel group); a box holds one
+    // 16-channel chunk (two groups), laid out group-major
+    const bool plane = nx % kTcM == 0 && ny % 2 == 0;
+    const int  bx = plane ? kStripRows : (nx >= kTcM ? kTcM : nx);
+    const int  by = plane ? 4 : kTcM / bx;
     CUtensorMap map;
     cuuint64_t  dims[5] = {8, cuuint64_t(nx), cuuint64_t(ny), cuuint64_t(nz), cuuint64_t(cin / 8)};
     cuuint64_t  strides[4] = {cuuint64_t(ldx) * 2, cuuint64_t(ldx) * 2 * nx, cuuint64_t(ldx) * 2 * nx * ny, 16};
-    cuuint32_t  box[5] = {8, cuuint32_t(bx), cuuint32_t(by), 1, cuuint32_t(cin / 8)};
+    cuuint32_t  box[5] = {8, cuuint32_t(bx), cuuint32_t(by), 1, 2};
     cuuint32_t  estr[5] = {1, 1, 1, 1, 1};
     const CUresult cr = encode(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(x), dims, strides, box, estr,
                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -438,17 +490,23 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
     }
     TcParams p{};
     p.nx = nx, p.ny = ny, p.nz = nz, p.kc = cin / 16;
-    p.strip = strip ? 1 : 0;
-    p.a_lbo = uint32_t(rows) * 16u;
-    p.a_bytes = p.a_lbo * uint32_t(cin / 8);
-    p.b_bytes = uint32_t(strip ? 3 : 1) * uint32_t(cout) * uint32_t(cin) * 2u;
+    p.plane = plane ? 1 : 0;
+    p.ntile = plane ? 2 : 1;
+    p.a_row = bx;
+    p.a_lbo = uint32_t(bx * by) * 16u;
+    p.a_bytes = p.a_lbo * 2u;
+    p.b_bytes = uint32_t(plane ? 9 : 1) * uint32_t(cout) * 32u;
     p.stage_bytes = ((p.a_bytes + 127u) & ~127u) + ((p.b_bytes + 127u) & ~127u);
-    // depth: as many stages as fit in ~108 KB (two CTAs per SM), 2 to 8
-    p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, (108u * 1024u) / p.stage_bytes)));
-    p.tiles = int64_t(nx) * ny * nz / kTcM;
+    uint32_t cols = 32;
+    while (cols < uint32_t(2 * p.ntile * cout)) cols *= 2;
+    p.tmem_cols = cols;
+    // depth: as many stages as fit in ~108 KB (two CTAs per SM) or ~200 KB (one), 2 to 8
+    const uint32_t budget = cols <= 256 ? 108u * 1024u : 200u * 1024u;
+    p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, budget / p.stage_bytes)));
+    p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * nz : int64_t(nx) * ny * nz / kTcM;
     p.wpk = static_cast<const __nv_bfloat16*>(wpacked);
     p.bias = bias, p.y = y, p.ldy = ldy, p.relu = relu, p.accumulate = accumulate;
-    if (p.tiles == 0) return NGB_OK;
+    if (p.units == 0) return NGB_OK;
     cudaStream_t s = as_stream(stream);
 #define NGB_TC(NN)                                                   \
     case NN:                                                         \

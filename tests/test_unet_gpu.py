@@ -205,3 +205,60 @@ def test_unet_tensor_cores_match_oracle_and_mma_path(ngb, cuda):
     net.tensor_cores = False
     z2 = net.forward(torch.from_numpy(r).to(cuda)).clone()
     assert float((z - z2).norm() / z2.norm()) <= 2e-3
+
+
+@pytest.mark.parametrize("dims", [(8, 64, 128), (4, 32, 256), (16, 64, 64), (7, 33, 128)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (32, 96), (64, 64)])
+def test_conv_tensor_cores_many_tiles_match_mma(ngb, cuda, dims, cin, cout):
+    """Grids with many more tiles than resident CTAs, so each persistent CTA
+    cycles through both TMEM accumulator buffers and many barrier phases:
+    the tcgen05 convolution against the mma.sync kernel on the same inputs
+    (plane mode, tap mode, and an odd ny that falls back to one-tile units)."""
+    import torch
+    nz, ny, nx = dims
+    L = ngb.lib()
+    assert L.ngb_conv3d_tc_supported(nx, ny, nz, cin, cin, cout, cout) == 1
+    g = torch.Generator(device="cpu").manual_seed(cin + cout + nx + ny)
+    X = torch.randn(nx * ny * nz, cin, generator=g).to(torch.bfloat16).to(cuda)
+    W = (torch.randn(cout, 27, cin, generator=g) / (27 * cin) ** 0.5).to(torch.bfloat16).to(cuda)
+    Wp = torch.empty_like(W)
+    ngb.check(L.ngb_conv3d_pack(cout, cin, ngb._ptr(W), ngb._ptr(Wp), None))
+    ref = torch.zeros(X.shape[0], cout, dtype=torch.float32, device=cuda)
+    for lo in range(0, cout, 64):
+        hi = min(cout, lo + 64)
+        ptr = ctypes.c_void_p(ref.data_ptr() + lo * 4)
+        ngb.check(L.ngb_conv3d(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(W[lo:hi]), None, ptr, cout, hi - lo, 1, 0, 0, None))
+    Y = torch.full_like(ref, float("nan"))
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), None, ngb._ptr(Y), cout, cout, 1, 0, 0, None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    scale = float(ref.abs().max())
+    err = float((Y - ref).abs().max())
+    assert err <= 1e-5 * scale, (err / scale, int(torch.isnan(Y).sum()))
+
+
+def test_unet_tensor_cores_match_mma_path_at_128(ngb, cuda):
+    """At 128^3 level 0 runs in plane mode with many tiles per CTA: the U-Net
+    forward pass and the layer gradients on the tensor cores against the
+    mma.sync network."""
+    import torch
+    from neon_gb300.learned import UNet
+    n = 128
+    net = UNet(seed=5, device=cuda)
+    net.w["c0d"] = net.w["c0d"] * 0 + torch.randn(net.w["c0d"].shape, generator=torch.Generator().manual_seed(3)).to(cuda) * 0.05
+    net.load_state_dict({k: v.cpu() for k, v in net.w.items()})
+    g = torch.Generator(device="cpu").manual_seed(21)
+    r = torch.randn(n ** 3, generator=g).to(cuda)
+    e = torch.randn(n ** 3, generator=g).to(cuda)
+    out = {}
+    for tc in (True, False):
+        net.tensor_cores = tc
+        z = net.forward(r).clone()
+        net.zero_grad()
+        net.backward(z - e)
+        out[tc] = (z, {k: v.clone() for k, v in net.g.items()})
+    (z1, g1), (z0, g0) = out[True], out[False]
+    assert torch.isfinite(z1).all()
+    assert float((z1 - z0).norm() / z0.norm()) <= 2e-3
+    for name in g0:
+        rel = float((g1[name] - g0[name]).norm() / max(float(g0[name].norm()), 1e-30))
+        assert rel <= 2e-2, (name, rel)
