@@ -73,39 +73,6 @@ __device__ __forceinline__ uint32_t bgrid_lidbits(const uint32_t* __restrict__ f
     return lid;
 }
 
-// Thread -> voxel of the block. Threads 0..215 take the 6^3 inner voxels
-// (i, j, k in 1..6), whose 19 or 27 pull sources all lie in the block itself;
-// threads 216..511 take the 296 voxels on the block's faces, in k-major order:
-// the k = 0 face (64), the rings of k = 1..6 (28 each: row j = 0, row j = 7,
-// then i = 0 / 7 of rows 1..6), the k = 7 face (64). Warps of inner voxels
-// then never run the neighbour-block arithmetic.
-constexpr int kInnerVoxels = 216;
-__device__ __forceinline__ void bgrid_thread_voxel(int t, int& i, int& j, int& k)
-{
-    if (t < kInnerVoxels) {
-        i = 1 + t % 6, j = 1 + (t / 6) % 6, k = 1 + t / 36;
-        return;
-    }
-    const int r = t - kInnerVoxels;
-    if (r < 64) {
-        i = r & 7, j = r >> 3, k = 0;
-    } else if (r < 64 + 6 * 28) {
-        const int u = r - 64, ring = u % 28;
-        k = 1 + u / 28;
-        if (ring < 8) {
-            i = ring, j = 0;
-        } else if (ring < 16) {
-            i = ring - 8, j = 7;
-        } else {
-            const int w = ring - 16;
-            j = 1 + (w >> 1), i = (w & 1) ? 7 : 0;
-        }
-    } else {
-        const int w = r - 64 - 6 * 28;
-        i = w & 7, j = w >> 3, k = 7;
-    }
-}
-
 // Source pointer of direction q for this voxel: the pulled neighbour
 // population, or the voxel's own opposite population when q is masked (the
 // half-way bounce-back rule). A source outside every block is taken as a wall,
@@ -126,27 +93,15 @@ __device__ __forceinline__ const S* bgrid_src(const S* __restrict__ fin, const u
 }
 
 template <int Q, typename S, bool F64>
-__global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 27 ? (sizeof(S) == 2 ? 2 : 3) : (sizeof(S) == 2 ? 3 : 4)))
-    bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+__global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
                                                                  const uint32_t* __restrict__ flags,
                                                                  BParams<typename std::conditional<F64, double, float>::type> p)
 {
     using L = Lattice<Q>;
     const uint32_t      b = blockIdx.x;
-    // 16-bit storage is issue-bound: inner voxels first (see bgrid_thread_voxel);
-    // FP32 is bandwidth-bound and keeps the natural order (whole 32-byte rows per access)
-    constexpr bool      kPermute = sizeof(S) == 2;
-    const int           t = threadIdx.x;
-    const bool          inner = kPermute && t < kInnerVoxels;
-    int                 i, j, k, v;
-    if constexpr (kPermute) {
-        bgrid_thread_voxel(t, i, j, k);
-        v = i + 8 * j + 64 * k;
-    } else {
-        v = t, i = t & 7, j = (t >> 3) & 7, k = t >> 6;
-    }
+    const int           v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
     __shared__ uint32_t sconn[27];  // this block's neighbour blocks
-    if (t < 27) sconn[t] = __ldg(p.conn + size_t(b) * 27 + t);
+    if (v < 27) sconn[v] = __ldg(p.conn + size_t(b) * 27 + v);
     const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
     __syncthreads();
     const int    cls = flag_class(f);
@@ -164,23 +119,15 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 27 ? (sizeof(S) 
     const uint32_t m = flag_mask(f);
     const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m) : 0u;
 
-    // own voxel of plane 0: inner voxels without walls read every source at a
-    // fixed offset from it (no neighbour-block arithmetic)
-    const S* own = fin + bq * kBlockVoxels + v;
     if constexpr (F64) {
         S pop[Q];
-        if (inner && m == 0) {
 #pragma unroll
-            for (int q = 0; q < Q; q++) pop[q] = __ldg(own + q * kBlockVoxels - (L::cx(q) + 8 * L::cy(q) + 64 * L::cz(q)));
-        } else {
-#pragma unroll
-            for (int q = 0; q < Q; q++) {
-                bool      masked;
-                const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
-                const int o = L::opp(q);
-                pop[q] = __ldg(src);
-                if (masked) pop[q] = pop[q] + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
-            }
+        for (int q = 0; q < Q; q++) {
+            bool      masked;
+            const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
+            const int o = L::opp(q);
+            pop[q] = __ldg(src);
+            if (masked) pop[q] = pop[q] + S((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
         }
         S out[Q];
         bgk_f64_ref<Q, S>(pop, p.omega, out);
@@ -188,20 +135,14 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 27 ? (sizeof(S) 
         for (int q = 0; q < Q; q++) fout[(bq + q) * kBlockVoxels + v] = out[q];
     } else {
         float g[Q];
-        if (inner && m == 0) {
 #pragma unroll
-            for (int q = 0; q < Q; q++)
-                g[q] = PairIO<S>::to_g1(__ldg(own + q * kBlockVoxels - (L::cx(q) + 8 * L::cy(q) + 64 * L::cz(q))), float(L::w(q)));
-        } else {
-#pragma unroll
-            for (int q = 0; q < Q; q++) {
-                bool      masked;
-                const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
-                const int o = L::opp(q);
-                // w(opp q) == w(q), so one conversion serves both cases
-                g[q] = PairIO<S>::to_g1(__ldg(src), float(L::w(q)));
-                if (masked) g[q] = g[q] + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
-            }
+        for (int q = 0; q < Q; q++) {
+            bool      masked;
+            const S*  src = bgrid_src<Q, S>(fin, sconn, bq, v, i, j, k, q, m, masked);
+            const int o = L::opp(q);
+            // w(opp q) == w(q), so one conversion serves both cases
+            g[q] = PairIO<S>::to_g1(__ldg(src), float(L::w(q)));
+            if (masked) g[q] = g[q] + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
         }
         bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
 #pragma unroll
