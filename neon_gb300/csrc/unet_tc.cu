@@ -172,6 +172,9 @@ struct TcParams {
     uint32_t             a_lbo;           // bytes between the two 8-channel groups of the A image
     int                  a_row;           // plane mode: voxels per image row (130)
     int64_t              units;
+    int                  resident;        // 1: all weights stay in shared memory (stages carry A only)
+    uint32_t             w_bytes;         // bytes of the packed weights (27 * N * Cin * 2)
+    uint32_t             w_region;        // shared bytes reserved for resident weights (1024-aligned)
     const __nv_bfloat16* wpk;  // packed weights (ngb_conv3d_pack)
     const float*         bias;
     void*                y;
@@ -208,9 +211,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     constexpr uint32_t kIdesc = idesc_bf16_f32(kTcM, N);
 
     extern __shared__ uint8_t smem_raw[];
-    uint8_t* stages = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* wres = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* stages = wres + p.w_region;
 
-    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[2], tempty_bar[2], drain_bar;
+    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[2], tempty_bar[2], drain_bar, w_bar;
     __shared__ uint32_t     tmem_base_sh;
     __shared__ volatile int abort_sh;
 
@@ -226,6 +230,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
             mbar_init(&tempty_bar[a], 4);
         }
         mbar_init(&drain_bar, 1);
+        mbar_init(&w_bar, 1);
         abort_sh = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -246,6 +251,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
 
     if (warp == 0 && lane == 0) {
         // ------------------------------------------------ TMA producer
+        if (p.resident) {  // the whole packed weight image, once
+            mbar_expect_tx(&w_bar, p.w_bytes);
+            bulk_load(wres, p.wpk, p.w_bytes, &w_bar);
+        }
         uint32_t k = 0;
         bool     ok = true;
         for (int64_t u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
@@ -267,17 +276,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
                     tma_load_5d(st, &xmap, t.x0 + dxi - 1, t.y0 + dyi - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
                     boff = ((size_t(dzi) * p.kc + chunk) * 9 + dyi * 3 + dxi) * slice;
                 }
-                bulk_load(st + b_off, reinterpret_cast<const uint8_t*>(p.wpk) + boff, p.b_bytes, &full_bar[s]);
+                if (!p.resident) bulk_load(st + b_off, reinterpret_cast<const uint8_t*>(p.wpk) + boff, p.b_bytes, &full_bar[s]);
             }
         }
         // copies still in flight land before the CTA leaves: the latest phase of
         // each stage used is complete once its bytes have arrived
         const uint32_t used = k < ns ? k : ns;
         for (uint32_t j = k - used; j < k; j++) mbar_drain(&full_bar[j % ns], (j / ns) & 1u);
+        if (p.resident) mbar_drain(&w_bar, 0);
     } else if (warp == 1 && lane == 0) {
         // ------------------------------------------------ MMA issuer
         uint32_t k = 0, j = 0;
-        bool     ok = true;
+        bool     ok = !p.resident || mbar_wait(&w_bar, 0, &abort_sh);
         for (int64_t u = blockIdx.x; u < p.units && ok; u += gridDim.x, j++) {
             const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
             if (!(ok = mbar_wait(&tempty_bar[a], ph ^ 1u, &abort_sh))) break;
@@ -288,7 +298,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
                 if (!(ok = mbar_wait(&full_bar[s], (k / ns) & 1u, &abort_sh))) break;
                 tc_fence_after();
                 const uint32_t sa = smem_u32(stages + size_t(s) * p.stage_bytes);
-                const uint32_t sb = sa + b_off;
+                uint32_t       sb = sa + b_off;
+                if (p.resident) {  // this stage's weight slices inside the resident image
+                    const int chunk = i % p.kc, outer = i / p.kc;
+                    const uint32_t slot = p.plane ? uint32_t((outer * p.kc + chunk) * 9)
+                                                  : uint32_t(((outer / 9) * p.kc + chunk) * 9 + outer % 9);
+                    sb = smem_u32(wres) + slot * slice;
+                }
                 if (p.plane) {
                     // the first stage of a unit overwrites each tile's accumulator with its first MMA
                     for (int tt = 0; tt < 2; tt++)
@@ -412,15 +428,25 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 template <int N, bool F32OUT>
 int launch_tc(const CUtensorMap& map, const TcParams& p, cudaStream_t s)
 {
-    const size_t smem = size_t(p.nstages) * p.stage_bytes + 1024;  // + alignment slack
+    const size_t smem = p.w_region + size_t(p.nstages) * p.stage_bytes + 1024;  // + alignment slack
     NGB_CUDA_TRY(cudaFuncSetAttribute(conv3d_tc_kernel<N, F32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    int dev = 0, sms = 0, per_sm = 0;
+    // the whole unified L1 / shared array as shared memory: two CTAs per SM where they fit
+    NGB_CUDA_TRY(cudaFuncSetAttribute(conv3d_tc_kernel<N, F32OUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      int(cudaSharedmemCarveoutMaxShared)));
+    int dev = 0, sms = 0, smem_sm = 0, smem_reserved = 0;
     NGB_CUDA_TRY(cudaGetDevice(&dev));
     NGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    NGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv3d_tc_kernel<N, F32OUT>, kTcThreads, smem));
-    // persistent CTAs, all resident at once: at most 512 / tmem_cols per SM (TMEM), 2 at most
-    const int     by_tmem = int(512u / p.tmem_cols);
-    const int64_t grid = std::min<int64_t>(p.units, int64_t(sms) * std::max(1, std::min(std::min(per_sm, by_tmem), 2)));
+    NGB_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    NGB_CUDA_TRY(cudaDeviceGetAttribute(&smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+    cudaFuncAttributes fa{};
+    NGB_CUDA_TRY(cudaFuncGetAttributes(&fa, conv3d_tc_kernel<N, F32OUT>));
+    // persistent CTAs, all resident at once: as many per SM as shared memory,
+    // registers and TMEM (512 columns) allow, 2 at most
+    const int by_smem = smem_sm / int(smem + fa.sharedSizeBytes + size_t(smem_reserved));
+    const int by_regs = 65536 / std::max(1, fa.numRegs * kTcThreads);
+    const int by_tmem = int(512u / p.tmem_cols);
+    const int per_sm = std::max(1, std::min(std::min(by_smem, by_regs), std::min(by_tmem, 2)));
+    const int64_t grid = std::min<int64_t>(p.units, int64_t(sms) * per_sm);
     conv3d_tc_kernel<N, F32OUT><<<int(grid), kTcThreads, smem, s>>>(map, p);
     NGB_LAUNCH_CHECK("conv3d_tc_kernel");
     return NGB_OK;
@@ -495,13 +521,16 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
     p.a_row = bx;
     p.a_lbo = uint32_t(bx * by) * 16u;
     p.a_bytes = p.a_lbo * 2u;
-    p.b_bytes = uint32_t(plane ? 9 : 1) * uint32_t(cout) * 32u;
+    p.w_bytes = uint32_t(27 * cout * cin * 2);
+    p.resident = p.w_bytes <= 56u * 1024u ? 1 : 0;  // most layers: weights loaded once per CTA
+    p.w_region = p.resident ? (p.w_bytes + 1023u) & ~1023u : 0u;
+    p.b_bytes = p.resident ? 0u : uint32_t(plane ? 9 : 1) * uint32_t(cout) * 32u;
     p.stage_bytes = ((p.a_bytes + 127u) & ~127u) + ((p.b_bytes + 127u) & ~127u);
     uint32_t cols = 32;
     while (cols < uint32_t(2 * p.ntile * cout)) cols *= 2;
     p.tmem_cols = cols;
     // depth: as many stages as fit in ~108 KB (two CTAs per SM) or ~200 KB (one), 2 to 8
-    const uint32_t budget = cols <= 256 ? 108u * 1024u : 200u * 1024u;
+    const uint32_t budget = (cols <= 256 ? 108u * 1024u : 200u * 1024u) - p.w_region;
     p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, budget / p.stage_bytes)));
     p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * nz : int64_t(nx) * ny * nz / kTcM;
     p.wpk = static_cast<const __nv_bfloat16*>(wpacked);
