@@ -41,6 +41,7 @@ struct Dom {
     const int8_t* bd;
     double        invd[7];  // h^2 / n for n valid neighbours (host-computed: no division on the device)
     float         invf[7];  // the same, rounded to float (no FP64 conversion on the device)
+    int32_t       zc;       // planes per CG work item (make_dom: enough items to fill the GPU)
 };
 
 // Dot-product accumulator of one thread. For FP32 operands the exact product
@@ -82,6 +83,12 @@ Dom make_dom(const ngb_poisson_desc* d)
     g.invd[0] = 1.0;
     for (int n = 1; n <= 6; n++) g.invd[n] = d->h * d->h / double(n);
     for (int n = 0; n <= 6; n++) g.invf[n] = float(g.invd[n]);
+    // CG work items are 32 x 16 (pass A) column tiles times zc planes: at
+    // least four per SM, with chunks as long as that allows (each costs two
+    // extra planes of loads at its start)
+    const int64_t cols = int64_t((d->nx + 31) / 32) * ((d->ny + 15) / 16);
+    g.zc = 64;
+    while (g.zc > 8 && cols * ((d->nz + g.zc - 1) / g.zc) < int64_t(sm_count()) * 4) g.zc /= 2;
     return g;
 }
 
@@ -304,18 +311,24 @@ __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const 
 }
 
 // pass A: beta from device scalars; p' = z + beta p; s = A p'; pAp = <p', s>;
-// alpha = rz / pAp. 2.5-D blocking: a CTA takes a 32 x 8 (x, y) tile and
-// marches along z through a chunk of kZC planes. Each thread computes p' of its
-// own cell once per plane (two loads); 84 threads also compute the in-plane
-// halo into shared memory; the z neighbours stay in registers. So every p'
-// value is formed from r and p once per tile instead of once per stencil use.
-constexpr int kTX = 32, kTY = 8, kZC = 64;
-constexpr int kHalo = 2 * (kTX + 2) + 2 * kTY;  // halo cells of one plane
-static_assert(kTX * kTY == kBX && kHalo <= kBX, "tile shape");
+// alpha = rz / pAp. 2.5-D blocking: a CTA takes a 32 x 16 (x, y) tile and
+// marches along z through a chunk of d.zc planes; each thread owns the cells
+// (x, y) and (x, y + 8) of the tile. Each thread computes p' of its own cells
+// once per plane (two loads each); 100 threads also compute the in-plane halo
+// into shared memory; the z neighbours stay in registers. So every p' value
+// is formed from r and p once per tile instead of once per stencil use.
+constexpr int kTX = 32, kTYA = 16, kRY = kTYA / (kBX / kTX);
+constexpr int kTY = kBX / kTX;                    // pass B tile height (one column per thread)
+constexpr int kHalo = 2 * (kTX + 2) + 2 * kTYA;  // halo cells of one plane of a pass-A tile
+static_assert(kRY == 2 && kHalo <= kBX, "tile shape");
 
 __host__ __device__ inline int pass_a_items(const Dom& d)
 {
-    return ((d.nx + kTX - 1) / kTX) * ((d.ny + kTY - 1) / kTY) * ((d.nz + kZC - 1) / kZC);
+    return ((d.nx + kTX - 1) / kTX) * ((d.ny + kTYA - 1) / kTYA) * ((d.nz + d.zc - 1) / d.zc);
+}
+__host__ __device__ inline int pass_b_items(const Dom& d)
+{
+    return ((d.nx + kTX - 1) / kTX) * ((d.ny + kTY - 1) / kTY) * ((d.nz + d.zc - 1) / d.zc);
 }
 
 template <typename T>
@@ -342,76 +355,93 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     const T      tb = T(beta);
     const T      invh2 = T(1.0) / (T(d.h) * T(d.h));
     const T      dg6 = invdiag6<T>(d, jac);
-    __shared__ T planes[2][kTY + 2][kTX + 2];  // double-buffered: one barrier per plane
-    const int    lx = threadIdx.x % kTX, ly = threadIdx.x / kTX;
+    __shared__ T planes[2][kTYA + 2][kTX + 2];  // double-buffered: one barrier per plane
+    const int    lx = threadIdx.x % kTX, ly0 = threadIdx.x / kTX;  // rows ly0 and ly0 + 8 of the tile
     // this thread's halo cell (threads < kHalo), in tile coordinates
     int        hx = 0, hy = 0;
     const bool halo = threadIdx.x < kHalo;
     if (threadIdx.x < kTX + 2) {
         hx = threadIdx.x - 1, hy = -1;
     } else if (threadIdx.x < 2 * (kTX + 2)) {
-        hx = threadIdx.x - (kTX + 2) - 1, hy = kTY;
+        hx = threadIdx.x - (kTX + 2) - 1, hy = kTYA;
     } else if (halo) {
         const int k = threadIdx.x - 2 * (kTX + 2);
         hx = (k & 1) ? kTX : -1, hy = k >> 1;
     }
-    const int     ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTY - 1) / kTY;
+    const int     ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTYA - 1) / kTYA;
     const int     items = pass_a_items(d);
     const int64_t pl = int64_t(d.nx) * d.ny;
     DotAcc<T>     acc;
+    // p' of a column at plane zz from its raw values; 0 outside the grid
+    auto pn = [&](bool ok, bool face, int64_t col, int xx, int yy, int zz, T rv, T pv) -> T {
+        if (!ok || zz < 0 || zz >= d.nz) return T(0);
+        T dgv;
+        if constexpr (BOX)
+            dgv = (face || zz == 0 || zz == d.nz - 1) ? T(1) : dg6;
+        else
+            dgv = invdiag_of<T>(d, xx, yy, zz, col + zz * pl, jac);
+        return T(dgv * rv) + tb * pv;
+    };
+    // raw (r, p) of a column at plane zz; zeros outside the grid
+    auto load = [&](bool ok, int64_t col, int zz, T& rv, T& pv) {
+        if (ok && zz >= 0 && zz < d.nz) {
+            rv = r[col + zz * pl];
+            pv = p_old[col + zz * pl];
+        } else {
+            rv = T(0), pv = T(0);
+        }
+    };
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int tx = item % ntx, rest = item / ntx, ty = rest % nty, zc = rest / nty;
-        const int x = tx * kTX + lx, y = ty * kTY + ly, z0 = zc * kZC, z1 = min(z0 + kZC, d.nz);
-        const int gx = tx * kTX + hx, gy = ty * kTY + hy;
-        const bool    own = x < d.nx && y < d.ny;
+        const int x = tx * kTX + lx, z0 = zc * d.zc, z1 = min(z0 + d.zc, d.nz);
+        const int gx = tx * kTX + hx, gy = ty * kTYA + hy;
         const bool    hown = halo && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
-        const int64_t oc = own ? x + int64_t(d.nx) * y : 0, hc = hown ? gx + int64_t(d.nx) * gy : 0;
-        const bool    oface = x == 0 || y == 0 || x == d.nx - 1 || y == d.ny - 1;
+        const int64_t hc = hown ? gx + int64_t(d.nx) * gy : 0;
         const bool    hface = gx == 0 || gy == 0 || gx == d.nx - 1 || gy == d.ny - 1;
-        // raw (r, p) of a column at plane zz; zeros outside the grid
-        auto load = [&](bool ok, int64_t col, int zz, T& rv, T& pv) {
-            if (ok && zz >= 0 && zz < d.nz) {
-                rv = r[col + zz * pl];
-                pv = p_old[col + zz * pl];
-            } else {
-                rv = T(0), pv = T(0);
-            }
-        };
-        // p' of a column at plane zz from its raw values; 0 outside the grid
-        auto pn = [&](bool ok, bool face, int64_t col, int xx, int yy, int zz, T rv, T pv) -> T {
-            if (!ok || zz < 0 || zz >= d.nz) return T(0);
-            T dgv;
-            if constexpr (BOX)
-                dgv = (face || zz == 0 || zz == d.nz - 1) ? T(1) : dg6;
-            else
-                dgv = invdiag_of<T>(d, xx, yy, zz, col + zz * pl, jac);
-            return T(dgv * rv) + tb * pv;
-        };
-        T ra, pa, rb, pb, r1, p1, hr, hp;
-        load(own, oc, z0 - 1, ra, pa);
-        load(own, oc, z0, rb, pb);
-        load(own, oc, z0 + 1, r1, p1);
+        int     y[kRY];
+        bool    own[kRY], oface[kRY];
+        int64_t oc[kRY];
+        T       pprev[kRY], pc[kRY], r1[kRY], p1[kRY];
+#pragma unroll
+        for (int c = 0; c < kRY; c++) {
+            y[c] = ty * kTYA + ly0 + 8 * c;
+            own[c] = x < d.nx && y[c] < d.ny;
+            oc[c] = own[c] ? x + int64_t(d.nx) * y[c] : 0;
+            oface[c] = x == 0 || y[c] == 0 || x == d.nx - 1 || y[c] == d.ny - 1;
+            T ra, pa, rb, pb;
+            load(own[c], oc[c], z0 - 1, ra, pa);
+            load(own[c], oc[c], z0, rb, pb);
+            load(own[c], oc[c], z0 + 1, r1[c], p1[c]);
+            pprev[c] = pn(own[c], oface[c], oc[c], x, y[c], z0 - 1, ra, pa);
+            pc[c] = pn(own[c], oface[c], oc[c], x, y[c], z0, rb, pb);
+        }
+        T hr, hp;
         load(hown, hc, z0, hr, hp);
-        T pprev = pn(own, oface, oc, x, y, z0 - 1, ra, pa);
-        T pc = pn(own, oface, oc, x, y, z0, rb, pb);
         // the previous item's last plane may share a buffer with this item's first
         __syncthreads();
-        int64_t i = oc + int64_t(z0) * pl;  // this thread's cell of plane z
-        for (int z = z0; z < z1; z++, i += pl) {
+        for (int z = z0; z < z1; z++) {
             // one plane of lookahead: these loads are used in the next iteration
-            T r2, p2, hr2, hp2;
-            load(own, oc, z + 2, r2, p2);
+            T r2[kRY], p2[kRY], hr2, hp2, pnext[kRY];
+#pragma unroll
+            for (int c = 0; c < kRY; c++) {
+                load(own[c], oc[c], z + 2, r2[c], p2[c]);
+                pnext[c] = pn(own[c], oface[c], oc[c], x, y[c], z + 1, r1[c], p1[c]);
+            }
             load(hown, hc, z + 1, hr2, hp2);
-            const T pnext = pn(own, oface, oc, x, y, z + 1, r1, p1);
             const T hv = pn(hown, hface, hc, gx, gy, z, hr, hp);
             // buffer z & 1 was last read in iteration z - 2, before the barrier of iteration z - 1
             T (*plane)[kTX + 2] = planes[z & 1];
-            plane[ly + 1][lx + 1] = pc;
+#pragma unroll
+            for (int c = 0; c < kRY; c++) plane[ly0 + 8 * c + 1][lx + 1] = pc[c];
             if (halo) plane[hy + 1][hx + 1] = hv;
             __syncthreads();
-            if (own) {
+#pragma unroll
+            for (int c = 0; c < kRY; c++) {
+                if (!own[c]) continue;
+                const int     ly = ly0 + 8 * c;
+                const int64_t i = oc[c] + int64_t(z) * pl;
                 T             sc;
-                const bool    inner = !oface && z >= 1 && z < d.nz - 1;
+                const bool    inner = !oface[c] && z >= 1 && z < d.nz - 1;
                 if (BOX || (!d.bd && inner)) {
                     if (inner) {
                         T sum = T(0);
@@ -419,32 +449,36 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
                         sum = sum + plane[ly + 1][lx];
                         sum = sum + plane[ly + 2][lx + 1];
                         sum = sum + plane[ly][lx + 1];
-                        sum = sum + pnext;
-                        sum = sum + pprev;
-                        sc = (-sum + T(6) * pc) * invh2;
+                        sum = sum + pnext[c];
+                        sum = sum + pprev[c];
+                        sc = (-sum + T(6) * pc[c]) * invh2;
                     } else {
-                        sc = pc;  // Fixed face row
+                        sc = pc[c];  // Fixed face row
                     }
-                } else if (is_fixed(d, x, y, z, i)) {
-                    sc = pc;
+                } else if (is_fixed(d, x, y[c], z, i)) {
+                    sc = pc[c];
                 } else {  // neighbours in the oracle's order +x, -x, +y, -y, +z, -z, valid ones only
                     T   sum = T(0);
                     int n = 0;
                     if (x + 1 < d.nx) sum = sum + plane[ly + 1][lx + 2], n++;
                     if (x > 0) sum = sum + plane[ly + 1][lx], n++;
-                    if (y + 1 < d.ny) sum = sum + plane[ly + 2][lx + 1], n++;
-                    if (y > 0) sum = sum + plane[ly][lx + 1], n++;
-                    if (z + 1 < d.nz) sum = sum + pnext, n++;
-                    if (z > 0) sum = sum + pprev, n++;
-                    sc = (-sum + T(n) * pc) * invh2;
+                    if (y[c] + 1 < d.ny) sum = sum + plane[ly + 2][lx + 1], n++;
+                    if (y[c] > 0) sum = sum + plane[ly][lx + 1], n++;
+                    if (z + 1 < d.nz) sum = sum + pnext[c], n++;
+                    if (z > 0) sum = sum + pprev[c], n++;
+                    sc = (-sum + T(n) * pc[c]) * invh2;
                 }
-                p_new[i] = pc;
+                p_new[i] = pc[c];
                 s[i] = sc;
-                acc.add(pc, sc);
+                acc.add(pc[c], sc);
             }
-            pprev = pc;
-            pc = pnext;
-            r1 = r2, p1 = p2, hr = hr2, hp = hp2;
+#pragma unroll
+            for (int c = 0; c < kRY; c++) {
+                pprev[c] = pc[c];
+                pc[c] = pnext[c];
+                r1[c] = r2[c], p1[c] = p2[c];
+            }
+            hr = hr2, hp = hp2;
         }
     }
     double v[1] = {acc.value()};
@@ -455,8 +489,8 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     }
 }
 
-// pass B: x_lo += alpha p; r -= alpha s; rz' = <r, z>; rr = <r, r>. The
-// work items of pass A (32 x 8 columns, chunks of kZC planes): each thread
+// pass B: x_lo += alpha p; r -= alpha s; rz' = <r, z>; rr = <r, r>. Work
+// items of 32 x 8 columns and chunks of d.zc planes: each thread
 // walks its column with a running index, the loads of the next plane in
 // flight while the current one is updated; BOX as in pass A.
 template <typename T, bool BOX>
@@ -469,12 +503,12 @@ __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* _
     const T       dg6 = invdiag6<T>(d, jac);
     const int     lx = threadIdx.x % kTX, ly = threadIdx.x / kTX;
     const int     ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTY - 1) / kTY;
-    const int     items = pass_a_items(d);
+    const int     items = pass_b_items(d);
     const int64_t pl = int64_t(d.nx) * d.ny;
     DotAcc<T>     a0, a1;
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int tx = item % ntx, rest = item / ntx, ty = rest % nty, zc = rest / nty;
-        const int x = tx * kTX + lx, y = ty * kTY + ly, z0 = zc * kZC, z1 = min(z0 + kZC, d.nz);
+        const int x = tx * kTX + lx, y = ty * kTY + ly, z0 = zc * d.zc, z1 = min(z0 + d.zc, d.nz);
         if (x >= d.nx || y >= d.ny) continue;  // no barrier in this kernel
         const bool oface = x == 0 || y == 0 || x == d.nx - 1 || y == d.ny - 1;
         int64_t    i = x + int64_t(d.nx) * y + int64_t(z0) * pl;
@@ -591,7 +625,7 @@ int validate(const ngb_poisson_desc* d)
     NGB_CHECK_ARG(d->field == NGB_STORE_F32 || d->field == NGB_STORE_F64, "field must be NGB_STORE_F32 or NGB_STORE_F64");
     NGB_CHECK_ARG(d->h > 0, "h must be positive");
     NGB_CHECK_ARG(make_dom(d).segs < (int64_t(1) << 31), "grid too large (ny * nz * ceil(nx / 256) >= 2^31)");
-    NGB_CHECK_ARG(int64_t((d->nx + kTX - 1) / kTX) * ((d->ny + kTY - 1) / kTY) * ((d->nz + kZC - 1) / kZC) < (int64_t(1) << 31),
+    NGB_CHECK_ARG(int64_t((d->nx + kTX - 1) / kTX) * ((d->ny + kTY - 1) / kTY) * ((d->nz + 7) / 8) < (int64_t(1) << 31),
                   "grid too large for the CG tiling");
     return NGB_OK;
 }
@@ -645,6 +679,8 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
     NGB_LAUNCH_CHECK("cg_init_kernel");
     NGB_CUDA_TRY(cudaMemsetAsync(p1, 0, size_t(desc->nx) * desc->ny * desc->nz * sizeof(T), s));
 
+    // the two passes: no more CTAs than work items (partials hold `grid` entries)
+    const int grid_a = std::min(grid, pass_a_items(d)), grid_b = std::min(grid, pass_b_items(d));
     // Capture `check_every` iterations (rounded up to even: p ping-pongs) once.
     const int    per = std::max(2, (prm->check_every + 1) / 2 * 2);
     cudaStream_t cs;
@@ -656,13 +692,13 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
             T* pa = (it % 2 == 0) ? p0 : p1;
             T* pb = (it % 2 == 0) ? p1 : p0;
             if (d.bd)
-                cg_pass_a_kernel<T, false><<<grid, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
+                cg_pass_a_kernel<T, false><<<grid_a, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
             else
-                cg_pass_a_kernel<T, true><<<grid, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
+                cg_pass_a_kernel<T, true><<<grid_a, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
             if (d.bd)
-                cg_pass_b_kernel<T, false><<<grid, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
+                cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
             else
-                cg_pass_b_kernel<T, true><<<grid, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
+                cg_pass_b_kernel<T, true><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
             cg_refresh1_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, x, xlo);
             cg_refresh2_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, b, x, r, w.partials);
         }
