@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--extra", action="store_true", help="also time the other storage/lattice forms")
+    ap.add_argument("--profiles", default="", help="cavity: write the centre-line velocity profiles into this directory")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson", "learned", "accuracy"],
                     help="cavity: dense LBM (default, the headline); sphere: bGrid flow over a sphere; "
                          "poisson: Jacobi-PCG to 1e-8; learned: U-Net-preconditioned FCG vs Jacobi-PCG to 1e-8; "
@@ -252,6 +253,15 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = bpu * V / (per_step_ms * 1e-3) / 1e9
     traffic = profiled_traffic("lbm_%s_%s_dense_%d.md" % (lat, st, n))
+
+    # ---------------- centre-line velocity profiles (RunCavityTwoPop.cu:110-148)
+    if args.profiles and rank == 0:
+        done = args.warmup + (args.warmup % 2) + args.steps
+        u = torch.zeros(3 * V, dtype=torch.float64, device=dev)
+        ngb.lbm_dense_macroscopic(desc, fa if args.steps % 2 == 0 else fb, None, u, stream=stream)
+        os.makedirs(args.profiles, exist_ok=True)
+        ngb.write_cavity_profiles(args.profiles, done, *ngb.cavity_profiles(u, n, n, n, ulb))
+        del u
 
     # ---------------- end to end through the host-buffer C-ABI call
     e2e = None

@@ -235,6 +235,37 @@ def lbm_dense_macroscopic(desc, fin, rho=None, u=None, flags=None, stream=None):
                                                  _stream(stream)))
 
 
+def cavity_profiles(u, nx, ny, nz, ulid):
+    """Centre-line velocity profiles of the lid-driven cavity, as
+    RunCavityTwoPop.cu:110-148 writes them: u_x / ulid along y through
+    (nx/2, nz/2) and u_y / ulid along x through (ny/2, nz/2), positions
+    normalised by the grid size, sorted. `u` is the velocity of
+    ngb_lbm_dense_macroscopic (3 planes of nx*ny*nz doubles, host or device).
+    Returns (x_profile, y_profile) as lists of (position, value)."""
+    import numpy as np
+    uu = np.asarray(u.cpu() if hasattr(u, "cpu") else u, dtype=np.float64).reshape(3, nz, ny, nx)
+    scale = 1.0 / ulid
+    xc, yc, zc = nx // 2, ny // 2, nz // 2
+    yprof = [(y / ny, float(uu[0, zc, y, xc]) * scale) for y in range(ny)]
+    xprof = [(x / nx, float(uu[1, zc, yc, x]) * scale) for x in range(nx)]
+    return xprof, yprof
+
+
+def write_cavity_profiles(directory, iteration, xprof, yprof):
+    """NeonUniformLBM_<iteration, 5 digits>_{X,Y}.dat with lines "position value"
+    in the reference's default stream format (6 significant digits)."""
+    import os
+    tag = "%05d" % iteration if iteration < 100000 else str(iteration)
+    paths = []
+    for prof, axis in ((yprof, "Y"), (xprof, "X")):
+        path = os.path.join(directory, "NeonUniformLBM_%s_%s.dat" % (tag, axis))
+        with open(path, "w") as f:
+            for pos, val in prof:
+                f.write("%g %g\n" % (pos, val))
+        paths.append(path)
+    return paths
+
+
 # ----------------------------------------------------------------------------- bGrid
 class BGrid:
     """A block-sparse grid (8^3 blocks) built on the device from a dense byte

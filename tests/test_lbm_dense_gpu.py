@@ -206,3 +206,22 @@ def test_invalid_arguments_report_errors(ngb, cuda):
     d.box_cavity = 0
     with pytest.raises(ngb.NeonError, match="flags required"):
         ngb.lbm_dense_step(d, x, torch.empty_like(x))
+
+
+def test_cavity_profiles_match_oracle(ngb, orc, cuda):
+    """The velocity profiles of an FP64 cavity run: GPU macroscopic field
+    against the oracle's computeRhoAndU restatement, bit for bit."""
+    import torch
+    n, q, steps = 24, 19, 60
+    desc = ngb.lbm_dense_desc(n, n, n, q, "f64", ngb.cavity_omega(n, 0.1, 100.0), ngb.lid_wall_terms(q, 0.1))
+    fa = torch.empty(q * n ** 3, dtype=torch.float64, device=cuda)
+    fb = torch.empty_like(fa)
+    ngb.lbm_cavity_init(desc, 0.1, fa, fb)
+    ngb.lbm_dense_run(desc, fa, fb, steps)
+    u = torch.zeros(3 * n ** 3, dtype=torch.float64, device=cuda)
+    ngb.lbm_dense_macroscopic(desc, fa, None, u)
+    pop64, oflags, _ = oracle_cavity(orc, n, q, 0, steps)
+    uo = oracle_velocity(orc, n, q, 0, oflags, pop64)
+    xg, yg = ngb.cavity_profiles(u, n, n, n, 0.1)
+    xo, yo = ngb.cavity_profiles(uo, n, n, n, 0.1)
+    assert xg == xo and yg == yo

@@ -71,3 +71,22 @@ def test_wall_mask_semantics(orc):
             sx, sy, sz = x - c[0], y - c[1], z - c[2]
             wall = sx in (0, n - 1) or sy in (0, n - 1) or sz in (0, n - 1)
             assert bool(mask >> q & 1) == (wall and c != (0, 0, 0))
+
+
+def test_cavity_profiles_format(tmp_path):
+    """Centre-line profiles as the reference's cavity run writes them
+    (RunCavityTwoPop.cu:110-148): u_x / ulid along y at (nx/2, nz/2),
+    u_y / ulid along x at (ny/2, nz/2), "%g %g" lines, 5-digit iteration."""
+    import neon_gb300 as ngb
+    nx, ny, nz = 6, 5, 4
+    u = np.zeros((3, nz, ny, nx))
+    u[0] = np.arange(nx * ny * nz).reshape(nz, ny, nx) * 0.01
+    u[1] = -np.arange(nx * ny * nz).reshape(nz, ny, nx) * 0.02
+    xp, yp = ngb.cavity_profiles(u.ravel(), nx, ny, nz, 0.1)
+    assert [p for p, _ in yp] == [y / ny for y in range(ny)]
+    assert np.allclose([v for _, v in yp], [u[0, 2, y, 3] / 0.1 for y in range(ny)])
+    assert np.allclose([v for _, v in xp], [u[1, 2, 2, x] / 0.1 for x in range(nx)])
+    py, px = ngb.write_cavity_profiles(str(tmp_path), 42, xp, yp)
+    assert py.endswith("NeonUniformLBM_00042_Y.dat") and px.endswith("NeonUniformLBM_00042_X.dat")
+    lines = open(py).read().splitlines()
+    assert len(lines) == ny and lines[1] == "%g %g" % (yp[1][0], yp[1][1])
