@@ -34,11 +34,7 @@
 // (read by ngb_conv3d_tc_check), waits for its own copies and MMAs with the
 // same bound, frees its TMEM and returns.
 #include "common.cuh"
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
-#include <mutex>
+#include "tma.cuh"
 
 namespace ngb {
 namespace {
@@ -51,32 +47,6 @@ constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.b32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
 // Wait for the phase of `parity` to complete; false when this CTA has given up
 // (its own limit ran out, or another role's did).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
@@ -95,21 +65,6 @@ __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity)
     for (uint32_t i = 0; i < kWaitLimit; i++)
         if (mbar_try_wait(bar, parity)) return;
     atomicExch(&g_tc_error, 1);
-}
-
-__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c1, int c2, int c3, int c4, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
-        "[%7];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -232,7 +187,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         mbar_init(&drain_bar, 1);
         mbar_init(&w_bar, 1);
         abort_sh = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init_fence();
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
@@ -269,11 +224,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
                 size_t boff;
                 if (p.plane) {
                     const int dzi = outer;
-                    tma_load_5d(st, &xmap, t.x0 - 1, t.y0 - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
+                    tma_load_5d(st, &xmap, 0, t.x0 - 1, t.y0 - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
                     boff = (size_t(dzi) * p.kc + chunk) * 9 * slice;
                 } else {
                     const int dzi = outer / 9, dyi = (outer / 3) % 3, dxi = outer % 3;
-                    tma_load_5d(st, &xmap, t.x0 + dxi - 1, t.y0 + dyi - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
+                    tma_load_5d(st, &xmap, 0, t.x0 + dxi - 1, t.y0 + dyi - 1, t.z0 + dzi - 1, 2 * chunk, &full_bar[s]);
                     boff = ((size_t(dzi) * p.kc + chunk) * 9 + dyi * 3 + dxi) * slice;
                 }
                 if (!p.resident) bulk_load(st + b_off, reinterpret_cast<const uint8_t*>(p.wpk) + boff, p.b_bytes, &full_bar[s]);
@@ -407,20 +362,6 @@ __global__ void conv3d_pack_kernel(int cout, int cin, const __nv_bfloat16* __res
         const int c16 = int(r % kc), dz = int(r / kc);
         out[i] = w[(int64_t(n) * 27 + 9 * dz + 3 * dy + dx) * cin + c16 * 16 + h * 8 + e];
     }
-}
-
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::once_flag                    once;
-    std::call_once(once, []() {
-        void*                           p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    });
-    return fn;
 }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
