@@ -3,6 +3,7 @@
 // sequence of the dense kernel; FP64 keeps the reference operation order).
 #include "bgrid.cuh"
 #include "lbm_shifted.cuh"
+#include <mutex>
 #include <random>
 #include <vector>
 
@@ -92,6 +93,23 @@ __device__ __forceinline__ const S* bgrid_src(const S* __restrict__ fin, const u
     return masked ? fin + (bq + L::opp(q)) * kBlockVoxels + v : fin + (size_t(nb) * Q + q) * kBlockVoxels + nv;
 }
 
+// Outlet voxel (zero-gradient outflow): copy the populations of the x-1
+// neighbour when it is a valid voxel.
+template <int Q, typename S>
+__device__ __forceinline__ void bgrid_outlet(const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* mask,
+                                             const uint32_t* conn, uint32_t b, int v, int i, int j, int k)
+{
+    uint32_t     nb;
+    int          nv;
+    const size_t bq = size_t(b) * Q;
+    if (bgrid_valid_ngh(mask, conn, b, i, j, k, -1, 0, 0, nb, nv)) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) fout[(bq + q) * kBlockVoxels + v] = fin[(size_t(nb) * Q + q) * kBlockVoxels + nv];
+    }
+}
+
+// One thread per voxel, each pull source resolved per direction (FP64 with
+// the reference's operation order, or the FP32 shifted form).
 template <int Q, typename S, bool F64>
 __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgrid_lbm_kernel(const S* __restrict__ fin, S* __restrict__ fout,
                                                                  const uint32_t* __restrict__ flags,
@@ -106,13 +124,8 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgr
     __syncthreads();
     const int    cls = flag_class(f);
     const size_t bq = size_t(b) * Q;
-    if (cls == NGB_CELL_OUTLET) {  // zero-gradient outflow: copy the x-1 neighbour
-        uint32_t nb;
-        int      nv;
-        if (bgrid_valid_ngh(p.mask, p.conn, b, i, j, k, -1, 0, 0, nb, nv)) {
-#pragma unroll
-            for (int q = 0; q < Q; q++) fout[(bq + q) * kBlockVoxels + v] = fin[(size_t(nb) * Q + q) * kBlockVoxels + nv];
-        }
+    if (cls == NGB_CELL_OUTLET) {
+        bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v, i, j, k);
         return;
     }
     if (cls != NGB_CELL_BULK) return;
@@ -148,6 +161,209 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgr
 #pragma unroll
         for (int q = 0; q < Q; q++) PairIO<S>::store1(fout + (bq + q) * kBlockVoxels + v, g[q], float(L::w(q)));
     }
+}
+
+// ---------------------------------------------------------------- staged step (16-bit D3Q19)
+// Each moving direction q gets a 9^3 cube in shared memory holding every value
+// the block's voxels pull along q: voxel (i,j,k)'s own population q sits at
+// (i + [cx>0], j + [cy>0], k + [cz>0]), so the source (i,j,k) - c_q of every
+// voxel falls at (i - cx + [cx>0], ...) inside the cube; the cube cells that
+// are not own positions (the halo: 64 per face direction, 120 per edge
+// direction, 169 per corner direction) come from the neighbour blocks. A
+// compile-time table lists every halo cell (cube index, neighbour slot, source
+// element), so filling the halo is a table walk spread over the block's
+// threads; after one barrier every pull is a shared load at a fixed offset.
+constexpr int kCube = 729;
+
+template <int Q>
+__host__ __device__ constexpr bool is_rest(int q)
+{
+    return Lattice<Q>::cx(q) == 0 && Lattice<Q>::cy(q) == 0 && Lattice<Q>::cz(q) == 0;
+}
+template <int Q>
+__host__ __device__ constexpr int rest_dir()
+{
+    int r = 0;
+    for (int q = 0; q < Q; q++)
+        if (is_rest<Q>(q)) r = q;
+    return r;
+}
+// Index of a moving direction among the moving directions (q order).
+template <int Q>
+__host__ __device__ constexpr int moving_index(int q)
+{
+    int n = 0;
+    for (int p = 0; p < q; p++) n += is_rest<Q>(p) ? 0 : 1;
+    return n;
+}
+// Cube offset of a voxel's own population along q, and of its pull source.
+template <int Q>
+__host__ __device__ constexpr int cube_own(int q)
+{
+    return moving_index<Q>(q) * kCube + (Lattice<Q>::cx(q) > 0) + 9 * (Lattice<Q>::cy(q) > 0) + 81 * (Lattice<Q>::cz(q) > 0);
+}
+template <int Q>
+__host__ __device__ constexpr int cube_src(int q)
+{
+    return cube_own<Q>(q) - Lattice<Q>::cx(q) - 9 * Lattice<Q>::cy(q) - 81 * Lattice<Q>::cz(q);
+}
+template <int Q>
+constexpr int halo_count()
+{
+    int n = 0;
+    for (int q = 0; q < Q; q++) {
+        if (is_rest<Q>(q)) continue;
+        const int in = (Lattice<Q>::cx(q) ? 7 : 8) * (Lattice<Q>::cy(q) ? 7 : 8) * (Lattice<Q>::cz(q) ? 7 : 8);
+        n += kBlockVoxels - in;
+    }
+    return n;
+}
+
+// Halo cells: dst = cube index | neighbour slot << 16 (slot (fx+1) + 3(fy+1) +
+// 9(fz+1) of the connectivity row), src = q * 512 + voxel in that block.
+template <int Q>
+struct HaloTable {
+    static constexpr int n = halo_count<Q>();
+    uint32_t             dst[n];
+    uint32_t             src[n];
+};
+
+template <int Q>
+constexpr HaloTable<Q> make_halo_table()
+{
+    HaloTable<Q> t{};
+    int          n = 0;
+    for (int q = 0; q < Q; q++) {
+        if (is_rest<Q>(q)) continue;
+        const int cx = Lattice<Q>::cx(q), cy = Lattice<Q>::cy(q), cz = Lattice<Q>::cz(q);
+        for (int k = 0; k < 8; k++)
+            for (int j = 0; j < 8; j++)
+                for (int i = 0; i < 8; i++) {
+                    const int si = i - cx, sj = j - cy, sk = k - cz;
+                    const int fx = si < 0 ? -1 : (si > 7 ? 1 : 0), fy = sj < 0 ? -1 : (sj > 7 ? 1 : 0),
+                              fz = sk < 0 ? -1 : (sk > 7 ? 1 : 0);
+                    if (fx == 0 && fy == 0 && fz == 0) continue;
+                    const int cube = cube_src<Q>(q) + i + 9 * j + 81 * k;
+                    const int slot = (fx + 1) + 3 * (fy + 1) + 9 * (fz + 1);
+                    const int nv = (si - 8 * fx) + 8 * (sj - 8 * fy) + 64 * (sk - 8 * fz);
+                    t.dst[n] = uint32_t(cube) | (uint32_t(slot) << 16);
+                    t.src[n] = uint32_t(q * kBlockVoxels + nv);
+                    n++;
+                }
+    }
+    return t;
+}
+
+__device__ const HaloTable<19> g_halo19 = make_halo_table<19>();
+
+template <int Q>
+__device__ __forceinline__ const HaloTable<Q>& halo_table();
+template <>
+__device__ __forceinline__ const HaloTable<19>& halo_table<19>() { return g_halo19; }
+
+template <int Q, typename S>
+constexpr size_t staged_smem() { return size_t(Q - 1) * kCube * sizeof(S); }
+
+template <int Q, typename S>
+__global__ void __launch_bounds__(kBlockVoxels, Q == 19 ? 4 : 3)
+    bgrid_lbm_staged_kernel(const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* __restrict__ flags, BParams<float> p)
+{
+    using L = Lattice<Q>;
+    constexpr int       kRest = rest_dir<Q>();
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    S*                  st = reinterpret_cast<S*>(smem_raw);
+    __shared__ uint32_t sconn[27];
+    __shared__ uint32_t smissing;  // bit s set: neighbour slot s has no block
+
+    const uint32_t b = blockIdx.x;
+    const int      v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
+    if (v < 32) {
+        const uint32_t nb = v < 27 ? __ldg(p.conn + size_t(b) * 27 + v) : 0u;
+        if (v < 27) sconn[v] = nb;
+        const uint32_t miss = __ballot_sync(0xffffffffu, v < 27 && nb == NGB_BGRID_NO_BLOCK);
+        if (v == 0) smissing = miss;
+    }
+    const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
+    // this voxel's own populations into their cubes
+    const S* own = fin + size_t(b) * Q * kBlockVoxels + v;
+    const int po = i + 9 * j + 81 * k;
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+        if (!is_rest<Q>(q)) st[po + cube_own<Q>(q)] = own[q * kBlockVoxels];
+    const S rest = own[kRest * kBlockVoxels];
+    // halo cells from the neighbour blocks (a missing block leaves its cells
+    // unset: every voxel pulling from one treats the direction as a wall)
+    const HaloTable<Q>& h = halo_table<Q>();
+#pragma unroll 4
+    for (int it = v; it < HaloTable<Q>::n; it += kBlockVoxels) {
+        const uint32_t d = __ldg(&h.dst[it]);
+        const uint32_t nb = __ldg(p.conn + size_t(b) * 27 + (d >> 16));
+        if (nb != NGB_BGRID_NO_BLOCK) st[d & 0xffffu] = __ldg(fin + size_t(nb) * Q * kBlockVoxels + __ldg(&h.src[it]));
+    }
+    __syncthreads();
+
+    const int cls = flag_class(f);
+    if (cls == NGB_CELL_OUTLET) {
+        bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v, i, j, k);
+        return;
+    }
+    if (cls != NGB_CELL_BULK) return;
+    uint32_t m = flag_mask(f);
+    if (smissing) {  // a source outside every block is a wall
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (is_rest<Q>(q)) continue;
+            int nv;
+            if (bgrid_pull_src<Q>(sconn, i, j, k, q, nv) == NGB_BGRID_NO_BLOCK) m |= 1u << q;
+        }
+    }
+    const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m) : 0u;
+    const S*       sp = st + po;
+    float          g[Q];
+    if (m == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; q++)
+            g[q] = PairIO<S>::to_g1(is_rest<Q>(q) ? rest : sp[cube_src<Q>(q)], float(L::w(q)));
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int o = L::opp(q);
+            if (is_rest<Q>(q)) {
+                g[q] = PairIO<S>::to_g1(rest, float(L::w(q)));
+            } else if ((m >> q) & 1u) {
+                // w(opp q) == w(q), so one conversion serves both cases
+                g[q] = PairIO<S>::to_g1(sp[cube_own<Q>(o)], float(L::w(q))) + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+            } else {
+                g[q] = PairIO<S>::to_g1(sp[cube_src<Q>(q)], float(L::w(q)));
+            }
+        }
+    }
+    bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
+    S* out = fout + size_t(b) * Q * kBlockVoxels + v;
+#pragma unroll
+    for (int q = 0; q < Q; q++) PairIO<S>::store1(out + q * kBlockVoxels, g[q], float(L::w(q)));
+}
+
+template <int Q, typename S>
+int launch_staged(const ngb_bgrid_desc* d, const void* fin, void* fout, const uint32_t* flags, const BParams<float>& p, cudaStream_t s)
+{
+    static std::once_flag once;
+    static cudaError_t    err = cudaSuccess;
+    std::call_once(once, []() {
+        err = cudaFuncSetAttribute(bgrid_lbm_staged_kernel<Q, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(staged_smem<Q, S>()));
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(bgrid_lbm_staged_kernel<Q, S>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       int(cudaSharedmemCarveoutMaxShared));
+    });
+    if (err != cudaSuccess) {
+        set_error("bGrid LBM kernel set-up failed: %s", cudaGetErrorString(err));
+        return NGB_ERR_CUDA;
+    }
+    bgrid_lbm_staged_kernel<Q, S><<<d->n_blocks, kBlockVoxels, staged_smem<Q, S>(), s>>>(static_cast<const S*>(fin),
+                                                                                         static_cast<S*>(fout), flags, p);
+    NGB_LAUNCH_CHECK("bgrid_lbm_staged_kernel");
+    return NGB_OK;
 }
 
 // ---------------------------------------------------------------- drag
@@ -273,35 +489,37 @@ int launch_bgrid_lbm(const ngb_bgrid_desc* d, const void* fin, void* fout, const
         for (int c = 0; c < 2; c++)
             for (int q = 0; q < 27; q++) p.wall[c][q] = d->wall_term[c][q];
         p.mask = d->mask, p.conn = d->conn;
+        const double* a = static_cast<const double*>(fin);
+        double*       o = static_cast<double*>(fout);
         if (q19)
-            bgrid_lbm_kernel<19, double, true><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const double*>(fin),
-                                                                                   static_cast<double*>(fout), flags, p);
+            bgrid_lbm_kernel<19, double, true><<<d->n_blocks, kBlockVoxels, 0, s>>>(a, o, flags, p);
         else
-            bgrid_lbm_kernel<27, double, true><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const double*>(fin),
-                                                                                   static_cast<double*>(fout), flags, p);
-    } else {
-        BParams<float> p{};
-        p.omega = float(d->omega);
-        // FP16 values are 2^14 g: the wall terms added to them scale alike
-        const float up = d->storage == NGB_STORE_F16OFF ? NGB_F16OFF_SCALE : 1.0f;
-        for (int c = 0; c < 2; c++)
-            for (int q = 0; q < 27; q++) p.wall[c][q] = float(d->wall_term[c][q]) * up;
-        p.mask = d->mask, p.conn = d->conn;
+            bgrid_lbm_kernel<27, double, true><<<d->n_blocks, kBlockVoxels, 0, s>>>(a, o, flags, p);
+        NGB_LAUNCH_CHECK("bgrid_lbm_kernel");
+        return NGB_OK;
+    }
+    BParams<float> p{};
+    p.omega = float(d->omega);
+    // FP16 values are 2^14 g: the wall terms added to them scale alike
+    const float up = d->storage == NGB_STORE_F16OFF ? NGB_F16OFF_SCALE : 1.0f;
+    for (int c = 0; c < 2; c++)
+        for (int q = 0; q < 27; q++) p.wall[c][q] = float(d->wall_term[c][q]) * up;
+    p.mask = d->mask, p.conn = d->conn;
+    // D3Q19 with 16-bit storage: the shared-memory staged kernel (measured
+    // faster there); FP32 storage and D3Q27: per-direction pull (the staged
+    // form measured slower for them)
+    if (q19 && d->storage == NGB_STORE_F16OFF) return launch_staged<19, __half>(d, fin, fout, flags, p, s);
+    if (q19 && d->storage == NGB_STORE_BF16OFF) return launch_staged<19, __nv_bfloat16>(d, fin, fout, flags, p, s);
 #define NGB_B(QQ, T) \
     bgrid_lbm_kernel<QQ, T, false><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)
-        switch (d->storage) {
-            case NGB_STORE_F32:
-                if (q19) NGB_B(19, float); else NGB_B(27, float);
-                break;
-            case NGB_STORE_F16OFF:
-                if (q19) NGB_B(19, __half); else NGB_B(27, __half);
-                break;
-            default:
-                if (q19) NGB_B(19, __nv_bfloat16); else NGB_B(27, __nv_bfloat16);
-                break;
-        }
-#undef NGB_B
+    switch (d->storage) {
+        case NGB_STORE_F32:
+            if (q19) NGB_B(19, float); else NGB_B(27, float);
+            break;
+        case NGB_STORE_F16OFF: NGB_B(27, __half); break;
+        default: NGB_B(27, __nv_bfloat16); break;
     }
+#undef NGB_B
     NGB_LAUNCH_CHECK("bgrid_lbm_kernel");
     return NGB_OK;
 }
