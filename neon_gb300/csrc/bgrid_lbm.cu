@@ -164,16 +164,21 @@ __global__ void __launch_bounds__(kBlockVoxels, F64 ? 1 : (Q == 19 ? 4 : 3)) bgr
 }
 
 // ---------------------------------------------------------------- staged step (16-bit D3Q19)
-// Each moving direction q gets a 9^3 cube in shared memory holding every value
-// the block's voxels pull along q: voxel (i,j,k)'s own population q sits at
-// (i + [cx>0], j + [cy>0], k + [cz>0]), so the source (i,j,k) - c_q of every
-// voxel falls at (i - cx + [cx>0], ...) inside the cube; the cube cells that
-// are not own positions (the halo: 64 per face direction, 120 per edge
-// direction, 169 per corner direction) come from the neighbour blocks. A
-// compile-time table lists every halo cell (cube index, neighbour slot, source
-// element), so filling the halo is a table walk spread over the block's
-// threads; after one barrier every pull is a shared load at a fixed offset.
-constexpr int kCube = 729;
+// Each moving direction q gets a cube in shared memory (x pitch 10, 9 rows,
+// 9 planes) holding every value the block's voxels pull along q: voxel
+// (i,j,k)'s own population q sits at (i + [cx != 0], j + [cy > 0],
+// k + [cz > 0]), so the source (i,j,k) - c_q of every voxel falls inside the
+// cube, and for an even i on an even x: a voxel pair (i, i+1) pulls each
+// direction with one 32-bit shared load. The cube cells that are not own
+// positions (the halo: 64 per face direction, 120 per edge direction) come
+// from the neighbour blocks through a compile-time table (cube index,
+// neighbour slot, source element) walked by the block's threads. One thread
+// per x-pair: the collision runs on FP32x2 pairs (per lane the scalar
+// sequence, so the results equal the per-voxel kernel's bit for bit) and each
+// direction is stored as one 32-bit word per pair. All global loads of a
+// thread (own pairs, halo values) are issued before its first shared store.
+constexpr int kPX = 10, kPY = 9, kCubeP = kPX * kPY * 9;
+constexpr int kStagedThreads = kBlockVoxels / 2;
 
 template <int Q>
 __host__ __device__ constexpr bool is_rest(int q)
@@ -196,16 +201,17 @@ __host__ __device__ constexpr int moving_index(int q)
     for (int p = 0; p < q; p++) n += is_rest<Q>(p) ? 0 : 1;
     return n;
 }
+__host__ __device__ constexpr int cube_voxel(int i, int j, int k) { return i + kPX * j + kPX * kPY * k; }
 // Cube offset of a voxel's own population along q, and of its pull source.
 template <int Q>
 __host__ __device__ constexpr int cube_own(int q)
 {
-    return moving_index<Q>(q) * kCube + (Lattice<Q>::cx(q) > 0) + 9 * (Lattice<Q>::cy(q) > 0) + 81 * (Lattice<Q>::cz(q) > 0);
+    return moving_index<Q>(q) * kCubeP + cube_voxel(Lattice<Q>::cx(q) != 0, Lattice<Q>::cy(q) > 0, Lattice<Q>::cz(q) > 0);
 }
 template <int Q>
 __host__ __device__ constexpr int cube_src(int q)
 {
-    return cube_own<Q>(q) - Lattice<Q>::cx(q) - 9 * Lattice<Q>::cy(q) - 81 * Lattice<Q>::cz(q);
+    return cube_own<Q>(q) - cube_voxel(Lattice<Q>::cx(q), Lattice<Q>::cy(q), Lattice<Q>::cz(q));
 }
 template <int Q>
 constexpr int halo_count()
@@ -243,7 +249,7 @@ constexpr HaloTable<Q> make_halo_table()
                     const int fx = si < 0 ? -1 : (si > 7 ? 1 : 0), fy = sj < 0 ? -1 : (sj > 7 ? 1 : 0),
                               fz = sk < 0 ? -1 : (sk > 7 ? 1 : 0);
                     if (fx == 0 && fy == 0 && fz == 0) continue;
-                    const int cube = cube_src<Q>(q) + i + 9 * j + 81 * k;
+                    const int cube = cube_src<Q>(q) + cube_voxel(i, j, k);
                     const int slot = (fx + 1) + 3 * (fy + 1) + 9 * (fz + 1);
                     const int nv = (si - 8 * fx) + 8 * (sj - 8 * fy) + 64 * (sk - 8 * fz);
                     t.dst[n] = uint32_t(cube) | (uint32_t(slot) << 16);
@@ -256,87 +262,32 @@ constexpr HaloTable<Q> make_halo_table()
 
 __device__ const HaloTable<19> g_halo19 = make_halo_table<19>();
 
-template <int Q>
-__device__ __forceinline__ const HaloTable<Q>& halo_table();
-template <>
-__device__ __forceinline__ const HaloTable<19>& halo_table<19>() { return g_halo19; }
+__device__ __forceinline__ __half        lo_of(__half2 w) { return __low2half(w); }
+__device__ __forceinline__ __half        hi_of(__half2 w) { return __high2half(w); }
+__device__ __forceinline__ __nv_bfloat16 lo_of(__nv_bfloat162 w) { return __low2bfloat16(w); }
+__device__ __forceinline__ __nv_bfloat16 hi_of(__nv_bfloat162 w) { return __high2bfloat16(w); }
 
-template <int Q, typename S>
-constexpr size_t staged_smem() { return size_t(Q - 1) * kCube * sizeof(S); }
-
-template <int Q, typename S>
-__global__ void __launch_bounds__(kBlockVoxels, Q == 19 ? 4 : 3)
-    bgrid_lbm_staged_kernel(const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* __restrict__ flags, BParams<float> p)
+// One bulk voxel of a pair whose partner is not bulk: scalar pull from the
+// cubes (lane 0 or 1 of the pair), collision, store.
+template <typename S>
+__device__ __forceinline__ void staged_voxel(const S* sp, const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* flags,
+                                             const uint32_t* sconn, const BParams<float>& p, uint32_t b, int v, int i, int j,
+                                             int k, uint32_t m)
 {
+    constexpr int  Q = 19;
     using L = Lattice<Q>;
-    constexpr int       kRest = rest_dir<Q>();
-    extern __shared__ __align__(16) uint8_t smem_raw[];
-    S*                  st = reinterpret_cast<S*>(smem_raw);
-    __shared__ uint32_t sconn[27];
-    __shared__ uint32_t smissing;  // bit s set: neighbour slot s has no block
-
-    const uint32_t b = blockIdx.x;
-    const int      v = threadIdx.x, i = v & 7, j = (v >> 3) & 7, k = v >> 6;
-    if (v < 32) {
-        const uint32_t nb = v < 27 ? __ldg(p.conn + size_t(b) * 27 + v) : 0u;
-        if (v < 27) sconn[v] = nb;
-        const uint32_t miss = __ballot_sync(0xffffffffu, v < 27 && nb == NGB_BGRID_NO_BLOCK);
-        if (v == 0) smissing = miss;
-    }
-    const uint32_t f = __ldg(flags + size_t(b) * kBlockVoxels + v);
-    // this voxel's own populations into their cubes
-    const S* own = fin + size_t(b) * Q * kBlockVoxels + v;
-    const int po = i + 9 * j + 81 * k;
-#pragma unroll
-    for (int q = 0; q < Q; q++)
-        if (!is_rest<Q>(q)) st[po + cube_own<Q>(q)] = own[q * kBlockVoxels];
-    const S rest = own[kRest * kBlockVoxels];
-    // halo cells from the neighbour blocks (a missing block leaves its cells
-    // unset: every voxel pulling from one treats the direction as a wall)
-    const HaloTable<Q>& h = halo_table<Q>();
-#pragma unroll 4
-    for (int it = v; it < HaloTable<Q>::n; it += kBlockVoxels) {
-        const uint32_t d = __ldg(&h.dst[it]);
-        const uint32_t nb = __ldg(p.conn + size_t(b) * 27 + (d >> 16));
-        if (nb != NGB_BGRID_NO_BLOCK) st[d & 0xffffu] = __ldg(fin + size_t(nb) * Q * kBlockVoxels + __ldg(&h.src[it]));
-    }
-    __syncthreads();
-
-    const int cls = flag_class(f);
-    if (cls == NGB_CELL_OUTLET) {
-        bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v, i, j, k);
-        return;
-    }
-    if (cls != NGB_CELL_BULK) return;
-    uint32_t m = flag_mask(f);
-    if (smissing) {  // a source outside every block is a wall
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            if (is_rest<Q>(q)) continue;
-            int nv;
-            if (bgrid_pull_src<Q>(sconn, i, j, k, q, nv) == NGB_BGRID_NO_BLOCK) m |= 1u << q;
-        }
-    }
     const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m) : 0u;
-    const S*       sp = st + po;
+    const S*       own = fin + size_t(b) * Q * kBlockVoxels + v;
     float          g[Q];
-    if (m == 0) {
 #pragma unroll
-        for (int q = 0; q < Q; q++)
-            g[q] = PairIO<S>::to_g1(is_rest<Q>(q) ? rest : sp[cube_src<Q>(q)], float(L::w(q)));
-    } else {
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            const int o = L::opp(q);
-            if (is_rest<Q>(q)) {
-                g[q] = PairIO<S>::to_g1(rest, float(L::w(q)));
-            } else if ((m >> q) & 1u) {
-                // w(opp q) == w(q), so one conversion serves both cases
-                g[q] = PairIO<S>::to_g1(sp[cube_own<Q>(o)], float(L::w(q))) + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
-            } else {
-                g[q] = PairIO<S>::to_g1(sp[cube_src<Q>(q)], float(L::w(q)));
-            }
-        }
+    for (int q = 0; q < Q; q++) {
+        const int o = L::opp(q);
+        if (is_rest<Q>(q))
+            g[q] = PairIO<S>::to_g1(own[q * kBlockVoxels], float(L::w(q)));
+        else if ((m >> q) & 1u)  // w(opp q) == w(q)
+            g[q] = PairIO<S>::to_g1(sp[cube_own<Q>(o)], float(L::w(q))) + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
+        else
+            g[q] = PairIO<S>::to_g1(sp[cube_src<Q>(q)], float(L::w(q)));
     }
     bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
     S* out = fout + size_t(b) * Q * kBlockVoxels + v;
@@ -344,24 +295,136 @@ __global__ void __launch_bounds__(kBlockVoxels, Q == 19 ? 4 : 3)
     for (int q = 0; q < Q; q++) PairIO<S>::store1(out + q * kBlockVoxels, g[q], float(L::w(q)));
 }
 
-template <int Q, typename S>
+template <typename S>
+constexpr size_t staged_smem()
+{
+    return size_t(18) * kCubeP * sizeof(S);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(kStagedThreads, 4)
+    bgrid_lbm_staged_kernel(const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* __restrict__ flags, BParams<float> p)
+{
+    constexpr int Q = 19;
+    using L = Lattice<Q>;
+    using W = typename PairIO<S>::Word;
+    constexpr int kHalo = HaloTable<Q>::n, kPer = (kHalo + kStagedThreads - 1) / kStagedThreads;
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    S*                  st = reinterpret_cast<S*>(smem_raw);
+    __shared__ uint32_t sconn[27];
+    __shared__ uint32_t smissing;  // bit s set: neighbour slot s has no block
+
+    const uint32_t b = blockIdx.x;
+    const int      t = threadIdx.x, i = 2 * (t & 3), j = (t >> 2) & 7, k = t >> 5, v = i + 8 * j + 64 * k;
+    if (t < 32) {
+        const uint32_t nb = t < 27 ? __ldg(p.conn + size_t(b) * 27 + t) : 0u;
+        if (t < 27) sconn[t] = nb;
+        const uint32_t miss = __ballot_sync(0xffffffffu, t < 27 && nb == NGB_BGRID_NO_BLOCK);
+        if (t == 0) smissing = miss;
+    }
+    const uint2 fl = __ldg(reinterpret_cast<const uint2*>(flags + size_t(b) * kBlockVoxels + v));
+    // own populations of the pair, and this thread's halo table entries
+    const S* own = fin + size_t(b) * Q * kBlockVoxels + v;
+    W        ov[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) ov[q] = __ldg(reinterpret_cast<const W*>(own + q * kBlockVoxels));
+    uint32_t hd[kPer], hs[kPer];
+#pragma unroll
+    for (int r = 0; r < kPer; r++) {
+        const int it = t + r * kStagedThreads;
+        hd[r] = it < kHalo ? __ldg(&g_halo19.dst[it]) : 0xffffffffu;
+        hs[r] = it < kHalo ? __ldg(&g_halo19.src[it]) : 0u;
+    }
+    __syncthreads();  // sconn
+    // halo values (a missing neighbour block leaves its cells unset: every
+    // voxel pulling from one treats the direction as a wall)
+    S hv[kPer];
+#pragma unroll
+    for (int r = 0; r < kPer; r++) {
+        const uint32_t nb = hd[r] != 0xffffffffu ? sconn[hd[r] >> 16] : NGB_BGRID_NO_BLOCK;
+        if (nb == NGB_BGRID_NO_BLOCK) hd[r] = 0xffffffffu;
+        hv[r] = nb != NGB_BGRID_NO_BLOCK ? __ldg(fin + size_t(nb) * Q * kBlockVoxels + hs[r]) : S();
+    }
+    const int pc = cube_voxel(i, j, k);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (is_rest<Q>(q)) continue;
+        S* d = st + pc + cube_own<Q>(q);
+        if ((cube_own<Q>(q) & 1) == 0) {  // unrolled: a compile-time test
+            *reinterpret_cast<W*>(d) = ov[q];
+        } else {
+            d[0] = lo_of(ov[q]);
+            d[1] = hi_of(ov[q]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kPer; r++)
+        if (hd[r] != 0xffffffffu) st[hd[r] & 0xffffu] = hv[r];
+    __syncthreads();
+
+    const int c0 = flag_class(fl.x), c1 = flag_class(fl.y);
+    uint32_t  m0 = flag_mask(fl.x), m1 = flag_mask(fl.y);
+    if (smissing) {  // a source outside every block is a wall
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (is_rest<Q>(q)) continue;
+            int nv;
+            if (bgrid_pull_src<Q>(sconn, i, j, k, q, nv) == NGB_BGRID_NO_BLOCK) m0 |= 1u << q;
+            if (bgrid_pull_src<Q>(sconn, i + 1, j, k, q, nv) == NGB_BGRID_NO_BLOCK) m1 |= 1u << q;
+        }
+    }
+    const S* sp = st + pc;
+    if (c0 == NGB_CELL_BULK && c1 == NGB_CELL_BULK) {
+        float2 g[Q];
+        if ((m0 | m1) == 0) {
+#pragma unroll
+            for (int q = 0; q < Q; q++)
+                g[q] = PairIO<S>::to_g(is_rest<Q>(q) ? ov[q] : *reinterpret_cast<const W*>(sp + cube_src<Q>(q)), float(L::w(q)));
+        } else {
+            const uint32_t l0 = m0 ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m0) : 0u;
+            const uint32_t l1 = m1 ? bgrid_lidbits<Q>(flags, p.mask, sconn, i + 1, j, k, m1) : 0u;
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                const int   o = L::opp(q);
+                const float w = float(L::w(q));  // w(opp q) == w(q)
+                if (is_rest<Q>(q)) {
+                    g[q] = PairIO<S>::to_g(ov[q], w);
+                } else {
+                    const S* a = sp + cube_src<Q>(q);
+                    const S* r = sp + cube_own<Q>(o);
+                    g[q].x = (m0 >> q) & 1u ? PairIO<S>::to_g1(r[0], w) + ((l0 >> q) & 1u ? p.wall[1][o] : p.wall[0][o])
+                                            : PairIO<S>::to_g1(a[0], w);
+                    g[q].y = (m1 >> q) & 1u ? PairIO<S>::to_g1(r[1], w) + ((l1 >> q) & 1u ? p.wall[1][o] : p.wall[0][o])
+                                            : PairIO<S>::to_g1(a[1], w);
+                }
+            }
+        }
+        bgk_shifted<Q, float2, StoreScale<S>::log2>(g, p.omega);
+        S* out = fout + size_t(b) * Q * kBlockVoxels + v;
+#pragma unroll
+        for (int q = 0; q < Q; q++) PairIO<S>::store(out + q * kBlockVoxels, g[q], float(L::w(q)));
+        return;
+    }
+    if (c0 == NGB_CELL_OUTLET) bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v, i, j, k);
+    if (c1 == NGB_CELL_OUTLET) bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v + 1, i + 1, j, k);
+    if (c0 == NGB_CELL_BULK) staged_voxel<S>(sp, fin, fout, flags, sconn, p, b, v, i, j, k, m0);
+    if (c1 == NGB_CELL_BULK) staged_voxel<S>(sp + 1, fin, fout, flags, sconn, p, b, v + 1, i + 1, j, k, m1);
+}
+
+template <typename S>
 int launch_staged(const ngb_bgrid_desc* d, const void* fin, void* fout, const uint32_t* flags, const BParams<float>& p, cudaStream_t s)
 {
     static std::once_flag once;
     static cudaError_t    err = cudaSuccess;
     std::call_once(once, []() {
-        err = cudaFuncSetAttribute(bgrid_lbm_staged_kernel<Q, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   int(staged_smem<Q, S>()));
-        if (err == cudaSuccess)
-            err = cudaFuncSetAttribute(bgrid_lbm_staged_kernel<Q, S>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                       int(cudaSharedmemCarveoutMaxShared));
+        err = cudaFuncSetAttribute(bgrid_lbm_staged_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(staged_smem<S>()));
     });
     if (err != cudaSuccess) {
         set_error("bGrid LBM kernel set-up failed: %s", cudaGetErrorString(err));
         return NGB_ERR_CUDA;
     }
-    bgrid_lbm_staged_kernel<Q, S><<<d->n_blocks, kBlockVoxels, staged_smem<Q, S>(), s>>>(static_cast<const S*>(fin),
-                                                                                         static_cast<S*>(fout), flags, p);
+    bgrid_lbm_staged_kernel<S><<<d->n_blocks, kStagedThreads, staged_smem<S>(), s>>>(static_cast<const S*>(fin),
+                                                                                    static_cast<S*>(fout), flags, p);
     NGB_LAUNCH_CHECK("bgrid_lbm_staged_kernel");
     return NGB_OK;
 }
@@ -508,8 +571,8 @@ int launch_bgrid_lbm(const ngb_bgrid_desc* d, const void* fin, void* fout, const
     // D3Q19 with 16-bit storage: the shared-memory staged kernel (measured
     // faster there); FP32 storage and D3Q27: per-direction pull (the staged
     // form measured slower for them)
-    if (q19 && d->storage == NGB_STORE_F16OFF) return launch_staged<19, __half>(d, fin, fout, flags, p, s);
-    if (q19 && d->storage == NGB_STORE_BF16OFF) return launch_staged<19, __nv_bfloat16>(d, fin, fout, flags, p, s);
+    if (q19 && d->storage == NGB_STORE_F16OFF) return launch_staged<__half>(d, fin, fout, flags, p, s);
+    if (q19 && d->storage == NGB_STORE_BF16OFF) return launch_staged<__nv_bfloat16>(d, fin, fout, flags, p, s);
 #define NGB_B(QQ, T) \
     bgrid_lbm_kernel<QQ, T, false><<<d->n_blocks, kBlockVoxels, 0, s>>>(static_cast<const T*>(fin), static_cast<T*>(fout), flags, p)
     switch (d->storage) {
