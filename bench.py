@@ -48,9 +48,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--extra", action="store_true", help="also time the other storage/lattice forms")
     ap.add_argument("--profiles", default="", help="cavity: write the centre-line velocity profiles into this directory")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson", "learned", "accuracy"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson", "learned", "unet", "accuracy"],
                     help="cavity: dense LBM (default, the headline); sphere: bGrid flow over a sphere; "
                          "poisson: Jacobi-PCG to 1e-8; learned: U-Net-preconditioned FCG vs Jacobi-PCG to 1e-8; "
+                         "unet: forward applications of the preconditioner network at --n; "
                          "accuracy: cavity velocity error of every storage form against FP64 after --sim-steps")
     ap.add_argument("--train-n", type=int, default=128, help="learned: training grid size")
     ap.add_argument("--train-pairs", type=int, default=2000, help="learned: solver-generated training pairs")
@@ -511,6 +512,60 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def bf16_peak():
+    """Dense BF16 tensor peak (TFLOP/s, burst) measured on this machine, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def run_unet(args):
+    """Forward applications of the learned preconditioner's network (3-level
+    U-Net, 16/32/64 channels, BF16 operands on the tcgen05 tensor cores, FP32
+    accumulate) at --n^3 with seeded weights and a seeded input; a step is one
+    application (10 convolutions, 2 pools, 2 upsamplings). `value` is TFLOP/s
+    of the whole application; the roofline is the measured BF16 dense peak."""
+    import torch
+    import neon_gb300 as ngb
+    from neon_gb300.learned import UNet
+    dev = torch.device("cuda", 0)
+    ngb.lib()
+    n = args.n
+    net = UNet(seed=0, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(2024)
+    r = torch.randn(n ** 3, device=dev, generator=g)
+    s = torch.cuda.current_stream(dev)
+    for _ in range(max(3, args.warmup)):
+        net.forward(r)
+    torch.cuda.synchronize()
+    clk = ClockSampler(torch.cuda.current_device())
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        net.forward(r)
+    e1.record(s)
+    e1.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = net.flops_forward(n)
+    tflops = flops / (ms * 1e-3) / 1e12
+    peak, kind = bf16_peak()
+    line = {"metric": "U-Net preconditioner forward TFLOP/s", "value": round(tflops, 1), "unit": "TFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "none", "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded weights and input)",
+            "config": {"workload": "U-Net 16/32/64, 3x3x3 convolutions, %d^3, one forward application per step" % n,
+                       "flop_per_step": flops, "inputs_vs_l2": "activations of %.1f GB per application, larger than L2" % (
+                           n ** 3 * 2 * (16 + 16 + 48 + 16) / 1e9)},
+            "roofline": {"bound": "tensor", "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(tflops / peak, 4), "peak_kind": kind, "traffic": None},
+            "clocks": clocks, "gpu_launches": 14 * args.steps}
+    print(json.dumps(line), flush=True)
+
+
 def run_accuracy(args):
     """Lid-driven cavity at --n for --sim-steps steps (default 2000) in every
     storage form of the lattice: MLUPS of each run and the relative L2 error of
@@ -594,6 +649,8 @@ def main():
         run_poisson(args)
     elif args.workload == "learned":
         run_learned(args)
+    elif args.workload == "unet":
+        run_unet(args)
     elif args.workload == "accuracy":
         run_accuracy(args)
     else:
