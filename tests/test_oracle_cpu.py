@@ -90,3 +90,12 @@ def test_cavity_profiles_format(tmp_path):
     assert py.endswith("NeonUniformLBM_00042_Y.dat") and px.endswith("NeonUniformLBM_00042_X.dat")
     lines = open(py).read().splitlines()
     assert len(lines) == ny and lines[1] == "%g %g" % (yp[1][0], yp[1][1])
+
+
+def test_cpu_baselines_quick():
+    """The CPU-baseline report runs (tiny sizes) and its numbers are sane."""
+    from oracle import cpu_baselines
+    out = cpu_baselines.main(quick=True)
+    assert all(r["mlups"] > 0 for r in out["lbm_d3q19_f32_cavity"])
+    assert all(r["mlups_active"] > 0 and r["active_cells"] > 0 for r in out["lbm_d3q19_f32_sphere"])
+    assert all(r["converged"] for r in out["poisson_jacobi_pcg_f32"])
