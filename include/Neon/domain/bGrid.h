@@ -299,8 +299,11 @@ class bGrid {
     {
         return "[bGrid] " + mBlocks->dim.to_string() + " blocks " + std::to_string(mBlocks->nBlocks);
     }
-    auto getSpan(Execution = Execution::device, int = 0, DataView = DataView::STANDARD) const -> bSpan
+    // One partition: STANDARD and INTERNAL hold every active block, BOUNDARY none
+    // (a single partition's blocks are all internal, bGrid_imp.h:57).
+    auto getSpan(Execution = Execution::device, int = 0, DataView dv = DataView::STANDARD) const -> bSpan
     {
+        if (dv == DataView::BOUNDARY) return bSpan{0, mBlocks->dMask};
         return bSpan{mBlocks->nBlocks, mBlocks->dMask};
     }
 
@@ -324,14 +327,17 @@ class bGrid {
             auto        f = lambda(L);
             set::Launch l;
             l.signature = set::bytes_of(f);
+            l.stencil = L.isStencil();
+            // one partition: every block is internal, the BOUNDARY view is empty
             if constexpr (execution == Execution::device) {
-                l.run = [span, f](cudaStream_t s) {
-                    if (span.nBlocks == 0) return;
+                l.runView = [span, f](cudaStream_t s, DataView dv) {
+                    if (span.nBlocks == 0 || dv == DataView::BOUNDARY) return;
                     bgrid_container_kernel<<<span.nBlocks, dim3(8, 8, 8), 0, s>>>(span, f);
                     NEON_CUDA_CHECK(cudaGetLastError());
                 };
             } else {
-                l.run = [blocks, f](cudaStream_t s) mutable {
+                l.runView = [blocks, f](cudaStream_t s, DataView dv) mutable {
+                    if (dv == DataView::BOUNDARY) return;
                     NEON_CUDA_CHECK(cudaStreamSynchronize(s));
                     const bSpan hs{blocks->nBlocks, blocks->hMask.data()};
                     bIndex      idx;
@@ -340,6 +346,7 @@ class bGrid {
                             if (hs.setAndValidate(idx, b, v & 7, (v >> 3) & 7, v >> 6)) f(idx);
                 };
             }
+            l.run = [rv = l.runView](cudaStream_t s) { rv(s, DataView::STANDARD); };
             return l;
         });
     }

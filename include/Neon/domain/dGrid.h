@@ -7,6 +7,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdlib>
+
 #include "Neon/core/core.h"
 #include "Neon/domain/Stencil.h"
 #include "Neon/domain/interface.h"
@@ -27,14 +30,50 @@ struct dIndex {
     NEON_CUDA_HOST_DEVICE auto getLocation() const -> const int32_3d& { return mLocation; }
 };
 
+// Cells of one data view (dSpan_imp.h:6-43, span table of dGrid_imp.h:79-128,
+// one partition: no halo). `dim` is the view's extent; thread z maps to grid z
+// by zOffset (INTERNAL: z + r over nz - 2r planes) or, for BOUNDARY, the lower
+// r planes stay and the upper r go to nz - r .. nz - 1 (r = the stencil's z
+// radius). The reference maps the upper boundary planes from the view's own
+// extent (z + r - 1), which for one partition would revisit internal planes;
+// here they are the grid's top r planes, so INTERNAL and BOUNDARY together
+// cover every cell once.
 struct dSpan {
-    int32_3d dim;
+    int32_3d dim;            // extent of the view
+    int      zOffset = 0;    // INTERNAL: r
+    int      zUpper = 0;     // BOUNDARY: first thread z of the upper slab (r), 0 otherwise
+    int      zUpperShift = 0;  // BOUNDARY: nz - 2r
     NEON_CUDA_HOST_DEVICE bool setAndValidate(dIndex& idx, int x, int y, int z) const
     {
-        idx = dIndex(x, y, z);
-        return x < dim.x && y < dim.y && z < dim.z;
+        const bool ok = x < dim.x && y < dim.y && z < dim.z;
+        const int  gz = z + zOffset + ((zUpper > 0 && z >= zUpper) ? zUpperShift : 0);
+        idx = dIndex(x, y, gz);
+        return ok;
     }
 };
+
+// The span of data view `dv` of an nx x ny x nz partition whose stencil reaches
+// r planes in z.
+inline dSpan make_dspan(const int32_3d& d, int r, DataView dv)
+{
+    dSpan s;
+    s.dim = d;
+    if (dv == DataView::STANDARD || r <= 0) {
+        if (dv == DataView::BOUNDARY) s.dim.z = 0;  // no stencil reach: nothing on the boundary
+        return s;
+    }
+    const int rr = r < d.z ? r : d.z;
+    if (dv == DataView::INTERNAL) {
+        s.dim.z = d.z - 2 * rr > 0 ? d.z - 2 * rr : 0;
+        s.zOffset = rr;
+    } else {  // BOUNDARY: the lower and upper slabs (all of z when they meet)
+        if (2 * rr >= d.z) return s;
+        s.dim.z = 2 * rr;
+        s.zUpper = rr;
+        s.zUpperShift = d.z - 2 * rr;
+    }
+    return s;
+}
 
 template <typename T, int C = 0>
 struct dPartition {
@@ -226,7 +265,17 @@ class dGrid {
     auto getBackend() const -> const Backend& { return mData->bk; }
     auto getStencil() const -> const Stencil& { return mData->stencil; }
     auto getImplementationName() const -> std::string { return "dGrid"; }
-    auto getSpan(Execution = Execution::device, int = 0, DataView = DataView::STANDARD) const -> dSpan { return dSpan{mData->dim}; }
+    auto getSpan(Execution = Execution::device, int = 0, DataView dv = DataView::STANDARD) const -> dSpan
+    {
+        return make_dspan(mData->dim, zRadius(), dv);
+    }
+    // Planes a stencil of this grid reaches in z (the halo radius of dGrid_imp.h:65-70).
+    auto zRadius() const -> int
+    {
+        int r = 0;
+        for (const auto& p : mData->stencil.neighbours()) r = std::max(r, std::abs(p.z));
+        return r;
+    }
     auto toString() const -> std::string { return "[dGrid] " + mData->dim.to_string(); }
 
     template <typename T, int C = 0>
@@ -242,21 +291,26 @@ class dGrid {
     template <Execution execution = Execution::device, typename LoadingLambda = void*>
     auto newContainer(const std::string& name, LoadingLambda lambda) const -> set::Container
     {
-        const dSpan   span{mData->dim};
-        const Backend bk = mData->bk;
-        return set::Container(name, bk, [span, lambda]() -> set::Launch {
+        const int32_3d dim = mData->dim;
+        const int      r = zRadius();
+        const Backend  bk = mData->bk;
+        return set::Container(name, bk, [dim, r, lambda]() -> set::Launch {
             set::Loader L(execution);
             auto        f = lambda(L);
             set::Launch l;
             l.signature = set::bytes_of(f);
+            l.stencil = L.isStencil();
             if constexpr (execution == Execution::device) {
-                l.run = [span, f](cudaStream_t s) {
+                l.runView = [dim, r, f](cudaStream_t s, DataView dv) {
+                    const dSpan span = make_dspan(dim, r, dv);
+                    if (span.dim.x <= 0 || span.dim.y <= 0 || span.dim.z <= 0) return;
                     const dim3 grid((span.dim.x + 255) / 256, span.dim.y, span.dim.z);
                     dgrid_container_kernel<<<grid, 256, 0, s>>>(span, f);
                     NEON_CUDA_CHECK(cudaGetLastError());
                 };
             } else {
-                l.run = [span, f](cudaStream_t s) mutable {
+                l.runView = [dim, r, f](cudaStream_t s, DataView dv) mutable {
+                    const dSpan span = make_dspan(dim, r, dv);
                     NEON_CUDA_CHECK(cudaStreamSynchronize(s));
                     dIndex idx;
                     for (int z = 0; z < span.dim.z; z++)
@@ -265,6 +319,7 @@ class dGrid {
                                 if (span.setAndValidate(idx, x, y, z)) f(idx);
                 };
             }
+            l.run = [rv = l.runView](cudaStream_t s) { rv(s, DataView::STANDARD); };
             return l;
         });
     }

@@ -8,6 +8,14 @@
 // grid's span. `prepare()` separates the two halves so that a Skeleton can
 // capture launches into a CUDA graph and detect when the compute lambda's
 // captured state changed (then it re-captures).
+//
+// Data views (one partition): a grid container runs over the STANDARD span
+// (every cell), the INTERNAL span or the BOUNDARY span (dGrid: the z slabs of
+// the stencil's radius at both ends; bGrid: empty, every block of a single
+// partition is internal). A container made by the library around one ABI
+// call (the LBM step, the Laplacian, ...) covers the whole grid when asked
+// for INTERNAL and does nothing for BOUNDARY, so INTERNAL then BOUNDARY still
+// visits every cell once.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -41,14 +49,17 @@ class Loader {
 
     // Const field: any pattern.
     template <typename Field_ta>
-    auto load(Field_ta& field, Pattern = Pattern::MAP, StencilSemantic = StencilSemantic::standard)
+    auto load(Field_ta& field, Pattern pattern = Pattern::MAP, StencilSemantic = StencilSemantic::standard)
         -> std::enable_if_t<std::is_const_v<Field_ta>, const typename Field_ta::Partition&>
     {
+        if (pattern == Pattern::STENCIL) mStencil = true;
         mPartitions.emplace_back(std::make_shared<Holder<typename Field_ta::Partition>>(field.getPartition(mExecution)));
         return static_cast<Holder<typename Field_ta::Partition>*>(mPartitions.back().get())->p;
     }
 
     auto getExecution() const -> Execution { return mExecution; }
+    // A field was loaded with the STENCIL pattern (the container reads neighbours).
+    auto isStencil() const -> bool { return mStencil; }
 
    private:
     struct HolderBase {
@@ -60,13 +71,26 @@ class Loader {
         P p;
     };
     Execution                                mExecution;
+    bool                                     mStencil = false;
     std::vector<std::shared_ptr<HolderBase>> mPartitions;
 };
 
-// One prepared launch: the kernel launch itself and the bytes of its parameters.
+// One prepared launch: the kernel launch over the whole grid, optionally the
+// launch over one data view, whether the container is a stencil, and the bytes
+// of its parameters.
 struct Launch {
-    std::function<void(cudaStream_t)> run;
-    std::vector<char>                 signature;
+    std::function<void(cudaStream_t)>           run;
+    std::function<void(cudaStream_t, DataView)> runView;
+    bool                                        stencil = false;
+    std::vector<char>                           signature;
+
+    void launch(cudaStream_t s, DataView dv) const
+    {
+        if (runView)
+            runView(s, dv);
+        else if (dv != DataView::BOUNDARY)
+            run(s);
+    }
 };
 
 class Container {
@@ -80,12 +104,12 @@ class Container {
     auto prepare() const -> Launch { return mPrepare(); }
     auto getBackend() const -> const Backend& { return mBackend; }
 
-    // Launch on the backend's stream `streamIdx` (asynchronous).
-    void run(int streamIdx = Backend::mainStreamIdx, DataView = DataView::STANDARD) const
+    // Launch over data view `dv` on the backend's stream `streamIdx` (asynchronous).
+    void run(int streamIdx = Backend::mainStreamIdx, DataView dv = DataView::STANDARD) const
     {
         if (!mPrepare) return;
-        Launch l = mPrepare();
-        l.run(mBackend.stream(streamIdx));
+        const Launch l = mPrepare();
+        l.launch(mBackend.stream(streamIdx), dv);
     }
 
    private:

@@ -9,6 +9,13 @@
 // value changed, another field was loaded), the sequence is captured again and
 // the executable graph updated. The graph .dot dump of Skeleton.h:43 is
 // written only when the environment variable NEON_GB300_DOT is set.
+//
+// OCC (MultiXpuGraph::optimizations, multiGpuGraph.cpp:106-200): with any
+// option other than Occ::none, a stencil container runs as its INTERNAL launch
+// followed by its BOUNDARY launch (the split of optimizeStandardOCC). With one
+// partition there is no halo transfer between the two, and the extended forms
+// (which also split the map containers feeding a stencil) give the same
+// launches as the standard one.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -112,7 +119,14 @@ class Skeleton {
         cudaGraph_t g = nullptr;
         NEON_CUDA_CHECK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         try {
-            for (auto& l : launches) l.run(cs);
+            for (auto& l : launches) {
+                if (mOptions.occ() != Occ::none && l.stencil && l.runView) {
+                    l.runView(cs, DataView::INTERNAL);
+                    l.runView(cs, DataView::BOUNDARY);
+                } else {
+                    l.launch(cs, DataView::STANDARD);
+                }
+            }
         } catch (...) {
             cudaStreamEndCapture(cs, &g);
             if (g) cudaGraphDestroy(g);

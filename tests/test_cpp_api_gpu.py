@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "tests", "cpp")
 BUILD = os.path.join(CPP, "_build")
-PROGRAMS = ["api_stencil", "api_lbm", "api_poisson"]
+PROGRAMS = ["api_stencil", "api_lbm", "api_poisson", "api_dataview"]
 
 
 def _compile(name):
@@ -103,3 +103,11 @@ def test_poisson_cg_t(programs, orc, tmp_path):
     assert abs(its - res[0]) <= 2, (its, res[0])
     # the program returns x rounded to float (the field type)
     assert np.linalg.norm(xg - xo) / np.linalg.norm(xo) <= 1e-6
+
+
+def test_data_views_and_occ(programs):
+    """DataView INTERNAL / BOUNDARY spans of one partition (dGrid: the
+    stencil's z planes at both ends are BOUNDARY; bGrid: every block is
+    internal) and a Skeleton with Occ::standard give the STANDARD result."""
+    out = _run(programs["api_dataview"])
+    assert out.count("ok=1") == 6 and "ok=0" not in out, out
