@@ -2,3 +2,4 @@
 #pragma once
 #include "Neon/domain/bGrid.h"
 #include "Neon/domain/dGrid.h"
+#include "Neon/domain/eGrid.h"

@@ -131,6 +131,32 @@ int ngb_lbm_dense_macroscopic(const ngb_lbm_dense_desc* desc, const void* fin, c
  * Block-sparse grid (bGrid, 8x8x8 blocks), single partition
  * ---------------------------------------------------------------------- */
 
+/* ------------------------------------------------------------------------
+ * Element-sparse grid (eGrid), single partition
+ * ---------------------------------------------------------------------- */
+
+/* int32 scratch entries ngb_egrid_count needs. */
+#define NGB_EGRID_SCRATCH(nx, ny, nz) ((((int64_t)(nx) * (ny) * (nz)) + 2047) / 2048 + 1)
+
+/* Phase 1 of the eGrid construction on the device (eGrid_imp.h:8-129, which
+ * runs Partitioner1D at block size 1; one partition: every active cell is an
+ * internal element, in the order z, then y, then x fastest,
+ * SpanClassifier.h:228-237). `active` is a dense nx*ny*nz byte map (x
+ * fastest, non-zero = active). elem_of[nx*ny*nz] receives each cell's element
+ * index or -1, *count (device) the number of elements; `scratch` holds
+ * NGB_EGRID_SCRATCH(nx, ny, nz) int32. Fewer than 2^31 cells. */
+int ngb_egrid_count(int32_t nx, int32_t ny, int32_t nz, const uint8_t* active, int32_t* elem_of, int32_t* scratch, int32_t* count,
+                    void* stream);
+
+/* Phase 2: origin[3*count] = (x, y, z) of every element (the global mapping of
+ * Partitioner1D.h:212-255) and, for the `npts` stencil offsets in `points`
+ * (host, 3 int8 per point, in the stencil's neighbour order, at most 64),
+ * conn[s*count + e] = the element at origin[e] + points[s], or -1 outside the
+ * grid or on an inactive cell (Partitioner1D.h:338-380; read by
+ * ePartition_imp.h isValidNgh). */
+int ngb_egrid_fill(int32_t nx, int32_t ny, int32_t nz, const int32_t* elem_of, int32_t count, const int8_t* points, int32_t npts,
+                   int32_t* origin, int32_t* conn, void* stream);
+
 /* Candidate blocks per axis: ceil(n / 8). */
 #define NGB_BGRID_BLOCKS(n) (((n) + 7) / 8)
 #define NGB_BGRID_NO_BLOCK 0xffffffffu

@@ -86,6 +86,8 @@ _bd = ctypes.POINTER(BGridDesc)
 # Signatures of the entry points beyond the dense LBM ones: name -> (argtypes, restype).
 _EXTRA_SIGNATURES = {
     "ngb_bgrid_count": ([_i32, _i32, _i32, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_egrid_count": ([_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_egrid_fill": ([_i32, _i32, _i32, _vp, _i32, _vp, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_bgrid_fill": ([_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "ngb_bgrid_wall_mask": ([_bd, _vp, _vp], ctypes.c_int),
     "ngb_bgrid_lbm_step": ([_bd, _vp, _vp, _vp, _vp], ctypes.c_int),
@@ -313,6 +315,35 @@ def bgrid_lbm_step(desc, fin, fout, flags, stream=None):
 def bgrid_drag(desc, fin, flags, partials, force, stream=None):
     return check(lib().ngb_bgrid_drag(ctypes.byref(desc), _ptr(fin), _ptr(flags), _ptr(partials), _ptr(force),
                                       _stream(stream)))
+
+
+# ----------------------------------------------------------------------------- eGrid
+class EGrid:
+    """An element-sparse grid of one partition built on the device from a dense
+    byte activity map (torch uint8 tensor on cuda, nx*ny*nz, x fastest) and a
+    list of stencil offsets (Neon::eGrid's construction, eGrid_imp.h:8-129):
+    `count` elements in z, y, x order, `origin` (3 x int32 per element) and
+    `conn` (int32, conn[s*count + e] = neighbour element along points[s] or -1)."""
+
+    def __init__(self, nx, ny, nz, active, points, stream=None):
+        import numpy as np
+        import torch
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.points = [tuple(int(v) for v in p) for p in points]
+        dev = active.device
+        V = nx * ny * nz
+        self.elem_of = torch.empty(V, dtype=torch.int32, device=dev)
+        scratch = torch.empty((V + 2047) // 2048 + 1, dtype=torch.int32, device=dev)
+        cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+        check(lib().ngb_egrid_count(nx, ny, nz, _ptr(active), _ptr(self.elem_of), _ptr(scratch), _ptr(cnt), _stream(stream)))
+        self.count = int(cnt.item())
+        n = max(self.count, 1)
+        self.origin = torch.empty(3 * n, dtype=torch.int32, device=dev)
+        self.conn = torch.empty(max(len(self.points), 1) * n, dtype=torch.int32, device=dev)
+        pts = np.array(self.points, dtype=np.int8).reshape(-1)
+        check(lib().ngb_egrid_fill(nx, ny, nz, _ptr(self.elem_of), self.count,
+                                   pts.ctypes.data_as(ctypes.c_void_p) if len(self.points) else None, len(self.points),
+                                   _ptr(self.origin), _ptr(self.conn), _stream(stream)))
 
 
 def bgrid_flags_from_dense(desc, nx, ny, nz, cls, flags, stream=None):

@@ -68,6 +68,8 @@ def lib():
                                       c_double, c_double, c_uint64, c_void_p, c_void_p]
         L.orc_flags_from_classes.argtypes = [c_int, c_int, c_int, c_int, c_void_p, c_void_p]
         L.orc_box_boundary.argtypes = [c_int, c_int, c_int, c_void_p]
+        L.orc_egrid_build.argtypes = [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+        L.orc_egrid_build.restype = c_int64
         L.orc_gaussian_sources.argtypes = [c_int, c_int, c_int, c_uint64, c_void_p, c_void_p]
         L.orc_laplacian_f64.argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]
         L.orc_laplacian_f32.argtypes = [c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]

@@ -356,6 +356,48 @@ int orc_flags_from_classes(int nx, int ny, int nz, int Q, const uint8_t* cls, ui
     return 0;
 }
 
+// ------------------------------------------------------------------ eGrid
+// eGrid of one partition (eGrid_imp.h:8-129 -> Partitioner1D at block size 1):
+// elements are the active cells in z, y, x order (SpanClassifier.h:228-237);
+// origin = the cell (Partitioner1D.h:212-255); conn[s * count + e] = element at
+// origin + points[s] or -1 (Partitioner1D.h:338-380, ePartition_imp.h isValidNgh).
+// Returns the element count; origin / conn are written when non-null.
+int64_t orc_egrid_build(int nx, int ny, int nz, const uint8_t* active, const int8_t* points, int npts, int32_t* origin, int32_t* conn)
+{
+    const size_t         V = size_t(nx) * ny * nz;
+    std::vector<int32_t> elem(V, -1);
+    int64_t              count = 0;
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const size_t i = lin(x, y, z, nx, ny);
+                if (!active[i]) continue;
+                elem[i] = int32_t(count);
+                if (origin) {
+                    origin[3 * count] = x;
+                    origin[3 * count + 1] = y;
+                    origin[3 * count + 2] = z;
+                }
+                count++;
+            }
+    if (conn) {
+        int64_t e = 0;
+        for (int z = 0; z < nz; z++)
+            for (int y = 0; y < ny; y++)
+                for (int x = 0; x < nx; x++) {
+                    if (!active[lin(x, y, z, nx, ny)]) continue;
+                    for (int s = 0; s < npts; s++) {
+                        const int xx = x + points[3 * s], yy = y + points[3 * s + 1], zz = z + points[3 * s + 2];
+                        int32_t   v = -1;
+                        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < nx && yy < ny && zz < nz) v = elem[lin(xx, yy, zz, nx, ny)];
+                        conn[int64_t(s) * count + e] = v;
+                    }
+                    e++;
+                }
+    }
+    return count;
+}
+
 // ------------------------------------------------------------------ Poisson
 void orc_box_boundary(int nx, int ny, int nz, int8_t* bd) { box_boundary(nx, ny, nz, bd); }
 

@@ -6,7 +6,8 @@
 //       the two boundary planes untouched),
 //   (3) then over DataView::BOUNDARY (every cell now equals (1)),
 //   (4) in a Skeleton with Occ::standard (equal to (1)),
-// and, for bGrid, INTERNAL equal to STANDARD with BOUNDARY writing nothing.
+// and, for bGrid and eGrid, INTERNAL equal to STANDARD with BOUNDARY writing
+// nothing (one partition: every block / element is internal).
 // Prints one "dataview <grid> <dims> ok=<0|1>" line per case; exits 1 on any
 // mismatch.
 #include <cstdio>
@@ -96,7 +97,8 @@ bool check(Neon::index_3d dim, bool dense_grid)
     const auto si = grid.getSpan(Neon::Execution::device, 0, Neon::DataView::INTERNAL);
     const auto sb = grid.getSpan(Neon::Execution::device, 0, Neon::DataView::BOUNDARY);
     if constexpr (std::is_same_v<Grid, Neon::dGrid>) ok = ok && si.dim.z + sb.dim.z == s.dim.z;
-    else ok = ok && si.nBlocks == s.nBlocks && sb.nBlocks == 0;
+    else if constexpr (std::is_same_v<Grid, Neon::bGrid>) ok = ok && si.nBlocks == s.nBlocks && sb.nBlocks == 0;
+    else ok = ok && si.count == s.count && sb.count == 0;
 
     std::printf("dataview %s %dx%dx%d ok=%d\n", grid.getImplementationName().c_str(), dim.x, dim.y, dim.z, ok ? 1 : 0);
     return ok;
@@ -109,5 +111,6 @@ int main()
     for (auto d : {Neon::index_3d(10, 17, 13), Neon::index_3d(17, 1, 77), Neon::index_3d(5, 6, 2), Neon::index_3d(4, 4, 1)})
         ok = check<Neon::dGrid>(d, true) && ok;
     for (auto d : {Neon::index_3d(10, 17, 24), Neon::index_3d(17, 1, 77)}) ok = check<Neon::bGrid>(d, false) && ok;
+    for (auto d : {Neon::index_3d(10, 17, 13), Neon::index_3d(3, 1, 40)}) ok = check<Neon::eGrid>(d, false) && ok;
     return ok ? 0 : 1;
 }

@@ -95,6 +95,28 @@ void run(const std::string& outdir, Neon::index_3d dim, int iters)
     std::printf("%s %dx%dx%d ok stencil-throw=%d\n", grid.getImplementationName().c_str(), dim.x, dim.y, dim.z, int(threw));
 }
 
+// eGrid on a sparse domain (cells with (x + y + z) % 3 != 0 active): inactive
+// cells are not neighbours. Writes <grid>_<dims>_sparse_Y.bin (dense, 0 off the domain).
+void run_sparse_egrid(const std::string& outdir, Neon::index_3d dim)
+{
+    Neon::Backend bk(std::vector<int>{0}, Neon::Runtime::stream);
+    Neon::eGrid   grid(bk, dim, [](const Neon::index_3d& p) { return (p.x + p.y + p.z) % 3 != 0; },
+                       Neon::domain::Stencil::s7_Laplace_t());
+    auto          X = grid.newField<int64_t, 0>("X", 1, 0);
+    auto          Y = grid.newField<int64_t, 0>("Y", 1, 0);
+    X.forEachActiveCell([&](const Neon::index_3d& p, int, int64_t& v) {
+        v = int64_t(p.z) + 1000LL * p.y + 1000000LL * p.x + 10000000000LL;
+    });
+    X.updateDeviceData(0);
+    laplace(X, Y).run(0);
+    Y.updateHostData(0);
+    bk.sync(0);
+    dump<Neon::eGrid>(outdir + "/eGrid_" + std::to_string(dim.x) + "x" + std::to_string(dim.y) + "x" + std::to_string(dim.z) +
+                          "_sparse_Y.bin",
+                      Y, dim);
+    std::printf("eGrid sparse %dx%dx%d elements=%lld\n", dim.x, dim.y, dim.z, (long long)grid.getNumActiveCells());
+}
+
 int main(int argc, char** argv)
 {
     const std::string outdir = argc > 1 ? argv[1] : ".";
@@ -102,9 +124,11 @@ int main(int argc, char** argv)
     // runHelper.h:36 dimensions; bGrid pads z to 24 for its tests (runHelper.h:77-81)
     for (auto d : {Neon::index_3d(10, 17, 13), Neon::index_3d(1, 1, 100), Neon::index_3d(17, 1, 77)}) {
         run<Neon::dGrid>(outdir, d, iters);
+        run<Neon::eGrid>(outdir, d, iters);
         Neon::index_3d db = d;
         if (db.z < 24) db.z = 24;
         run<Neon::bGrid>(outdir, db, iters);
     }
+    run_sparse_egrid(outdir, Neon::index_3d(19, 11, 23));
     return 0;
 }

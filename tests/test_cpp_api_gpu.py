@@ -49,8 +49,8 @@ def _run(exe, *args):
 
 def test_domain_and_skeleton_stencil(programs, orc, tmp_path):
     out = _run(programs["api_stencil"], tmp_path)
-    assert out.count("stencil-throw=1") == 6, out
-    for grid, dims in [("dGrid", d) for d in [(10, 17, 13), (1, 1, 100), (17, 1, 77)]] + \
+    assert out.count("stencil-throw=1") == 9, out
+    for grid, dims in [(g, d) for d in [(10, 17, 13), (1, 1, 100), (17, 1, 77)] for g in ("dGrid", "eGrid")] + \
                       [("bGrid", d) for d in [(10, 17, 24), (1, 1, 100), (17, 1, 77)]]:
         nx, ny, nz = dims
         V = nx * ny * nz
@@ -67,6 +67,23 @@ def test_domain_and_skeleton_stencil(programs, orc, tmp_path):
             orc.orc_laplace_i64(nx, ny, nz, None, P(xs), P(y))
             orc.orc_laplace_i64(nx, ny, nz, None, P(y), P(xs))
         assert np.array_equal(np.fromfile(str(tag) + "_skel_X.bin", np.int64), xs)
+
+
+def test_egrid_sparse_stencil(programs, orc, tmp_path):
+    """eGrid on a sparse domain through newContainer: inactive cells are not
+    neighbours (the oracle's TestData::laplace with the same activity map)."""
+    out = _run(programs["api_stencil"], tmp_path)
+    nx, ny, nz = 19, 11, 23
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    act = ((x + y + z) % 3 != 0).astype(np.uint8).ravel()
+    assert "eGrid sparse 19x11x23 elements=%d" % int(act.sum()) in out, out
+    x0 = np.zeros(nx * ny * nz, np.int64)
+    orc.orc_masked_values_i64(nx, ny, nz, 1, 3, P(x0))
+    y0 = np.zeros_like(x0)
+    orc.orc_laplace_i64(nx, ny, nz, P(act), P(x0), P(y0))
+    got = np.fromfile(str(tmp_path / "eGrid_19x11x23_sparse_Y.bin"), np.int64)
+    m = act.astype(bool)
+    assert np.array_equal(got[m], y0[m])
 
 
 def test_lbm_cavity_user_and_gb300_containers(programs, orc, tmp_path):
@@ -110,4 +127,4 @@ def test_data_views_and_occ(programs):
     stencil's z planes at both ends are BOUNDARY; bGrid: every block is
     internal) and a Skeleton with Occ::standard give the STANDARD result."""
     out = _run(programs["api_dataview"])
-    assert out.count("ok=1") == 6 and "ok=0" not in out, out
+    assert out.count("ok=1") == 8 and "ok=0" not in out, out
