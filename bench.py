@@ -19,6 +19,7 @@ here) on all host threads, on bounded z-slab samples of the same lattice.
 import argparse
 import ctypes
 import json
+import math
 import os
 import re
 import subprocess
@@ -41,7 +42,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=384)
+    ap.add_argument("--n", type=int, default=0, help="grid size (default: 384 for the LBM workloads, 512 for poisson/learned, 256 for unet)")
     ap.add_argument("--lattice", default="d3q19", choices=["d3q19", "d3q27"])
     ap.add_argument("--storage", default="f32", choices=["f64", "f32", "f16off", "bf16off"])
     ap.add_argument("--no-e2e", action="store_true")
@@ -53,14 +54,19 @@ def parse():
                          "poisson: Jacobi-PCG to 1e-8; learned: U-Net-preconditioned FCG vs Jacobi-PCG to 1e-8; "
                          "unet: forward applications of the preconditioner network at --n; "
                          "accuracy: cavity velocity error of every storage form against FP64 after --sim-steps")
-    ap.add_argument("--train-n", type=int, default=128, help="learned: training grid size")
+    ap.add_argument("--train-n", type=int, default=64,
+                    help="learned: training grid size = the coarsest level of the V-cycle")
+    ap.add_argument("--lr", type=float, default=3e-4, help="learned: Adam learning rate")
     ap.add_argument("--train-pairs", type=int, default=2000, help="learned: solver-generated training pairs")
     ap.add_argument("--epochs", type=int, default=2, help="learned: training epochs")
     ap.add_argument("--weights", default="", help="learned: load U-Net weights from this file instead of training")
     ap.add_argument("--save-weights", default="", help="learned: save the trained weights here")
     ap.add_argument("--scale", type=int, default=1, help="sphere case size divisor")
     ap.add_argument("--sim-steps", type=int, default=0, help="sphere: steps of the drag comparison run")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.n <= 0:
+        args.n = {"poisson": 512, "learned": 512, "unet": 256}.get(args.workload, 384)
+    return args
 
 
 def dist_env():
@@ -446,7 +452,12 @@ def run_learned(args):
     seeded k^-2 Gaussian random fields at --train-n, then used inside flexible
     CG (with Jacobi-PCG fallback on stagnation) on the Gaussian-source Poisson
     problem at --n, against device Jacobi-PCG on the same problem; both to a
-    1e-8 relative true residual. `value` is the FCG solve time (seconds)."""
+    1e-8 relative true residual. For --n > --train-n the network is the
+    coarsest-level solve of a V-cycle (damped-Jacobi smoothing and
+    full-weighting / trilinear transfers on the levels between --n and
+    --train-n); the same cycle without the network is timed beside it. For
+    --n == --train-n the network preconditions the fine grid directly.
+    `value` is the FCG solve time (seconds)."""
     import torch
     import neon_gb300 as ngb
     from neon_gb300 import fcg
@@ -467,7 +478,7 @@ def run_learned(args):
         pairs = fcg.make_training_set(args.train_n, systems, captures, seed=2024, device=dev)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        losses = fcg.train(net, pairs, epochs=args.epochs, lr=1e-3)
+        losses = fcg.train(net, pairs, epochs=args.epochs, lr=args.lr)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         k = max(1, len(losses) // 10)
@@ -485,30 +496,52 @@ def run_learned(args):
     ws = ngb.cg_workspace(d, dev)
     x = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
     pcg = ngb.cg_solve(d, b, x, ws, tol=1e-8, max_iter=20000, refresh_every=50, check_every=50, jacobi=True)
-    # FCG: one warm-up application of the network, then the timed solve
-    net.forward(b)
-    torch.cuda.synchronize()
-    x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
-    res = fcg.fcg_solve(net, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
+    # FCG preconditioned by the V-cycle whose coarsest level (--train-n) is the network
+    levels = max(0, int(round(math.log2(n / args.train_n))))
+    if args.train_n << levels != n:
+        raise SystemExit("learned: --n must be --train-n times a power of two")
+    vc = fcg.VCycle(n, levels, net, device=dev) if levels > 0 else None
+    if vc is not None:
+        vc(b)  # warm-up (network buffers at the coarsest size)
+        torch.cuda.synchronize()
+        x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
+        res = fcg.fcg_solve_vcycle(vc, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
+        # the same cycle without the network (coarsest correction zero)
+        x3 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
+        plain = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, coarse="none", device=dev), b, x3, tol=1e-8, max_iter=4000,
+                                     fallback=True, ws=ws)
+    else:
+        net.forward(b)
+        torch.cuda.synchronize()
+        x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
+        res = fcg.fcg_solve(net, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
+        plain = None
     agree = float((x2 - x).norm() / x.norm())
-    # U-Net forward cost at n (device time)
+    # U-Net forward cost at the size it runs at (device time)
+    nn_ = n >> levels
+    rc = b[:nn_ ** 3].clone()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(3):
-        net.forward(b)
+        net.forward(rc)
     e1.record()
     e1.synchronize()
     fwd_ms = e0.elapsed_time(e1) / 3
+    cfg = {"workload": "Poisson 7-point, zero Dirichlet, %d^3; FCG(1) with a V-cycle of %d damped-Jacobi levels whose "
+                       "coarsest (%d^3) solve is the U-Net 16/32/64 trained at %d^3" % (n, levels, nn_, args.train_n),
+           "fcg_iterations": res["iterations"], "fcg_fallback": res["fallback"],
+           "fallback_iterations": res["fallback_iterations"], "fcg_rel_residual": res["rel_residual"],
+           "converged": res["converged"], "pcg_seconds": round(pcg["seconds"], 4),
+           "pcg_iterations": pcg["iterations"], "speedup_vs_pcg": round(pcg["seconds"] / res["seconds"], 3),
+           "solution_rel_diff": agree, "unet_forward_ms": round(fwd_ms, 3),
+           "unet_forward_tflops": round(net.flops_forward(nn_) / fwd_ms / 1e9, 1), "training": train}
+    if plain is not None:
+        cfg["without_network"] = {"seconds": round(plain["seconds"], 4), "iterations": plain["iterations"],
+                                  "fallback": plain["fallback"], "fallback_iterations": plain["fallback_iterations"],
+                                  "converged": plain["converged"]}
     line = {"metric": "Poisson seconds to 1e-8: learned FCG vs Jacobi-PCG", "value": round(res["seconds"], 4), "unit": "s",
             "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "dtype": "bf16",
-            "data": "synthetic (8 seeded Gaussians, sigma 8; training on seeded k^-2 fields)",
-            "config": {"workload": "Poisson 7-point, zero Dirichlet, %d^3; U-Net 16/32/64 trained at %d^3" % (n, args.train_n),
-                       "fcg_iterations": res["iterations"], "fcg_fallback": res["fallback"],
-                       "fallback_iterations": res["fallback_iterations"], "fcg_rel_residual": res["rel_residual"],
-                       "converged": res["converged"], "pcg_seconds": round(pcg["seconds"], 4),
-                       "pcg_iterations": pcg["iterations"], "speedup_vs_pcg": round(pcg["seconds"] / res["seconds"], 3),
-                       "solution_rel_diff": agree, "unet_forward_ms": round(fwd_ms, 2),
-                       "unet_forward_tflops": round(net.flops_forward(n) / fwd_ms / 1e9, 1), "training": train}}
+            "data": "synthetic (8 seeded Gaussians, sigma 8; training on seeded k^-2 fields)", "config": cfg}
     print(json.dumps(line), flush=True)
 
 

@@ -395,6 +395,33 @@ int ngb_adam(int64_t n, float* p, const float* g, float* m, float* s, float lr, 
 /* wt[ci][26 - t][co] = BF16(w[co][t][ci]): weights of the backward-data convolution. */
 int ngb_flip_weights(int32_t cout, int32_t cin, const float* w, void* wt, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Multilevel learned preconditioner: smoothing and grid transfer between
+ * vertex-centred levels (no reference counterpart; libNeonSolver has CG
+ * only). FP32 fields on the box-face Dirichlet problem (desc->bd == NULL,
+ * desc->field NGB_STORE_F32); A is the operator of ngb_laplacian_apply with
+ * spacing desc->h. Coarse node I sits on fine node 2I: a fine grid of even
+ * dims n has the coarse grid n/2 with spacing 2h. Face nodes of every level
+ * are Fixed and written as 0.
+ * ---------------------------------------------------------------------- */
+
+/* Damped Jacobi on the Free nodes: out = u + omega h^2/6 (r - A u). With u
+ * NULL, out is the result of two sweeps from u = 0 in one stencil pass over
+ * r (2 c r - c^2 A r, c = omega h^2/6; r must be 0 on the face nodes). */
+int ngb_mg_jacobi(const ngb_poisson_desc* desc, const void* u, const void* r, void* out, double omega, void* stream);
+
+/* out = r - A u on the Free nodes (u NULL: u = 0). */
+int ngb_mg_residual(const ngb_poisson_desc* desc, const void* u, const void* r, void* out, void* stream);
+
+/* Full-weighting restriction to the coarse grid (dims/2): rc(I) = scale *
+ * sum_a w_a res(2I + a), w = (1/4, 1/2, 1/4) per axis, on coarse interior
+ * nodes; fine dims even and >= 6. */
+int ngb_mg_restrict(const ngb_poisson_desc* fine, const void* res, void* rc, double scale, void* stream);
+
+/* u += P ec on the fine Free nodes, P the trilinear interpolation from the
+ * coarse grid (dims/2) that ngb_mg_restrict's weights are the transpose of. */
+int ngb_mg_prolong_add(const ngb_poisson_desc* fine, const void* ec, void* u, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

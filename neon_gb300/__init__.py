@@ -135,6 +135,10 @@ _EXTRA_SIGNATURES.update({
     "ngb_adam": ([ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                   _i32, _vp, _vp], ctypes.c_int),
     "ngb_flip_weights": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_mg_jacobi": ([_pd, _vp, _vp, _vp, _dbl, _vp], ctypes.c_int),
+    "ngb_mg_residual": ([_pd, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_mg_restrict": ([_pd, _vp, _vp, _dbl, _vp], ctypes.c_int),
+    "ngb_mg_prolong_add": ([_pd, _vp, _vp, _vp], ctypes.c_int),
     "ngb_conv3d_tc_supported": ([_i32, _i32, _i32, _i32, _i32, _i32, _i32], ctypes.c_int),
     "ngb_conv3d_pack": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_conv3d_tc": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
@@ -396,6 +400,25 @@ def poisson_desc(nx, ny, nz, field="f32", h=1.0, bd=None):
 
 def laplacian_apply(desc, u, out, stream=None):
     return check(lib().ngb_laplacian_apply(ctypes.byref(desc), _ptr(u), _ptr(out), _stream(stream)))
+
+
+def mg_jacobi(desc, u, r, out, omega, stream=None):
+    """out = u + omega h^2/6 (r - A u) on Free nodes; u None: two sweeps from zero."""
+    return check(lib().ngb_mg_jacobi(ctypes.byref(desc), _ptr(u) if u is not None else None, _ptr(r), _ptr(out), omega,
+                                     _stream(stream)))
+
+
+def mg_residual(desc, u, r, out, stream=None):
+    return check(lib().ngb_mg_residual(ctypes.byref(desc), _ptr(u) if u is not None else None, _ptr(r), _ptr(out),
+                                       _stream(stream)))
+
+
+def mg_restrict(fine_desc, res, rc, scale=1.0, stream=None):
+    return check(lib().ngb_mg_restrict(ctypes.byref(fine_desc), _ptr(res), _ptr(rc), scale, _stream(stream)))
+
+
+def mg_prolong_add(fine_desc, ec, u, stream=None):
+    return check(lib().ngb_mg_prolong_add(ctypes.byref(fine_desc), _ptr(ec), _ptr(u), _stream(stream)))
 
 
 def dot(a, b, result, scratch=None, stream=None):

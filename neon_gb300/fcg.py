@@ -20,7 +20,8 @@ import time
 
 import torch
 
-from . import (STORE_F32, STORE_F64, _ptr, cg_solve, cg_workspace, check, dot, laplacian_apply, lib, poisson_desc)
+from . import (STORE_F32, STORE_F64, _ptr, cg_solve, cg_workspace, check, dot, laplacian_apply, lib, mg_jacobi,
+                mg_prolong_add, mg_residual, mg_restrict, poisson_desc)
 
 
 def free_mask(n, device):
@@ -119,7 +120,8 @@ def train(net, pairs, epochs=2, lr=1e-3, log=None, seed=0):
 
 def fcg_solve(net, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=20, fallback=True, ws=None, smooth=2,
               omega=2.0 / 3.0):
-    """FCG(1) with z = M(r). b: float32 n^3 field (zero on the faces); x: float64 n^3 initial guess / result.
+    """FCG(1) with z = M(r) from the network on the fine grid. b: float32 n^3
+    field (zero on the faces); x: float64 n^3 initial guess / result.
 
     The network's output carries white rounding noise from its BF16
     activations at about 1e-3 of |z|; A amplifies it by up to 12 while
@@ -128,12 +130,8 @@ def fcg_solve(net, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=20, fallback
     z += omega D^-1 (r - A z) after the network remove that high-frequency
     error (each sweep scales it by at most 1/3 for omega = 2/3)."""
     n = round(b.numel() ** (1.0 / 3.0))
-    dev = b.device
-    ops = _Ops(n, dev)
-    mask = free_mask(n, dev)
-    t0 = time.perf_counter()
-    bn = ops.dot(b, b) ** 0.5
-    ax = torch.empty_like(x)
+    ops = _Ops(n, b.device)
+    mask = free_mask(n, b.device)
     az = torch.empty_like(b)
 
     def precondition(r):
@@ -144,14 +142,111 @@ def fcg_solve(net, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=20, fallback
             ops.A(z, az)
         return z, az.clone()
 
+    return _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws)
+
+
+class VCycle:
+    """Multilevel preconditioner z = M(r) whose coarsest-level solve is the network.
+
+    Levels l = 0..L are vertex-centred grids of n / 2^l nodes with spacing
+    2^l (ngb_mg_* kernels). On every level above the coarsest: two damped
+    Jacobi sweeps from zero, the residual, full-weighting restriction; on the
+    coarsest level the correction e_L solves A_{2^L} e_L = r_L, which is
+    A_1 e_L = 4^L r_L, the problem the network was trained on (A with unit
+    spacing): e_L = 4^L M(r_L); then trilinear prolongation and `post` Jacobi
+    sweeps back up. The smoothing levels remove the high-frequency error the
+    BF16 network output carries and the network supplies the smooth
+    components Jacobi cannot reach; the network's correction enters with the
+    energy-minimising step on the coarsest level. `coarse="none"` drops the
+    coarsest correction (the same cycle without the network)."""
+
+    def __init__(self, n, levels, net=None, coarse="net", omega=6.0 / 7.0, post=2, device="cuda"):
+        if coarse not in ("net", "none"):
+            raise ValueError("coarse must be 'net' or 'none'")
+        if coarse == "net" and net is None:
+            raise ValueError("coarse='net' needs a network")
+        if n % (1 << levels) != 0 or (n >> levels) < 8:
+            raise ValueError("n must be divisible by 2^levels with at least 8 nodes on the coarsest level")
+        self.n, self.levels, self.net, self.coarse = n, levels, net, coarse
+        self.omega, self.post = omega, post
+        self.descs = [poisson_desc(n >> l, n >> l, n >> l, "f32", float(1 << l)) for l in range(levels + 1)]
+        f32 = dict(dtype=torch.float32, device=device)
+        self.u = [torch.empty((n >> l) ** 3, **f32) for l in range(levels)]
+        self.tmp = [torch.empty((n >> l) ** 3, **f32) for l in range(levels)]
+        self.res = [torch.empty((n >> l) ** 3, **f32) for l in range(levels)]
+        self.r = [None] + [torch.empty((n >> l) ** 3, **f32) for l in range(1, levels + 1)]
+        self.coarse_mask = free_mask(n >> levels, device)
+
+    def __call__(self, r):
+        z = torch.empty_like(r)
+        return self._cycle(0, r, z)
+
+    def _cycle(self, l, r, out=None):
+        if l == self.levels:
+            return None if self.coarse == "none" else self._coarse_solve(l, r)
+        d = self.descs[l]
+        u = self.u[l] if out is None else out
+        mg_jacobi(d, None, r, u, self.omega)
+        mg_residual(d, u, r, self.res[l])
+        mg_restrict(d, self.res[l], self.r[l + 1], 1.0)
+        e = self._cycle(l + 1, self.r[l + 1])
+        if e is not None:
+            mg_prolong_add(d, e, u)
+        a, b = u, self.tmp[l]
+        for _ in range(self.post):
+            mg_jacobi(d, a, r, b, self.omega)
+            a, b = b, a
+        if a is not u:
+            u.copy_(a)
+        return u
+
+    def _coarse_solve(self, l, r):
+        """e = beta 4^l M(r): the network's answer to A_1 e = 4^l r, scaled by
+        the step beta = <e, r> / <e, A e> that minimises the coarse-level
+        error energy along e (0 when e is not a descent direction, so a poor
+        network output cannot make the cycle worse than the cycle without it).
+        Device-side: no host synchronisation."""
+        e = (self.net.forward(r) * float(4 ** l)).mul_(self.coarse_mask)
+        ae = torch.empty_like(e)
+        laplacian_apply(self.descs[l], e, ae)
+        num, den = torch.dot(e, r), torch.dot(e, ae)
+        beta = torch.where((num > 0) & (den > 0), num / den, torch.zeros_like(num))
+        return e.mul_(beta)
+
+
+def fcg_solve_vcycle(vcycle, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=30, fallback=True, ws=None):
+    """FCG(1) preconditioned by a VCycle (network on the coarsest level)."""
+    n = round(b.numel() ** (1.0 / 3.0))
+    ops = _Ops(n, b.device)
+    mask = free_mask(n, b.device)
+
+    def precondition(r):
+        z = vcycle(r)
+        az = torch.empty_like(z)
+        ops.A(z, az)
+        return z, az
+
+    return _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws)
+
+
+def _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws):
+    """FCG(1): p = z - (z.q_prev / p_prev.q_prev) p_prev, q = A p, alpha = p.r / p.q;
+    x in FP64, the true residual b - A x recomputed in FP64 every `refresh`
+    iterations; Jacobi-PCG takes over when it fails to halve over `stall`."""
+    n = ops.n
+    dev = b.device
+    t0 = time.perf_counter()
+    bn = ops.dot(b, b) ** 0.5
+    ax = torch.empty_like(x)
+    mask64 = mask.double()
+
     def true_residual():
         ops.A(x, ax)
-        rt = (b.double() - ax) * mask.double()
+        rt = (b - ax).mul_(mask64)
         return rt.float(), ops.dot(rt, rt) ** 0.5 / bn
 
     r, rel = true_residual()
     history = [rel]
-    q = torch.empty_like(b)
     p_prev = q_prev = None
     pq_prev = None
     it = 0
@@ -160,14 +255,14 @@ def fcg_solve(net, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=20, fallback
         z, az = precondition(r)
         if p_prev is not None:
             coef = ops.dot(z, q_prev) / pq_prev
-            p = z - coef * p_prev
-            q = az - coef * q_prev
+            p = z.add_(p_prev, alpha=-coef)
+            q = az.add_(q_prev, alpha=-coef)
         else:
             p, q = z, az
         pq = ops.dot(p, q)
         alpha = ops.dot(p, r) / pq
-        x.add_(p.double(), alpha=alpha)
-        r = r - alpha * q
+        x.add_(p, alpha=alpha)
+        r = r.add_(q, alpha=-alpha)
         p_prev, q_prev, pq_prev = p, q, pq
         it += 1
         if it % refresh == 0:
