@@ -101,6 +101,12 @@ int ngb_lbm_dense_step(const ngb_lbm_dense_desc* desc, const void* fin, void* fo
  * RunCavityTwoPop.cu:257-273 over LbmIterationD3Q19::run (LbmIteration.h:56-61). */
 int ngb_lbm_dense_run(const ngb_lbm_dense_desc* desc, void* fa, void* fb, const uint32_t* flags, int32_t nsteps, void* stream);
 
+/* Kernel launches one step of `desc` issues (1, or 2 where the analytic
+ * cavity runs as a core + wall-shell kernel pair): launch accounting for
+ * callers that size graphs or count kernels. No reference counterpart.
+ * Returns a negative status for an invalid desc. */
+int ngb_lbm_dense_kernels_per_step(const ngb_lbm_dense_desc* desc);
+
 /* Host-buffer form of ngb_lbm_dense_run for callers whose populations live
  * in host memory: copies host_in (pinned or pageable, q*plane_stride
  * elements) into fa, runs nsteps, and copies the newest populations back to

@@ -61,6 +61,7 @@ def _declare(L):
     L.ngb_lbm_wall_mask.argtypes = [i32, i32, i32, i32, vp, vp]
     L.ngb_lbm_cavity_init.argtypes = [dp, dbl, vp, vp, vp, vp]
     L.ngb_lbm_dense_macroscopic.argtypes = [dp, vp, vp, vp, vp, vp]
+    L.ngb_lbm_dense_kernels_per_step.argtypes = [dp]
     for name, args in _EXTRA_SIGNATURES.items():
         fn = getattr(L, name, None)
         if fn is not None:
@@ -400,6 +401,14 @@ def poisson_desc(nx, ny, nz, field="f32", h=1.0, bd=None):
 
 def laplacian_apply(desc, u, out, stream=None):
     return check(lib().ngb_laplacian_apply(ctypes.byref(desc), _ptr(u), _ptr(out), _stream(stream)))
+
+
+def lbm_dense_kernels_per_step(desc):
+    """Kernel launches one ngb_lbm_dense_step of `desc` issues."""
+    n = lib().ngb_lbm_dense_kernels_per_step(ctypes.byref(desc))
+    if n < 0:
+        check(n)
+    return n
 
 
 def mg_jacobi(desc, u, r, out, omega, stream=None):

@@ -224,6 +224,14 @@ int ngb_lbm_dense_step(const ngb_lbm_dense_desc* d, const void* fin, void* fout,
     return step_impl(d, fin, fout, flags, as_stream(stream));
 }
 
+int ngb_lbm_dense_kernels_per_step(const ngb_lbm_dense_desc* d)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    if (d->storage == NGB_STORE_F64) return 1;
+    return lbm_dense_split(d->q, d->storage, params_f32(d)) ? 2 : 1;
+}
+
 int ngb_lbm_dense_run(const ngb_lbm_dense_desc* d, void* fa, void* fb, const uint32_t* flags, int32_t nsteps, void* stream)
 {
     int rc = validate(d);

@@ -187,6 +187,12 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __re
     for (int q = 0; q < Q; q++) fout[q * stride + cell] = out[q];
 }
 
+// Whether the FP32-compute launcher runs the analytic cavity as the core + shell kernel pair.
+inline bool lbm_dense_split(int Q, int storage, const DenseParams<float>& p)
+{
+    return p.box && p.nx >= 4 && p.ny >= 6 && p.nz >= 6 && (Q == 19 || storage == NGB_STORE_F32);
+}
+
 // Host-side launchers (lbm_dense.cu / lbm_dense_f64.cu).
 int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
                          cudaStream_t s);

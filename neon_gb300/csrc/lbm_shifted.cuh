@@ -227,16 +227,12 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
     }
 }
 
-// One cell per thread.
+// One cell (x, y, z): classification, pull, collision, stores.
 template <int Q, typename S>
-__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                     const uint32_t* __restrict__ flags, DenseParams<float> p,
-                                                                     const __grid_constant__ DirOffsets o)
+__device__ __forceinline__ void lbm_cell(const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* __restrict__ flags,
+                                         const DenseParams<float>& p, const DirOffsets& o, int x, int y, int z)
 {
     using L = Lattice<Q>;
-    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= p.nx) return;
     const int64_t cell = x + int64_t(p.nx) * (y + int64_t(p.ny) * z);
     uint32_t      mask, lidbits;
     const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
@@ -251,6 +247,88 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* _
     char* D = reinterpret_cast<char*>(fout + cell);
 #pragma unroll
     for (int q = 0; q < Q; q++) PairIO<S>::store1(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)));
+}
+
+// One cell per thread, every cell of the grid.
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_dense_single_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                     const uint32_t* __restrict__ flags, DenseParams<float> p,
+                                                                     const __grid_constant__ DirOffsets o)
+{
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    if (x >= p.nx) return;
+    lbm_cell<Q, S>(fin, fout, flags, p, o, x, blockIdx.y, blockIdx.z);
+}
+
+// Analytic cavity, split by the walls a cell can see. The core covers
+// x in [1, nx-2], y in [2, ny-3], z in [2, nz-3] (threads on x from 0, so
+// warps keep the alignment of the rows): every cell is bulk and its
+// only wall sources are the resting x walls of the cells x = 1 (directions
+// with c_x = +1) and x = nx-2 (c_x = -1), which read the cell's own opposite
+// population plus the bounce-back wall term. Warps without such a cell take
+// the plain pull (no classification at all); the two warps of a row that
+// hold one select the source per lane, so no warp diverges. The shell kernel
+// below takes the remaining bulk cells (y or z next to a wall).
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_box_core_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                 DenseParams<float> p, const __grid_constant__ DirOffsets o)
+{
+    using L = Lattice<Q>;
+    const int      x = blockIdx.x * kLbmBlockX + threadIdx.x;  // rows stay 128-byte aligned: x = 0 is a dead lane
+    const int      y = 2 + blockIdx.y, z = 2 + blockIdx.z;
+    const bool     live = x >= 1 && x <= p.nx - 2;
+    const bool     lo = x == 1, hi = x == p.nx - 2;
+    const unsigned edge_warp = __ballot_sync(0xffffffffu, live && (lo || hi));
+    if (!live) return;
+    const int64_t cell = x + int64_t(p.nx) * (y + int64_t(p.ny) * z);
+    const char*   P = reinterpret_cast<const char*>(fin + cell);
+    float         g[Q];
+    if (edge_warp == 0) {
+#pragma unroll
+        for (int q = 0; q < Q; q++) g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const int cx = L::cx(q);
+            if (cx == 0) {
+                g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
+            } else {
+                const int     oq = L::opp(q);
+                const bool    wall = cx > 0 ? lo : hi;
+                const int64_t off = wall ? o.own[oq] : o.pull[q];
+                const float   wt = wall ? p.wall[0][oq] : 0.f;
+                const float   w = float(wall ? L::w(oq) : L::w(q));
+                const float   v = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + off)), w);
+                g[q] = wall ? v + wt : v;
+            }
+        }
+    }
+    bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
+    char* D = reinterpret_cast<char*>(fout + cell);
+#pragma unroll
+    for (int q = 0; q < Q; q++) PairIO<S>::store1(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)));
+}
+
+// The rest of the analytic cavity's bulk cells: the planes z = 1 and
+// z = nz-2 (y in [1, ny-2]) and the rows y = 1 and y = ny-2 of the planes
+// z in [2, nz-3], x in [1, nx-2]; blockIdx.y enumerates these rows.
+template <int Q, typename S>
+__global__ void __launch_bounds__(kLbmBlockX) lbm_box_shell_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                  DenseParams<float> p, const __grid_constant__ DirOffsets o)
+{
+    const int x = blockIdx.x * kLbmBlockX + threadIdx.x;
+    if (x < 1 || x > p.nx - 2) return;
+    const int r = blockIdx.y, ry = p.ny - 2, rz = p.nz - 4;
+    int       y, z;
+    if (r < 2 * ry) {
+        z = r < ry ? 1 : p.nz - 2;
+        y = 1 + (r < ry ? r : r - ry);
+    } else {
+        const int t = r - 2 * ry;
+        y = t < rz ? 1 : p.ny - 2;
+        z = 2 + (t < rz ? t : t - rz);
+    }
+    lbm_cell<Q, S>(fin, fout, nullptr, p, o, x, y, z);
 }
 
 }  // namespace ngb
