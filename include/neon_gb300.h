@@ -290,6 +290,21 @@ size_t ngb_dot_scratch_doubles(int64_t n);
  * (dGrid::dot, dGrid_imp.h:254-281; ReduceKernels.cuh:7-76 compiled out). */
 int ngb_dot(int64_t n, int32_t field, const void* a, const void* b, double* result, double* scratch, void* stream);
 
+/* Flexible CG(1) vector steps with device-side scalars, so an iteration
+ * needs no host round trip (no counterpart in the reference: libNeonSolver
+ * has plain CG only). FP32 vectors of n elements, FP64 solution x, sums
+ * accumulated as in ngb_dot. `scratch` holds ngb_fcg_scratch_doubles(n)
+ * doubles; calls on one scratch must not overlap on the GPU.
+ * Direction: coef = *zq / *pq_prev (zq NULL: first direction, coef 0);
+ * p = z - coef p_prev and q = az - coef q_prev overwrite z and az;
+ * out[0] = <p, q>, out[1] = <p, r> (device doubles). */
+size_t ngb_fcg_scratch_doubles(int64_t n);
+int    ngb_fcg_direction(int64_t n, void* z, void* az, const void* p_prev, const void* q_prev, const void* r, const double* zq,
+                         const double* pq_prev, double* out, double* scratch, void* stream);
+/* Update: alpha = pq_pr[1] / pq_pr[0]; x += alpha p, r -= alpha q; *rr = <r, r>. */
+int ngb_fcg_update(int64_t n, double* x, const void* p, void* r, const void* q, const double* pq_pr, double* rr, double* scratch,
+                   void* stream);
+
 /* Allocation-free form of ngb_dot (no counterpart in the reference): for
  * callers that cannot allocate device memory where they need the reduction
  * (between launches of a stream-ordered pipeline, where cudaMalloc would
@@ -415,6 +430,9 @@ int ngb_flip_weights(int32_t cout, int32_t cin, const float* w, void* wt, void* 
  * NULL, out is the result of two sweeps from u = 0 in one stencil pass over
  * r (2 c r - c^2 A r, c = omega h^2/6; r must be 0 on the face nodes). */
 int ngb_mg_jacobi(const ngb_poisson_desc* desc, const void* u, const void* r, void* out, double omega, void* stream);
+
+/* out = A u on the Free nodes, 0 on the face nodes. */
+int ngb_mg_apply(const ngb_poisson_desc* desc, const void* u, void* out, void* stream);
 
 /* out = r - A u on the Free nodes (u NULL: u = 0). */
 int ngb_mg_residual(const ngb_poisson_desc* desc, const void* u, const void* r, void* out, void* stream);

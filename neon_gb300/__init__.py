@@ -137,7 +137,11 @@ _EXTRA_SIGNATURES.update({
                   _i32, _vp, _vp], ctypes.c_int),
     "ngb_flip_weights": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_mg_jacobi": ([_pd, _vp, _vp, _vp, _dbl, _vp], ctypes.c_int),
+    "ngb_fcg_scratch_doubles": ([ctypes.c_int64], ctypes.c_size_t),
+    "ngb_fcg_direction": ([ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_fcg_update": ([ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "ngb_mg_residual": ([_pd, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_mg_apply": ([_pd, _vp, _vp, _vp], ctypes.c_int),
     "ngb_mg_restrict": ([_pd, _vp, _vp, _dbl, _vp], ctypes.c_int),
     "ngb_mg_prolong_add": ([_pd, _vp, _vp, _vp], ctypes.c_int),
     "ngb_conv3d_tc_supported": ([_i32, _i32, _i32, _i32, _i32, _i32, _i32], ctypes.c_int),
@@ -415,6 +419,11 @@ def mg_jacobi(desc, u, r, out, omega, stream=None):
     """out = u + omega h^2/6 (r - A u) on Free nodes; u None: two sweeps from zero."""
     return check(lib().ngb_mg_jacobi(ctypes.byref(desc), _ptr(u) if u is not None else None, _ptr(r), _ptr(out), omega,
                                      _stream(stream)))
+
+
+def mg_apply(desc, u, out, stream=None):
+    """out = A u on Free nodes, 0 on the box faces (FP32, box-face Dirichlet problem)."""
+    return check(lib().ngb_mg_apply(ctypes.byref(desc), _ptr(u), _ptr(out), _stream(stream)))
 
 
 def mg_residual(desc, u, r, out, stream=None):

@@ -17,8 +17,8 @@
 //       u2 = 2 c r - c^2 A r with c = omega h^2 / 6;
 //   residual: res = r - A u on Free nodes, 0 on faces.
 //
-// One thread per node, x fastest (coalesced rows, the six neighbours of a
-// node come from the rows the warp and its neighbours read: L1/L2 hits).
+// The stencil passes walk columns in z (mg_column_kernel); restriction takes
+// one thread per coarse node, prolongation one per fine x-pair.
 #include "common.cuh"
 
 namespace ngb {
@@ -36,34 +36,60 @@ __device__ __forceinline__ bool interior(const Box& b, int x, int y, int z)
     return x > 0 && y > 0 && z > 0 && x < b.nx - 1 && y < b.ny - 1 && z < b.nz - 1;
 }
 
-// (6 u_c - sum of the six neighbours) / h^2 at an interior node (every neighbour exists)
-__device__ __forceinline__ float apply_a(const Box& b, const float* __restrict__ u, int64_t i)
+// Stencil passes as column walks: a CTA of 32 x 8 threads owns 32 x 8
+// columns and walks kZChunk planes in z; the column's stencil values at
+// z-1, z, z+1 stay in registers, the x neighbours come from the adjacent
+// lanes (shuffles; the two tile-edge lanes load theirs), the y neighbours
+// from the rows the CTA's other warps loaded a plane earlier (L1).
+//   MODE 0: out = v + c (r - A v)        (one Jacobi sweep on u = v)
+//   MODE 1: out = 2 c v - c^2 A v        (two sweeps from zero, v = r)
+//   MODE 2: out = r - A v                (residual)
+//   MODE 3: out = v                      (residual with u = 0, v = r)
+//   MODE 4: out = A v
+// Every mode writes 0 on the face nodes.
+constexpr int kZX = 32, kZY = 8, kZChunk = 16;
+
+template <int MODE>
+__global__ void __launch_bounds__(kZX * kZY) mg_column_kernel(Box b, const float* __restrict__ v, const float* __restrict__ r,
+                                                             float* __restrict__ out, float c)
 {
+    const int     lane = threadIdx.x;
+    const int     x = blockIdx.x * kZX + lane, y = blockIdx.y * kZY + threadIdx.y;
+    const int     z0 = blockIdx.z * kZChunk, z1 = min(z0 + kZChunk, b.nz);
+    const bool    col = x < b.nx && y < b.ny;
+    const bool    inner_col = col && x > 0 && y > 0 && x < b.nx - 1 && y < b.ny - 1;
     const int64_t sy = b.nx, sz = int64_t(b.nx) * b.ny;
-    const float   s = ((__ldg(u + i - 1) + __ldg(u + i + 1)) + (__ldg(u + i - sy) + __ldg(u + i + sy))) +
-                    (__ldg(u + i - sz) + __ldg(u + i + sz));
-    return __fmul_rn(__fmaf_rn(6.f, __ldg(u + i), -s), b.inv_h2);
+    const int64_t i0 = col ? x + sy * y : 0;
+    auto          at = [&](int zz) { return (col && zz >= 0 && zz < b.nz) ? __ldg(v + i0 + sz * zz) : 0.f; };
+    float         vm = at(z0 - 1), vc = at(z0);
+    for (int z = z0; z < z1; z++) {
+        const float   vp = at(z + 1);
+        float         left = __shfl_up_sync(0xffffffffu, vc, 1), right = __shfl_down_sync(0xffffffffu, vc, 1);
+        const int64_t i = i0 + sz * z;
+        if (lane == 0) left = (inner_col && z > 0 && z < b.nz - 1) ? __ldg(v + i - 1) : 0.f;
+        if (lane == kZX - 1) right = (inner_col && z > 0 && z < b.nz - 1) ? __ldg(v + i + 1) : 0.f;
+        if (col) {
+            float o = 0.f;
+            if (inner_col && z > 0 && z < b.nz - 1) {
+                if (MODE == 3) {
+                    o = vc;
+                } else {
+                    const float s = ((left + right) + (__ldg(v + i - sy) + __ldg(v + i + sy))) + (vm + vp);
+                    const float av = __fmul_rn(__fmaf_rn(6.f, vc, -s), b.inv_h2);
+                    if (MODE == 0) o = __fmaf_rn(c, __ldg(r + i) - av, vc);
+                    if (MODE == 1) o = __fmaf_rn(-c * c, av, 2.f * c * vc);
+                    if (MODE == 2) o = __ldg(r + i) - av;
+                    if (MODE == 4) o = av;
+                }
+            }
+            out[i] = o;
+        }
+        vm = vc;
+        vc = vp;
+    }
 }
 
-// mode 0: out = u + c (r - A u); mode 1: out = 2 c r - c^2 A r (two sweeps from zero);
-// mode 2: out = r - A u (residual); mode 3: residual with u = 0 (copy of r on Free nodes)
-template <int MODE>
-__global__ void __launch_bounds__(kMgBX) mg_point_kernel(Box b, const float* __restrict__ u, const float* __restrict__ r,
-                                                        float* __restrict__ out, float c)
-{
-    const int x = blockIdx.x * kMgBX + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= b.nx) return;
-    const int64_t i = x + int64_t(b.nx) * (y + int64_t(b.ny) * z);
-    if (!interior(b, x, y, z)) {
-        out[i] = 0.f;
-        return;
-    }
-    const float ri = __ldg(r + i);
-    if (MODE == 0) out[i] = __fmaf_rn(c, ri - apply_a(b, u, i), __ldg(u + i));
-    if (MODE == 1) out[i] = __fmaf_rn(-c * c, apply_a(b, r, i), 2.f * c * ri);
-    if (MODE == 2) out[i] = ri - apply_a(b, u, i);
-    if (MODE == 3) out[i] = ri;
-}
+dim3 column_grid(const Box& b) { return dim3((b.nx + kZX - 1) / kZX, (b.ny + kZY - 1) / kZY, (b.nz + kZChunk - 1) / kZChunk); }
 
 __global__ void __launch_bounds__(kMgBX) mg_restrict_kernel(Box f, Box c, const float* __restrict__ res, float* __restrict__ rc,
                                                            float scale)
@@ -92,38 +118,35 @@ __global__ void __launch_bounds__(kMgBX) mg_restrict_kernel(Box f, Box c, const 
     rc[o] = scale * acc;
 }
 
+// One thread per fine x-pair (2X, 2X+1) of a row: fine 2X takes coarse X,
+// fine 2X+1 the mean of X and X+1 (per axis likewise for y and z); the pair
+// of u values is read and written as one float2.
 __global__ void __launch_bounds__(kMgBX) mg_prolong_add_kernel(Box f, Box c, const float* __restrict__ ec, float* __restrict__ u)
 {
-    const int x = blockIdx.x * kMgBX + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
-    if (x >= f.nx) return;
-    const int64_t i = x + int64_t(f.nx) * (y + int64_t(f.ny) * z);
-    if (!interior(f, x, y, z)) return;
+    const int X = blockIdx.x * kMgBX + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+    if (X >= c.nx || y == 0 || z == 0 || y == f.ny - 1 || z == f.nz - 1) return;
     const int64_t sy = c.nx, sz = int64_t(c.nx) * c.ny;
-    // per axis: one coarse node (even) or the mean of two (odd); fine interior nodes map inside the coarse grid
-    const int   x0 = x >> 1, y0 = y >> 1, z0 = z >> 1;
-    const int   x1 = x0 + (x & 1), y1 = y0 + (y & 1), z1 = z0 + (z & 1);
-    const float wx = (x & 1) ? 0.5f : 1.f, wy = (y & 1) ? 0.5f : 1.f, wz = (z & 1) ? 0.5f : 1.f;
-    auto        at = [&](int X, int Y, int Z) { return __ldg(ec + X + sy * Y + sz * Z); };
-    float       v = at(x0, y0, z0);
-    if (x & 1) v += at(x1, y0, z0);
-    float vy = v;
-    if (y & 1) {
-        float t = at(x0, y1, z0);
-        if (x & 1) t += at(x1, y1, z0);
-        vy += t;
-    }
-    float vz = vy;
-    if (z & 1) {
-        float t = at(x0, y0, z1);
-        if (x & 1) t += at(x1, y0, z1);
-        if (y & 1) {
-            float t2 = at(x0, y1, z1);
-            if (x & 1) t2 += at(x1, y1, z1);
-            t += t2;
+    const int     y0 = y >> 1, z0 = z >> 1;
+    const bool    yo = y & 1, zo = z & 1;
+    // sum over the coarse rows/planes of this fine (y, z) at coarse column Xc
+    auto g = [&](int Xc) {
+        const float* p = ec + Xc + sy * y0 + sz * z0;
+        float        a = __ldg(p);
+        if (yo) a += __ldg(p + sy);
+        if (zo) {
+            float t = __ldg(p + sz);
+            if (yo) t += __ldg(p + sz + sy);
+            a += t;
         }
-        vz += t;
-    }
-    u[i] += wx * wy * wz * vz;
+        return a;
+    };
+    const float w = (yo ? 0.5f : 1.f) * (zo ? 0.5f : 1.f);
+    const float g0 = g(X), g1 = X + 1 < c.nx ? g(X + 1) : 0.f;
+    float2*     up = reinterpret_cast<float2*>(u + 2 * X + int64_t(f.nx) * (y + int64_t(f.ny) * z));
+    float2      uv = *up;
+    if (X > 0) uv.x += w * g0;                 // fine x = 2X (x = 0 is a face)
+    if (2 * X + 1 < f.nx - 1) uv.y += 0.5f * w * (g0 + g1);  // fine x = 2X + 1 (x = nx - 1 is a face)
+    *up = uv;
 }
 
 int check_desc(const ngb_poisson_desc* d)
@@ -157,12 +180,13 @@ int ngb_mg_jacobi(const ngb_poisson_desc* d, const void* u, const void* r, void*
     const Box   b = box_of(d);
     const float c = float(omega * d->h * d->h / 6.0);
     cudaStream_t s = as_stream(stream);
+    const dim3 blk(kZX, kZY);
     if (u)
-        mg_point_kernel<0><<<grid_of(b), kMgBX, 0, s>>>(b, static_cast<const float*>(u), static_cast<const float*>(r),
-                                                        static_cast<float*>(out), c);
+        mg_column_kernel<0><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(u), static_cast<const float*>(r),
+                                                           static_cast<float*>(out), c);
     else
-        mg_point_kernel<1><<<grid_of(b), kMgBX, 0, s>>>(b, nullptr, static_cast<const float*>(r), static_cast<float*>(out), c);
-    NGB_LAUNCH_CHECK("mg_point_kernel");
+        mg_column_kernel<1><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(r), nullptr, static_cast<float*>(out), c);
+    NGB_LAUNCH_CHECK("mg_column_kernel");
     return NGB_OK;
 }
 
@@ -173,12 +197,25 @@ int ngb_mg_residual(const ngb_poisson_desc* d, const void* u, const void* r, voi
     NGB_CHECK_ARG(r && out && r != out && u != out, "r/out must be distinct non-NULL device pointers, u must differ from out");
     const Box    b = box_of(d);
     cudaStream_t s = as_stream(stream);
+    const dim3 blk(kZX, kZY);
     if (u)
-        mg_point_kernel<2><<<grid_of(b), kMgBX, 0, s>>>(b, static_cast<const float*>(u), static_cast<const float*>(r),
-                                                        static_cast<float*>(out), 0.f);
+        mg_column_kernel<2><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(u), static_cast<const float*>(r),
+                                                           static_cast<float*>(out), 0.f);
     else
-        mg_point_kernel<3><<<grid_of(b), kMgBX, 0, s>>>(b, nullptr, static_cast<const float*>(r), static_cast<float*>(out), 0.f);
-    NGB_LAUNCH_CHECK("mg_point_kernel");
+        mg_column_kernel<3><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(r), nullptr, static_cast<float*>(out), 0.f);
+    NGB_LAUNCH_CHECK("mg_column_kernel");
+    return NGB_OK;
+}
+
+int ngb_mg_apply(const ngb_poisson_desc* d, const void* u, void* out, void* stream)
+{
+    int rc = check_desc(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(u && out && u != out, "u/out must be distinct non-NULL device pointers");
+    const Box b = box_of(d);
+    mg_column_kernel<4><<<column_grid(b), dim3(kZX, kZY), 0, as_stream(stream)>>>(b, static_cast<const float*>(u), nullptr,
+                                                                                    static_cast<float*>(out), 0.f);
+    NGB_LAUNCH_CHECK("mg_column_kernel");
     return NGB_OK;
 }
 
@@ -204,9 +241,11 @@ int ngb_mg_prolong_add(const ngb_poisson_desc* fine, const void* ec, void* u, vo
     NGB_CHECK_ARG(fine->nx % 2 == 0 && fine->ny % 2 == 0 && fine->nz % 2 == 0 && fine->nx >= 6 && fine->ny >= 6 && fine->nz >= 6,
                   "fine dims must be even and at least 6");
     NGB_CHECK_ARG(ec && u && ec != u, "ec/u must be distinct non-NULL device pointers");
+    NGB_CHECK_ARG((reinterpret_cast<uintptr_t>(u) & 7) == 0, "u must be 8-byte aligned");
     const Box f = box_of(fine);
     const Box c{fine->nx / 2, fine->ny / 2, fine->nz / 2, f.inv_h2 * 0.25f};
-    mg_prolong_add_kernel<<<grid_of(f), kMgBX, 0, as_stream(stream)>>>(f, c, static_cast<const float*>(ec), static_cast<float*>(u));
+    mg_prolong_add_kernel<<<dim3((c.nx + kMgBX - 1) / kMgBX, f.ny, f.nz), kMgBX, 0, as_stream(stream)>>>(
+        f, c, static_cast<const float*>(ec), static_cast<float*>(u));
     NGB_LAUNCH_CHECK("mg_prolong_add_kernel");
     return NGB_OK;
 }

@@ -263,6 +263,102 @@ __global__ void __launch_bounds__(kBX) dot_kernel(int64_t n, const T* __restrict
     if (grid_sum<1>(v, partials, ticket, out) && threadIdx.x == 0) *result = out[0];
 }
 
+// FCG(1) direction with device scalars (no host round trip): coef = zq /
+// pq_prev (0 when zq is NULL: the first direction); p = z - coef p_prev and
+// q = az - coef q_prev overwrite z and az; out = {<p, q>, <p, r>}.
+__global__ void __launch_bounds__(kBX) fcg_direction_kernel(int64_t n, float* __restrict__ z, float* __restrict__ az,
+                                                           const float* __restrict__ pp, const float* __restrict__ qp,
+                                                           const float* __restrict__ r, const double* zq, const double* pq_prev,
+                                                           double* out, double* partials, unsigned int* ticket)
+{
+    const bool    first = zq == nullptr;
+    const float   coef = first ? 0.f : float(*zq / *pq_prev);
+    DotAcc<float> apq, apr;
+    const int64_t st = int64_t(gridDim.x) * kBX;
+    int64_t       i = int64_t(blockIdx.x) * kBX + threadIdx.x;
+    // four elements per trip, all loads first (more bytes in flight per thread)
+    for (; i + 3 * st < n; i += 4 * st) {
+        float p[4], q[4], rr[4], a[4], b[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            p[k] = z[i + k * st];
+            q[k] = az[i + k * st];
+            rr[k] = r[i + k * st];
+            if (!first) {
+                a[k] = pp[i + k * st];
+                b[k] = qp[i + k * st];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (!first) {
+                p[k] = __fmaf_rn(-coef, a[k], p[k]);
+                q[k] = __fmaf_rn(-coef, b[k], q[k]);
+                z[i + k * st] = p[k];
+                az[i + k * st] = q[k];
+            }
+            apq.add(p[k], q[k]);
+            apr.add(p[k], rr[k]);
+        }
+    }
+    for (; i < n; i += st) {
+        float p = z[i], q = az[i];
+        if (!first) {
+            p = __fmaf_rn(-coef, pp[i], p);
+            q = __fmaf_rn(-coef, qp[i], q);
+            z[i] = p;
+            az[i] = q;
+        }
+        apq.add(p, q);
+        apr.add(p, r[i]);
+    }
+    double v[2] = {apq.value(), apr.value()};
+    double o[2];
+    if (grid_sum<2>(v, partials, ticket, o) && threadIdx.x == 0) {
+        out[0] = o[0];
+        out[1] = o[1];
+    }
+}
+
+// FCG(1) update: alpha = pqpr[1] / pqpr[0]; x += alpha p (FP64), r -= alpha q; *rr = <r, r>.
+__global__ void __launch_bounds__(kBX) fcg_update_kernel(int64_t n, double* __restrict__ x, const float* __restrict__ p,
+                                                        float* __restrict__ r, const float* __restrict__ q,
+                                                        const double* pqpr, double* rr, double* partials, unsigned int* ticket)
+{
+    const double  alpha = pqpr[1] / pqpr[0];
+    const float   af = float(alpha);
+    DotAcc<float> acc;
+    const int64_t st = int64_t(gridDim.x) * kBX;
+    int64_t       i = int64_t(blockIdx.x) * kBX + threadIdx.x;
+    for (; i + 3 * st < n; i += 4 * st) {
+        double xv[4];
+        float  pv[4], qv[4], rv[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            xv[k] = x[i + k * st];
+            pv[k] = p[i + k * st];
+            qv[k] = q[i + k * st];
+            rv[k] = r[i + k * st];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            x[i + k * st] = fma(alpha, double(pv[k]), xv[k]);
+            const float ri = __fmaf_rn(-af, qv[k], rv[k]);
+            r[i + k * st] = ri;
+            acc.add(ri, ri);
+        }
+    }
+    for (; i < n; i += st) {
+        x[i] = fma(alpha, double(p[i]), x[i]);
+        const float ri = __fmaf_rn(-af, q[i], r[i]);
+        r[i] = ri;
+        acc.add(ri, ri);
+    }
+    double v[1] = {acc.value()};
+    double o[1];
+    if (grid_sum<1>(v, partials, ticket, o) && threadIdx.x == 0) *rr = o[0];
+}
+
 // r = T(b - A x_hi) (0 on Fixed rows); sums: |b|^2 over Free rows, r.z, |b - A x|^2.
 template <typename T>
 __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const T* __restrict__ bvec, const double* __restrict__ xh,
@@ -785,6 +881,40 @@ size_t ngb_dot_scratch_doubles(int64_t n)
 {
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((n + kBX - 1) / kBX, int64_t(sm_count()) * 4));
     return size_t(blocks) + 1;  // partials + one slot for the ticket
+}
+
+size_t ngb_fcg_scratch_doubles(int64_t n) { return 2 * (ngb_dot_scratch_doubles(n) - 1) + 1; }
+
+int ngb_fcg_direction(int64_t n, void* z, void* az, const void* p_prev, const void* q_prev, const void* r, const double* zq,
+                      const double* pq_prev, double* out, double* scratch, void* stream)
+{
+    NGB_CHECK_ARG(n > 0, "n must be positive");
+    NGB_CHECK_ARG(z && az && r && out && scratch, "NULL argument");
+    NGB_CHECK_ARG(!zq || (p_prev && q_prev && pq_prev), "zq given without p_prev, q_prev and pq_prev");
+    cudaStream_t s = as_stream(stream);
+    const int    blocks = int(ngb_dot_scratch_doubles(n) - 1);
+    unsigned int* ticket = reinterpret_cast<unsigned int*>(scratch + 2 * blocks);
+    NGB_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
+    fcg_direction_kernel<<<blocks, kBX, 0, s>>>(n, static_cast<float*>(z), static_cast<float*>(az), static_cast<const float*>(p_prev),
+                                                static_cast<const float*>(q_prev), static_cast<const float*>(r), zq, pq_prev, out,
+                                                scratch, ticket);
+    NGB_LAUNCH_CHECK("fcg_direction_kernel");
+    return NGB_OK;
+}
+
+int ngb_fcg_update(int64_t n, double* x, const void* p, void* r, const void* q, const double* pq_pr, double* rr, double* scratch,
+                   void* stream)
+{
+    NGB_CHECK_ARG(n > 0, "n must be positive");
+    NGB_CHECK_ARG(x && p && r && q && pq_pr && rr && scratch, "NULL argument");
+    cudaStream_t s = as_stream(stream);
+    const int    blocks = int(ngb_dot_scratch_doubles(n) - 1);
+    unsigned int* ticket = reinterpret_cast<unsigned int*>(scratch + 2 * blocks);
+    NGB_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
+    fcg_update_kernel<<<blocks, kBX, 0, s>>>(n, x, static_cast<const float*>(p), static_cast<float*>(r), static_cast<const float*>(q),
+                                             pq_pr, rr, scratch, ticket);
+    NGB_LAUNCH_CHECK("fcg_update_kernel");
+    return NGB_OK;
 }
 
 int ngb_dot(int64_t n, int32_t field, const void* a, const void* b, double* result, double* scratch, void* stream)

@@ -20,7 +20,7 @@ import time
 
 import torch
 
-from . import (STORE_F32, STORE_F64, _ptr, cg_solve, cg_workspace, check, dot, laplacian_apply, lib, mg_jacobi,
+from . import (STORE_F32, STORE_F64, _ptr, cg_solve, cg_workspace, check, dot, laplacian_apply, lib, mg_apply, mg_jacobi,
                 mg_prolong_add, mg_residual, mg_restrict, poisson_desc)
 
 
@@ -206,7 +206,7 @@ class VCycle:
         error energy along e (0 when e is not a descent direction, so a poor
         network output cannot make the cycle worse than the cycle without it).
         Device-side: no host synchronisation."""
-        e = (self.net.forward(r) * float(4 ** l)).mul_(self.coarse_mask)
+        e = (self.net.forward(r, sync=False) * float(4 ** l)).mul_(self.coarse_mask)
         ae = torch.empty_like(e)
         laplacian_apply(self.descs[l], e, ae)
         num, den = torch.dot(e, r), torch.dot(e, ae)
@@ -223,22 +223,30 @@ def fcg_solve_vcycle(vcycle, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=30
     def precondition(r):
         z = vcycle(r)
         az = torch.empty_like(z)
-        ops.A(z, az)
+        mg_apply(vcycle.descs[0], z, az)
         return z, az
 
-    return _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws)
+    net = vcycle.net if vcycle.coarse == "net" else None
+    return _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws,
+                check_net=net.check if net is not None else None)
 
 
-def _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws):
+def _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback, ws, check_net=None):
     """FCG(1): p = z - (z.q_prev / p_prev.q_prev) p_prev, q = A p, alpha = p.r / p.q;
     x in FP64, the true residual b - A x recomputed in FP64 every `refresh`
-    iterations; Jacobi-PCG takes over when it fails to halve over `stall`."""
+    iterations; Jacobi-PCG takes over when it fails to halve over `stall`.
+    The vector steps and their sums run in ngb_fcg_direction / ngb_fcg_update
+    with device scalars: one host read (|r|) per iteration."""
     n = ops.n
     dev = b.device
+    L = lib()
     t0 = time.perf_counter()
     bn = ops.dot(b, b) ** 0.5
     ax = torch.empty_like(x)
     mask64 = mask.double()
+    N = b.numel()
+    scratch = torch.empty(L.ngb_fcg_scratch_doubles(N), dtype=torch.float64, device=dev)
+    scal = torch.zeros(8, dtype=torch.float64, device=dev)  # zq, rr, (pq, pr) x 2 alternating
 
     def true_residual():
         ops.A(x, ax)
@@ -248,31 +256,32 @@ def _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback,
     r, rel = true_residual()
     history = [rel]
     p_prev = q_prev = None
-    pq_prev = None
     it = 0
     used_fallback = False
     while rel > tol and it < max_iter:
         z, az = precondition(r)
+        cur, prev = scal[2 + 2 * (it % 2):4 + 2 * (it % 2)], scal[2 + 2 * ((it + 1) % 2):4 + 2 * ((it + 1) % 2)]
         if p_prev is not None:
-            coef = ops.dot(z, q_prev) / pq_prev
-            p = z.add_(p_prev, alpha=-coef)
-            q = az.add_(q_prev, alpha=-coef)
+            dot(z, q_prev, scal[0:1], ops.scratch)
+            check(L.ngb_fcg_direction(N, _ptr(z), _ptr(az), _ptr(p_prev), _ptr(q_prev), _ptr(r), _ptr(scal[0:1]), _ptr(prev),
+                                      _ptr(cur), _ptr(scratch), None))
         else:
-            p, q = z, az
-        pq = ops.dot(p, q)
-        alpha = ops.dot(p, r) / pq
-        x.add_(p, alpha=alpha)
-        r = r.add_(q, alpha=-alpha)
-        p_prev, q_prev, pq_prev = p, q, pq
+            check(L.ngb_fcg_direction(N, _ptr(z), _ptr(az), None, None, _ptr(r), None, None, _ptr(cur), _ptr(scratch), None))
+        check(L.ngb_fcg_update(N, _ptr(x), _ptr(z), _ptr(r), _ptr(az), _ptr(cur), _ptr(scal[1:2]), _ptr(scratch), None))
+        p_prev, q_prev = z, az
         it += 1
         if it % refresh == 0:
+            if check_net is not None:
+                check_net()
             r, rel = true_residual()
             history.append(rel)
             if fallback and len(history) > stall // refresh and history[-1] > 0.5 * history[-1 - stall // refresh]:
                 used_fallback = True
                 break
         else:
-            rel = ops.dot(r, r) ** 0.5 / bn
+            rel = float(scal[1].item()) ** 0.5 / bn
+    if check_net is not None:
+        check_net()
     torch.cuda.synchronize()
     extra = {"iterations": 0}
     if used_fallback and rel > tol:

@@ -147,11 +147,18 @@ class UNet:
         check(lib().ngb_up2_bwd(n, n, n, C, _p(dy, dyoff), dy.shape[1], _p(dx), dx.shape[1], None))
 
     # ------------------------------------------------------------------ network
-    def forward(self, r):
-        """z = M(r) for a float32 field r of n^3 values (x fastest); returns z (float32)."""
+    def forward(self, r, sync=True):
+        """z = M(r) for a float32 field r of n^3 values (x fastest); returns z (float32).
+
+        sync=False keeps the input scale on the device and skips the
+        tensor-core time-out check (call check() later): no host round trip."""
         n = round(r.numel() ** (1.0 / 3.0))
         self._alloc(n)
-        sigma = float(torch.sqrt(torch.mean(r.double() ** 2)).item()) or 1.0
+        if sync:
+            sigma = float(torch.sqrt(torch.mean(r.double() ** 2)).item()) or 1.0
+        else:
+            rms = torch.sqrt(torch.mean(r.double() ** 2)).float()
+            sigma = torch.where(rms > 0, rms, torch.ones_like(rms))
         self.sigma = sigma
         self.in0.zero_()
         self.in0[:, 0] = (r / sigma).to(torch.bfloat16)
@@ -170,8 +177,13 @@ class UNet:
         self._up(0, self.d1b, 32, self.cat0, 0)
         self._conv(0, self.cat0, 0, 48, W["c0c"], self.d0a, 0, 16, relu=True)
         self._conv(0, self.d0a, 0, 16, W["c0d"], self.out, 0, 16, out_f32=True)
-        self._tc_check()
+        if sync:
+            self._tc_check()
         return self.out[:, 0] * sigma
+
+    def check(self):
+        """Raise if a tensor-core convolution since the last check timed out (synchronises)."""
+        self._tc_check()
 
     def backward(self, dz):
         """Accumulates dL/dw into self.g given dL/dz (float32 n^3) of the last forward."""

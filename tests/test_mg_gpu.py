@@ -64,7 +64,7 @@ def _close(got, ref, tol=1e-5):
     return float((got.double() - ref).abs().max() / max(float(ref.abs().max()), 1e-30)) <= tol
 
 
-@pytest.mark.parametrize("n,h", [(20, 1.0), (34, 2.0)])
+@pytest.mark.parametrize("n,h", [(20, 1.0), (34, 2.0), (70, 1.0)])
 def test_jacobi_and_residual_kernels(ngb, cuda, n, h):
     import torch
     d = ngb.poisson_desc(n, n, n, "f32", h)
@@ -80,6 +80,10 @@ def test_jacobi_and_residual_kernels(ngb, cuda, n, h):
     assert _close(out.reshape(n, n, n), u2)
     ngb.mg_residual(d, u.float().reshape(-1), r.float().reshape(-1), out)
     assert _close(out.reshape(n, n, n), (r - _lap64(u, h)) * _interior(n, cuda))
+    ngb.mg_residual(d, None, r.float().reshape(-1), out)
+    assert _close(out.reshape(n, n, n), r * _interior(n, cuda))
+    ngb.mg_apply(d, u.float().reshape(-1), out)
+    assert _close(out.reshape(n, n, n), _lap64(u, h) * _interior(n, cuda))
 
 
 @pytest.mark.parametrize("n", [12, 40])
@@ -150,3 +154,39 @@ def test_vcycle_fcg_converges_and_the_network_helps(ngb, cuda, trained32):
     assert plain["converged"], plain
     assert res["iterations"] < plain["iterations"] < pcg["iterations"], (res["iterations"], plain["iterations"],
                                                                          pcg["iterations"])
+
+
+def test_fcg_vector_steps_match_torch(ngb, cuda):
+    """ngb_fcg_direction / ngb_fcg_update against float64 torch restatements."""
+    import ctypes
+    import torch
+    L = ngb.lib()
+    n = 1_000_003
+    g = torch.Generator().manual_seed(7)
+    rnd = lambda: torch.randn(n, generator=g, dtype=torch.float64)
+    z, az, pp, qp, r = (rnd().float().to(cuda) for _ in range(5))
+    x = rnd().to(cuda)
+    scratch = torch.empty(L.ngb_fcg_scratch_doubles(n), dtype=torch.float64, device=cuda)
+    scal = torch.tensor([0.37, 0.0, 0.0, 0.0, 1.9], dtype=torch.float64, device=cuda)  # zq, rr, pq, pr, pq_prev
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    z0, az0, r0, x0 = z.double(), az.double(), r.double(), x.clone()
+    coef = 0.37 / 1.9
+    assert L.ngb_fcg_direction(n, P(z), P(az), P(pp), P(qp), P(r), P(scal[0:1]), P(scal[4:5]), P(scal[2:4]), P(scratch),
+                               None) == 0
+    p_ref = z0 - coef * pp.double()
+    q_ref = az0 - coef * qp.double()
+    assert float((z.double() - p_ref).abs().max()) <= 1e-6 * float(p_ref.abs().max())
+    assert float((az.double() - q_ref).abs().max()) <= 1e-6 * float(q_ref.abs().max())
+    pq, pr = float((z.double() * az.double()).sum()), float((z.double() * r0).sum())
+    assert abs(float(scal[2]) - pq) <= 1e-9 * float((z.double() * az.double()).abs().sum())
+    assert abs(float(scal[3]) - pr) <= 1e-9 * float((z.double() * r0).abs().sum())
+    assert L.ngb_fcg_update(n, P(x), P(z), P(r), P(az), P(scal[2:4]), P(scal[1:2]), P(scratch), None) == 0
+    alpha = float(scal[3]) / float(scal[2])
+    assert float((x - (x0 + alpha * z.double())).abs().max()) <= 1e-12 * float(x0.abs().max())
+    r_ref = r0 - alpha * az.double()
+    assert float((r.double() - r_ref).abs().max()) <= 1e-6 * float(r_ref.abs().max())
+    assert abs(float(scal[1]) - float((r.double() ** 2).sum())) <= 1e-9 * float((r.double() ** 2).sum())
+    # first direction: z and az are left as they are
+    z1 = z.clone()
+    assert L.ngb_fcg_direction(n, P(z), P(az), None, None, P(r), None, None, P(scal[2:4]), P(scratch), None) == 0
+    assert torch.equal(z, z1)
