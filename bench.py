@@ -39,7 +39,8 @@ BYTES_PER_UPDATE = {("d3q19", "f32"): 152, ("d3q19", "f64"): 304, ("d3q19", "f16
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 200; poisson: repeated solves, default 3)")
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="grid size (default: 384 for the LBM workloads, 512 for poisson/learned, 256 for unet)")
@@ -66,6 +67,8 @@ def parse():
     args = ap.parse_args()
     if args.n <= 0:
         args.n = {"poisson": 512, "learned": 512, "unet": 256}.get(args.workload, 384)
+    if args.steps is None:
+        args.steps = 3 if args.workload == "poisson" else 200
     return args
 
 
