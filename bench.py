@@ -79,6 +79,21 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(ms, world, device):
+    """Slowest rank's time: the whole job ends when the last replica ends."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mlups(world, cells, steps, ms):
+    """MLUPS of all replicas together (weak scaling: every rank updates `cells` per step)."""
+    return world * cells * steps / (ms * 1e3)
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -252,13 +267,9 @@ def run_ours(args):
     e1.synchronize()
     barrier()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
     per_step_ms = ms / args.steps
-    value = world * V * args.steps / (ms * 1e3)  # MLUPS, all ranks
+    value = whole_job_mlups(world, V, args.steps, ms)
     bpu = BYTES_PER_UPDATE[(lat, st)]
     peak, peak_kind = measured_peaks()
     # algorithmic bytes of the cells a step updates (the (n-2)^3 bulk cells; walls are not moved)
@@ -288,13 +299,9 @@ def run_ours(args):
         h1.record(stream)
         h1.synchronize()
         barrier()
-        ems = h0.elapsed_time(h1)
-        if world > 1:
-            t = torch.tensor([ems], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ems = float(t.item())
+        ems = max_over_ranks(h0.elapsed_time(h1), world, dev)
         nbytes = q * V * host_in.element_size()
-        e2e = {"value": round(world * V * args.steps / (ems * 1e3), 2), "unit": UNIT,
+        e2e = {"value": round(whole_job_mlups(world, V, args.steps, ems), 2), "unit": UNIT,
                "h2d_bytes_per_step": nbytes // args.steps, "d2h_bytes_per_step": nbytes // args.steps,
                "note": "one H2D of the populations, %d steps, one D2H of the result per timed call" % args.steps}
 

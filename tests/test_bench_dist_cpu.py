@@ -1,0 +1,53 @@
+"""Host logic of bench.py's multi-GPU path (replicas, one process per GPU):
+the timed region ends with the slowest rank and the value aggregates every
+rank's lattice updates. Run here as two gloo ranks on the CPU."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, q):
+    import torch
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms = 100.0 + 25.0 * rank  # rank 1 is the slower replica
+    got = bench.max_over_ranks(ms, world, torch.device("cpu"))
+    q.put((rank, got, bench.whole_job_mlups(world, 384 ** 3, 200, got)))
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_take_the_slowest_time_and_sum_the_work():
+    mp = pytest.importorskip("torch.multiprocessing")
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, ms, mlups in res:
+        assert ms == 125.0
+        assert abs(mlups - 2 * 384 ** 3 * 200 / (125.0 * 1e3)) < 1e-6
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(3.5, 1, None) == 3.5
+    assert bench.whole_job_mlups(1, 10 ** 6, 10, 2.0) == 5000.0
