@@ -38,9 +38,10 @@ __device__ __forceinline__ bool interior(const Box& b, int x, int y, int z)
 
 // Stencil passes as column walks: a CTA of 32 x 8 threads owns 32 x 8
 // columns and walks kZChunk planes in z; the column's stencil values at
-// z-1, z, z+1 stay in registers, the x neighbours come from the adjacent
-// lanes (shuffles; the two tile-edge lanes load theirs), the y neighbours
-// from the rows the CTA's other warps loaded a plane earlier (L1).
+// z-1 .. z+4 and r at z .. z+3 stay in registers (a prefetch ring three
+// planes deep), the x neighbours come from the adjacent lanes (shuffles; the
+// two tile-edge lanes load theirs), the y neighbours from the rows the
+// CTA's other warps loaded planes earlier (L1).
 //   MODE 0: out = v + c (r - A v)        (one Jacobi sweep on u = v)
 //   MODE 1: out = 2 c v - c^2 A v        (two sweeps from zero, v = r)
 //   MODE 2: out = r - A v                (residual)
@@ -61,9 +62,20 @@ __global__ void __launch_bounds__(kZX * kZY) mg_column_kernel(Box b, const float
     const int64_t sy = b.nx, sz = int64_t(b.nx) * b.ny;
     const int64_t i0 = col ? x + sy * y : 0;
     auto          at = [&](int zz) { return (col && zz >= 0 && zz < b.nz) ? __ldg(v + i0 + sz * zz) : 0.f; };
-    float         vm = at(z0 - 1), vc = at(z0);
+    constexpr bool kR = MODE == 0 || MODE == 2;
+    auto          rat = [&](int zz) { return (kR && col && zz < b.nz) ? __ldg(r + i0 + sz * zz) : 0.f; };
+    // the column's stencil values z-1 .. z+4 and r at z .. z+2 in registers: three planes of
+    // loads stay in flight while a plane is computed (a load used in its own trip exposed the
+    // whole DRAM latency once per plane)
+    // (planes beyond the chunk's last stencil source z1 are not loaded)
+    auto  atc = [&](int zz) { return zz <= z1 ? at(zz) : 0.f; };
+    auto  ratc = [&](int zz) { return zz < z1 ? rat(zz) : 0.f; };
+    float vm = at(z0 - 1), vc = at(z0), v1 = atc(z0 + 1), v2 = atc(z0 + 2), v3 = atc(z0 + 3);
+    float r0 = ratc(z0), r1 = ratc(z0 + 1), r2 = ratc(z0 + 2);
     for (int z = z0; z < z1; z++) {
-        const float   vp = at(z + 1);
+        const float   v4 = atc(z + 4);
+        const float   r3 = ratc(z + 3);
+        const float   vp = v1;
         float         left = __shfl_up_sync(0xffffffffu, vc, 1), right = __shfl_down_sync(0xffffffffu, vc, 1);
         const int64_t i = i0 + sz * z;
         if (lane == 0) left = (inner_col && z > 0 && z < b.nz - 1) ? __ldg(v + i - 1) : 0.f;
@@ -76,16 +88,22 @@ __global__ void __launch_bounds__(kZX * kZY) mg_column_kernel(Box b, const float
                 } else {
                     const float s = ((left + right) + (__ldg(v + i - sy) + __ldg(v + i + sy))) + (vm + vp);
                     const float av = __fmul_rn(__fmaf_rn(6.f, vc, -s), b.inv_h2);
-                    if (MODE == 0) o = __fmaf_rn(c, __ldg(r + i) - av, vc);
+                    if (MODE == 0) o = __fmaf_rn(c, r0 - av, vc);
                     if (MODE == 1) o = __fmaf_rn(-c * c, av, 2.f * c * vc);
-                    if (MODE == 2) o = __ldg(r + i) - av;
+                    if (MODE == 2) o = r0 - av;
                     if (MODE == 4) o = av;
                 }
             }
             out[i] = o;
         }
         vm = vc;
-        vc = vp;
+        vc = v1;
+        v1 = v2;
+        v2 = v3;
+        v3 = v4;
+        r0 = r1;
+        r1 = r2;
+        r2 = r3;
     }
 }
 
