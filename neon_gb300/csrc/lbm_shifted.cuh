@@ -9,17 +9,12 @@
 // The arithmetic is an explicit sequence of IEEE operations (this file is
 // compiled with --fmad=false; every fused multiply-add is written out), so a
 // CPU restatement using std::fmaf at the same places reproduces it bit for bit:
-//   P_a = sum_{c_a>0} g, M_a = sum_{c_a<0} g, Z = sum_{c_x=0} g (q ascending each)
-//   drho = (P_x + M_x) + Z; j_a = P_a - M_a
+//   drho = sum_q g_q (q ascending); j_a = sum_{c_a>0} g - sum_{c_a<0} g
 //   rho = 1 + drho; inv = 1 / rho; u = j * inv
 //   usq = fma(uz, uz, fma(uy, uy, ux*ux)); rus = rho * (1.5 * usq); base = drho - rus
-//   u3 = 3 u; omc = 1 - omega; per weight class: W = omega * w, wr = W rho, wb = W base
-//   rest direction: g' = fma(omc, g, wb)
-//   per direction q with opposite o (q < o): t = c_q . u3 (adds in x, y, z order),
-//          m = 0.5 t, a_q = fma(m, t, t), a_o = fma(m, t, -t),
-//          g'_q = fma(omc, g_q, fma(wr, a_q, wb)), g'_o = fma(omc, g_o, fma(wr, a_o, wb))
-// (the BGK relaxation (1 - omega) g + omega eq with omega folded into the
-// weights; q and its opposite share t and 0.5 t).
+//   u3 = 3 u; per weight class: wr = w rho, wb = w base
+//   per q: t = c . u3 (adds in x, y, z order); a = fma(0.5 t, t, t)
+//          eqg = fma(wr, a, wb); g' = fma(omega, eqg - g, g)
 #pragma once
 #include "lbm_kernels.cuh"
 
@@ -185,29 +180,26 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
 {
     constexpr float kUp = float(1u << SH), kDown = 1.0f / kUp;
     using L = Lattice<Q>;
-    V    P[3] = {splat<V>(0.f), splat<V>(0.f), splat<V>(0.f)}, M[3] = {splat<V>(0.f), splat<V>(0.f), splat<V>(0.f)};
-    V    Z = splat<V>(0.f);
-    bool sp[3] = {false, false, false}, sm[3] = {false, false, false}, sz = false;
+    V drho = g[0];
+#pragma unroll
+    for (int q = 1; q < Q; q++) drho = add2(drho, g[q]);
+    V    jp[3] = {splat<V>(0.f), splat<V>(0.f), splat<V>(0.f)}, jm[3] = {splat<V>(0.f), splat<V>(0.f), splat<V>(0.f)};
+    bool sp[3] = {false, false, false}, sm[3] = {false, false, false};
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         const int c[3] = {L::cx(q), L::cy(q), L::cz(q)};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
             if (c[a] > 0) {
-                P[a] = sp[a] ? add2(P[a], g[q]) : g[q];
+                jp[a] = sp[a] ? add2(jp[a], g[q]) : g[q];
                 sp[a] = true;
             } else if (c[a] < 0) {
-                M[a] = sm[a] ? add2(M[a], g[q]) : g[q];
+                jm[a] = sm[a] ? add2(jm[a], g[q]) : g[q];
                 sm[a] = true;
             }
         }
-        if (c[0] == 0) {
-            Z = sz ? add2(Z, g[q]) : g[q];
-            sz = true;
-        }
     }
-    V       drho = add2(add2(P[0], M[0]), Z);
-    const V jx = sub2(P[0], M[0]), jy = sub2(P[1], M[1]), jz = sub2(P[2], M[2]);
+    const V jx = sub2(jp[0], jm[0]), jy = sub2(jp[1], jm[1]), jz = sub2(jp[2], jm[2]);
     if constexpr (SH != 0) drho = mul2(drho, splat<V>(kDown));
     const V rho = add2(splat<V>(1.f), drho);
     V       inv = recip(rho);
@@ -217,28 +209,21 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
     const V rus = mul2(rho, mul2(splat<V>(1.5f), usq));
     const V base = sub2(drho, rus);
     const V u3x = mul2(splat<V>(3.f), ux), u3y = mul2(splat<V>(3.f), uy), u3z = mul2(splat<V>(3.f), uz);
-    const V omc = splat<V>(__fsub_rn(1.f, omega));
     V       wr[WeightClass<Q>::n], wb[WeightClass<Q>::n];
 #pragma unroll
     for (int k = 0; k < WeightClass<Q>::n; k++) {
-        const float W = __fmul_rn(omega, float(WeightClass<Q>::w(k)) * kUp);  // the scale is exact
-        wr[k] = mul2(splat<V>(W), rho);
-        wb[k] = mul2(splat<V>(W), base);
+        const float wk = float(WeightClass<Q>::w(k)) * kUp;  // exact
+        wr[k] = mul2(splat<V>(wk), rho);
+        wb[k] = mul2(splat<V>(wk), base);
     }
+    const V om = splat<V>(omega);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-        const int o = L::opp(q);
         const int k = WeightClass<Q>::of(q);
-        if (o < q) continue;
-        if (o == q) {
-            g[q] = fma2(omc, g[q], wb[k]);
-            continue;
-        }
-        const V t = cdot<Q, V>(q, u3x, u3y, u3z);
-        const V m = mul2(splat<V>(0.5f), t);
-        const V aq = fma2(m, t, t), ao = fma2(m, t, neg(t));
-        g[q] = fma2(omc, g[q], fma2(wr[k], aq, wb[k]));
-        g[o] = fma2(omc, g[o], fma2(wr[k], ao, wb[k]));
+        const V   t = cdot<Q, V>(q, u3x, u3y, u3z);
+        const V   a = fma2(mul2(splat<V>(0.5f), t), t, t);
+        const V   eqg = fma2(wr[k], a, wb[k]);
+        g[q] = fma2(om, sub2(eqg, g[q]), g[q]);
     }
 }
 

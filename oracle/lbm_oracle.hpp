@@ -368,14 +368,12 @@ void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Loa
 // the FP16/BF16 offset storage; no reference counterpart). Storage holds
 // f_q (FP32) or g_q = f_q - w_q (16-bit). Every operation is IEEE single
 // precision in this exact order, fused multiply-adds written as std::fmaf:
-//   P_a = sum_{c_a>0} g, M_a = sum_{c_a<0} g, Z = sum_{c_x=0} g, q ascending each
-//   drho = (P_x + M_x) + Z;  j_a = P_a - M_a
+//   drho = g_0 + g_1 + ... + g_{Q-1};  j_a = (sum_{c_a>0} g) - (sum_{c_a<0} g), q ascending
 //   rho = 1 + drho; inv = 1 / rho; u_a = j_a * inv
 //   usq = fma(uz, uz, fma(uy, uy, ux * ux)); rus = rho * (1.5 * usq); base = drho - rus
-//   u3_a = 3 * u_a; omc = 1 - omega; per weight w: W = omega * w, wr = W * rho, wb = W * base
-//   rest: g' = fma(omc, g, wb)
-//   per q < opp(q) = o: t = c_q . u3 (signed adds in x, y, z order); m = 0.5 * t
-//          g'_q = fma(omc, g_q, fma(wr, fma(m, t, t), wb)), g'_o = fma(omc, g_o, fma(wr, fma(m, t, -t), wb))
+//   u3_a = 3 * u_a; per weight w: wr = w * rho, wb = w * base
+//   per q: t = c_q . u3 (signed adds in x, y, z order); a = fma(0.5 * t, t, t)
+//          eqg = fma(wr, a, wb); g' = fma(omega, eqg - g, g)
 // Wall rule as the reference step: bit q set -> g(x, opp q) + wall term.
 template <int Q, typename LoadG, typename StoreG, typename WallTerm>
 void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega, LoadG loadg, StoreG storeg, WallTerm wall,
@@ -410,25 +408,21 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
                         g[q] = loadg(sx, sy, sz, q);
                     }
                 }
-                float pa[3] = {0, 0, 0}, ma[3] = {0, 0, 0}, zx = 0.f;
-                bool  sp[3] = {false, false, false}, sm[3] = {false, false, false}, sz = false;
-                for (int q = 0; q < Q; q++) {
+                float drho = g[0];
+                for (int q = 1; q < Q; q++) drho = drho + g[q];
+                float jp[3] = {0, 0, 0}, jm[3] = {0, 0, 0};
+                bool  sp[3] = {false, false, false}, sm[3] = {false, false, false};
+                for (int q = 0; q < Q; q++)
                     for (int a = 0; a < 3; a++) {
                         if (c[q][a] > 0) {
-                            pa[a] = sp[a] ? pa[a] + g[q] : g[q];
+                            jp[a] = sp[a] ? jp[a] + g[q] : g[q];
                             sp[a] = true;
                         } else if (c[q][a] < 0) {
-                            ma[a] = sm[a] ? ma[a] + g[q] : g[q];
+                            jm[a] = sm[a] ? jm[a] + g[q] : g[q];
                             sm[a] = true;
                         }
                     }
-                    if (c[q][0] == 0) {
-                        zx = sz ? zx + g[q] : g[q];
-                        sz = true;
-                    }
-                }
-                const float drho = (pa[0] + ma[0]) + zx;
-                const float jx = pa[0] - ma[0], jy = pa[1] - ma[1], jz = pa[2] - ma[2];
+                const float jx = jp[0] - jm[0], jy = jp[1] - jm[1], jz = jp[2] - jm[2];
                 const float rho = 1.f + drho;
                 const float inv = 1.f / rho;
                 const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
@@ -436,19 +430,10 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
                 const float rus = rho * (1.5f * usq);
                 const float base = drho - rus;
                 const float u3[3] = {3.f * ux, 3.f * uy, 3.f * uz};
-                const float omc = 1.f - omega;
-                float       out[27];
                 for (int q = 0; q < Q; q++) {
-                    const int o = op[q];
-                    if (o < q) continue;
-                    const float W = omega * w[q];  // w[o] == w[q]
-                    const float wr = W * rho, wb = W * base;
-                    if (o == q) {
-                        out[q] = std::fmaf(omc, g[q], wb);
-                        continue;
-                    }
-                    float t = 0.f;
-                    bool  started = false;
+                    const float wr = w[q] * rho, wb = w[q] * base;
+                    float       t = 0.f;
+                    bool        started = false;
                     for (int a = 0; a < 3; a++) {
                         if (c[q][a] == 0) continue;
                         if (!started) {
@@ -458,11 +443,10 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
                             t = c[q][a] > 0 ? t + u3[a] : t - u3[a];
                         }
                     }
-                    const float m = 0.5f * t;
-                    out[q] = std::fmaf(omc, g[q], std::fmaf(wr, std::fmaf(m, t, t), wb));
-                    out[o] = std::fmaf(omc, g[o], std::fmaf(wr, std::fmaf(m, t, -t), wb));
+                    const float a = std::fmaf(0.5f * t, t, t);
+                    const float eqg = std::fmaf(wr, a, wb);
+                    storeg(x, y, z, q, std::fmaf(omega, eqg - g[q], g[q]));
                 }
-                for (int q = 0; q < Q; q++) storeg(x, y, z, q, out[q]);
             }
 }
 
