@@ -48,7 +48,7 @@ __device__ __forceinline__ bool interior(const Box& b, int x, int y, int z)
 //   MODE 3: out = v                      (residual with u = 0, v = r)
 //   MODE 4: out = A v
 // Every mode writes 0 on the face nodes.
-constexpr int kZX = 32, kZY = 8, kZChunk = 16;
+constexpr int kZX = 32, kZY = 8, kZChunk = 32;
 
 template <int MODE>
 __global__ void __launch_bounds__(kZX * kZY) mg_column_kernel(Box b, const float* __restrict__ v, const float* __restrict__ r,
