@@ -138,7 +138,7 @@ def cavity_d3q19_f64(n, steps, ulb=0.1, re=100.0):
     return f.reshape(19, -1).ravel(), omega
 
 
-def main():
+def main(out=OUT):
     rng = np.random.default_rng(3)
     data = {}
     # integer stencil on the domain-stencil test box and a sparse random domain
@@ -163,8 +163,8 @@ def main():
     n, steps = 10, 60
     pops, omega = cavity_d3q19_f64(n, steps)
     data.update(cav_n=np.array(n), cav_steps=np.array(steps), cav_omega=np.array(omega), cav_pops=pops)
-    np.savez_compressed(OUT, **data)
-    print("wrote %s (%d arrays)" % (OUT, len(data)))
+    np.savez_compressed(out, **data)
+    print("wrote %s (%d arrays)" % (out, len(data)))
 
 
 if __name__ == "__main__":

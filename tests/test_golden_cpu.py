@@ -48,3 +48,21 @@ def test_oracle_cavity_matches_golden(orc, kat):
     pops, _, omega = oracle_cavity(orc, n, 19, 0, steps)
     assert abs(omega - float(kat["cav_omega"])) <= 1e-15
     assert rel_max(pops, kat["cav_pops"]) <= 1e-13
+
+
+def test_golden_fixture_regenerates(tmp_path, kat):
+    """The committed vectors are what tests/golden/make_golden.py produces."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(GOLDEN), "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    out = str(tmp_path / "kat.npz")
+    mod.main(out)
+    fresh = np.load(out)
+    assert sorted(fresh.files) == sorted(kat.files)
+    for k in kat.files:
+        if kat[k].dtype.kind == "f":  # FP64 sums may round differently under another BLAS
+            assert np.allclose(fresh[k], kat[k], rtol=1e-13, atol=0), k
+        else:
+            assert np.array_equal(fresh[k], kat[k]), k
