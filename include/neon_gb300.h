@@ -416,6 +416,20 @@ int ngb_adam(int64_t n, float* p, const float* g, float* m, float* s, float lr, 
 /* wt[ci][26 - t][co] = BF16(w[co][t][ci]): weights of the backward-data convolution. */
 int ngb_flip_weights(int32_t cout, int32_t cin, const float* w, void* wt, void* stream);
 
+/* Network input and output with the scale kept on the device (no host
+ * round trip). `rr` is a device double holding |r|^2 (ngb_dot), sigma =
+ * sqrt(rr / V) (1 for a zero field). Input: channel 0 of the channels-last
+ * BF16 tensor in0 (row stride ld) = bf16(r / sigma); the other channels are
+ * left as they are. Output: e = scale * sigma * out[v * ld] on the interior
+ * of the nx*ny*nz box, 0 on its faces. */
+int ngb_unet_input(int64_t V, const float* r, const double* rr, void* in0, int32_t ld, void* stream);
+int ngb_unet_output(int32_t nx, int32_t ny, int32_t nz, const float* out, int32_t ld, const double* rr, double scale, float* e,
+                    void* stream);
+
+/* e *= num / den when both device doubles are positive, else e = 0 (the
+ * energy-minimising step of a correction e: num = <e, r>, den = <e, A e>). */
+int ngb_scale_by_ratio(int64_t n, float* e, const double* num, const double* den, void* stream);
+
 /* ------------------------------------------------------------------------
  * Multilevel learned preconditioner: smoothing and grid transfer between
  * vertex-centred levels (no reference counterpart; libNeonSolver has CG

@@ -137,6 +137,9 @@ _EXTRA_SIGNATURES.update({
                   _i32, _vp, _vp], ctypes.c_int),
     "ngb_flip_weights": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_mg_jacobi": ([_pd, _vp, _vp, _vp, _dbl, _vp], ctypes.c_int),
+    "ngb_unet_input": ([ctypes.c_int64, _vp, _vp, _vp, _i32, _vp], ctypes.c_int),
+    "ngb_unet_output": ([_i32, _i32, _i32, _vp, _i32, _vp, _dbl, _vp, _vp], ctypes.c_int),
+    "ngb_scale_by_ratio": ([ctypes.c_int64, _vp, _vp, _vp, _vp], ctypes.c_int),
     "ngb_fcg_scratch_doubles": ([ctypes.c_int64], ctypes.c_size_t),
     "ngb_fcg_direction": ([ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "ngb_fcg_update": ([ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),

@@ -10,6 +10,7 @@
 // are formed without copies. Convolutions use zero padding.
 #include "common.cuh"
 
+#include <algorithm>
 #include <cstdint>
 
 namespace ngb {
@@ -305,6 +306,43 @@ int grid1d(int64_t n) { return int(std::min<int64_t>((n + 255) / 256, 152 * 16))
 
 Grid3 make_grid(int nx, int ny, int nz) { return Grid3{nx, ny, nz, int64_t(nx) * ny * nz}; }
 
+// Network input on the device: channel 0 of the channels-last BF16 input
+// = bf16(r / sigma), sigma = sqrt(rr / V) (the field's RMS; 1 for a zero
+// field). The network is bias-free with ReLU, so M(a r) = a M(r) for a > 0.
+__global__ void unet_input_kernel(int64_t V, const float* __restrict__ r, const double* __restrict__ rr, __nv_bfloat16* in0,
+                                  int32_t ld)
+{
+    const double ms = *rr / double(V);
+    const float  sigma = ms > 0.0 ? float(sqrt(ms)) : 1.f;
+    for (int64_t v = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < V; v += int64_t(gridDim.x) * blockDim.x)
+        in0[v * ld] = __float2bfloat16_rn(r[v] / sigma);
+}
+
+// e = scale * sigma * out[:, 0] on interior nodes of the nx*ny*nz box, 0 on its faces.
+__global__ void unet_output_kernel(int32_t nx, int32_t ny, int32_t nz, const float* __restrict__ out, int32_t ld,
+                                   const double* __restrict__ rr, float scale, float* __restrict__ e)
+{
+    const int64_t V = int64_t(nx) * ny * nz;
+    const double  ms = *rr / double(V);
+    const float   sigma = ms > 0.0 ? float(sqrt(ms)) : 1.f;
+    const float   k = scale * sigma;
+    for (int64_t v = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < V; v += int64_t(gridDim.x) * blockDim.x) {
+        const int  x = int(v % nx), y = int((v / nx) % ny), z = int(v / (int64_t(nx) * ny));
+        const bool face = x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1;
+        e[v] = face ? 0.f : out[v * ld] * k;
+    }
+}
+
+// e *= num / den when both are positive, else e = 0 (device scalars).
+__global__ void scale_by_ratio_kernel(int64_t n, float* __restrict__ e, const double* __restrict__ num, const double* __restrict__ den)
+{
+    const double a = *num, b = *den;
+    const float  beta = (a > 0.0 && b > 0.0) ? float(a / b) : 0.f;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) e[i] *= beta;
+}
+
+int stream_grid(int64_t n) { return int(std::min<int64_t>((n + 255) / 256, 152 * 16)); }
+
 }  // namespace
 }  // namespace ngb
 
@@ -430,6 +468,35 @@ int ngb_flip_weights(int32_t cout, int32_t cin, const float* w, void* wt, void* 
     NGB_CHECK_ARG(cout > 0 && cin > 0 && w && wt, "bad argument");
     flip_weights_kernel<<<grid1d(int64_t(cout) * 27 * cin), 256, 0, as_stream(stream)>>>(cout, cin, w, static_cast<__nv_bfloat16*>(wt));
     NGB_LAUNCH_CHECK("flip_weights_kernel");
+    return NGB_OK;
+}
+
+int ngb_unet_input(int64_t V, const float* r, const double* rr, void* in0, int32_t ld, void* stream)
+{
+    NGB_CHECK_ARG(V > 0 && ld >= 1, "V and ld must be positive");
+    NGB_CHECK_ARG(r && rr && in0, "NULL pointer");
+    unet_input_kernel<<<stream_grid(V), 256, 0, as_stream(stream)>>>(V, r, rr, static_cast<__nv_bfloat16*>(in0), ld);
+    NGB_LAUNCH_CHECK("unet_input_kernel");
+    return NGB_OK;
+}
+
+int ngb_unet_output(int32_t nx, int32_t ny, int32_t nz, const float* out, int32_t ld, const double* rr, double scale, float* e,
+                    void* stream)
+{
+    NGB_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1 && ld >= 1, "dims and ld must be positive");
+    NGB_CHECK_ARG(out && rr && e, "NULL pointer");
+    const int64_t V = int64_t(nx) * ny * nz;
+    unet_output_kernel<<<stream_grid(V), 256, 0, as_stream(stream)>>>(nx, ny, nz, out, ld, rr, float(scale), e);
+    NGB_LAUNCH_CHECK("unet_output_kernel");
+    return NGB_OK;
+}
+
+int ngb_scale_by_ratio(int64_t n, float* e, const double* num, const double* den, void* stream)
+{
+    NGB_CHECK_ARG(n > 0, "n must be positive");
+    NGB_CHECK_ARG(e && num && den, "NULL pointer");
+    scale_by_ratio_kernel<<<stream_grid(n), 256, 0, as_stream(stream)>>>(n, e, num, den);
+    NGB_LAUNCH_CHECK("scale_by_ratio_kernel");
     return NGB_OK;
 }
 

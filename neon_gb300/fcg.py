@@ -176,6 +176,10 @@ class VCycle:
         self.res = [torch.empty((n >> l) ** 3, **f32) for l in range(levels)]
         self.r = [None] + [torch.empty((n >> l) ** 3, **f32) for l in range(1, levels + 1)]
         self.coarse_mask = free_mask(n >> levels, device)
+        nc3 = (n >> levels) ** 3
+        self.e_coarse, self.ae_coarse = torch.empty(nc3, **f32), torch.empty(nc3, **f32)
+        self.scal = torch.zeros(3, dtype=torch.float64, device=device)  # |r|^2, <e, r>, <e, A e>
+        self.scratch = torch.empty(lib().ngb_dot_scratch_doubles(nc3), dtype=torch.float64, device=device)
 
     def __call__(self, r):
         z = torch.empty_like(r)
@@ -205,13 +209,14 @@ class VCycle:
         the step beta = <e, r> / <e, A e> that minimises the coarse-level
         error energy along e (0 when e is not a descent direction, so a poor
         network output cannot make the cycle worse than the cycle without it).
-        Device-side: no host synchronisation."""
-        e = (self.net.forward(r, sync=False) * float(4 ** l)).mul_(self.coarse_mask)
-        ae = torch.empty_like(e)
-        laplacian_apply(self.descs[l], e, ae)
-        num, den = torch.dot(e, r), torch.dot(e, ae)
-        beta = torch.where((num > 0) & (den > 0), num / den, torch.zeros_like(num))
-        return e.mul_(beta)
+        Device-side library calls only: no host synchronisation."""
+        e, ae, s = self.e_coarse, self.ae_coarse, self.scal
+        self.net.apply(r, e, float(4 ** l), s[0:1], self.scratch)
+        mg_apply(self.descs[l], e, ae)
+        dot(e, r, s[1:2], self.scratch)
+        dot(e, ae, s[2:3], self.scratch)
+        check(lib().ngb_scale_by_ratio(e.numel(), _ptr(e), _ptr(s[1:2]), _ptr(s[2:3]), None))
+        return e
 
 
 def fcg_solve_vcycle(vcycle, b, x, tol=1e-8, max_iter=2000, refresh=10, stall=30, fallback=True, ws=None):

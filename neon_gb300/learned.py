@@ -162,6 +162,13 @@ class UNet:
         self.sigma = sigma
         self.in0.zero_()
         self.in0[:, 0] = (r / sigma).to(torch.bfloat16)
+        self._layers()
+        if sync:
+            self._tc_check()
+        return self.out[:, 0] * sigma
+
+    def _layers(self):
+        """The convolutions, poolings and upsamplings from in0 to out."""
         W = self.wb
         self._conv(0, self.in0, 0, 16, W["c0a"], self.a0, 0, 16, relu=True)
         self._conv(0, self.a0, 0, 16, W["c0b"], self.cat0, 32, 16, relu=True)
@@ -177,13 +184,28 @@ class UNet:
         self._up(0, self.d1b, 32, self.cat0, 0)
         self._conv(0, self.cat0, 0, 48, W["c0c"], self.d0a, 0, 16, relu=True)
         self._conv(0, self.d0a, 0, 16, W["c0d"], self.out, 0, 16, out_f32=True)
-        if sync:
-            self._tc_check()
-        return self.out[:, 0] * sigma
 
     def check(self):
         """Raise if a tensor-core convolution since the last check timed out (synchronises)."""
         self._tc_check()
+
+    def apply(self, r, e, scale=1.0, rr=None, scratch=None):
+        """e = scale * M(r), 0 on the box faces, entirely on the device (no
+        host round trip, no torch arithmetic): |r|^2 by ngb_dot, the scaled
+        BF16 input and the scaled output by ngb_unet_input / ngb_unet_output.
+        Tensor-core time-outs are reported by check()."""
+        n = round(r.numel() ** (1.0 / 3.0))
+        self._alloc(n)
+        L = lib()
+        if rr is None:
+            rr = torch.zeros(1, dtype=torch.float64, device=self.dev)
+        if scratch is None:
+            scratch = torch.empty(L.ngb_dot_scratch_doubles(r.numel()), dtype=torch.float64, device=self.dev)
+        check(L.ngb_dot(r.numel(), STORE_F32, _ptr(r), _ptr(r), _ptr(rr), _ptr(scratch), None))
+        check(L.ngb_unet_input(r.numel(), _ptr(r), _ptr(rr), _ptr(self.in0), self.in0.shape[1], None))
+        self._layers()
+        check(L.ngb_unet_output(n, n, n, _ptr(self.out), self.out.shape[1], _ptr(rr), scale, _ptr(e), None))
+        return e
 
     def backward(self, dz):
         """Accumulates dL/dw into self.g given dL/dz (float32 n^3) of the last forward."""

@@ -190,3 +190,38 @@ def test_fcg_vector_steps_match_torch(ngb, cuda):
     z1 = z.clone()
     assert L.ngb_fcg_direction(n, P(z), P(az), None, None, P(r), None, None, P(scal[2:4]), P(scratch), None) == 0
     assert torch.equal(z, z1)
+
+
+def test_network_device_apply_matches_forward(ngb, cuda):
+    """UNet.apply (scale kept on the device, ngb_unet_input / ngb_unet_output)
+    against the torch-glued forward on the same weights: equal up to the BF16
+    rounding of an input whose scale differs in the last bit."""
+    import torch
+    from neon_gb300 import fcg
+    from neon_gb300.learned import UNet
+    n = 32
+    net = UNet(seed=3, device=cuda)
+    r = fcg.grf_k2(n, 5, cuda)
+    e = torch.full_like(r, float("nan"))
+    net.apply(r, e, 16.0)
+    net.check()
+    ref = net.forward(r) * 16.0 * fcg.free_mask(n, cuda)
+    torch.cuda.synchronize()
+    assert torch.isfinite(e).all()
+    assert float((e - ref).abs().max()) <= 1e-2 * float(ref.abs().max())
+    assert float(e.reshape(n, n, n)[0].abs().max()) == 0.0  # faces
+
+
+def test_scale_by_ratio(ngb, cuda):
+    import ctypes
+    import torch
+    L = ngb.lib()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    e = torch.arange(1000, dtype=torch.float32, device=cuda)
+    s = torch.tensor([3.0, 4.0, -1.0], dtype=torch.float64, device=cuda)
+    assert L.ngb_scale_by_ratio(1000, P(e), P(s[0:1]), P(s[1:2]), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(e, torch.arange(1000, dtype=torch.float32, device=cuda) * 0.75)
+    assert L.ngb_scale_by_ratio(1000, P(e), P(s[2:3]), P(s[1:2]), None) == 0  # a negative step is no step
+    torch.cuda.synchronize()
+    assert float(e.abs().max()) == 0.0
