@@ -60,3 +60,28 @@ def test_kernels_per_step_query(ngb):
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 19, "f64", 1.0, box_cavity=True)) == 1
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 19, "f32", 1.0, box_cavity=False)) == 1
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 5, 64, 19, "f32", 1.0, box_cavity=True)) == 1
+
+
+def test_new_entry_points_validate_without_gpu(ngb):
+    """Argument errors of the multilevel, FCG and network-scaling entry points
+    are reported before any CUDA call."""
+    import ctypes
+    L = ngb.lib()
+    odd = ngb.poisson_desc(13, 12, 12, "f32", 1.0)
+    assert L.ngb_mg_restrict(ctypes.byref(odd), ctypes.c_void_p(16), ctypes.c_void_p(32), 1.0, None) == -1
+    assert b"even" in L.ngb_last_error()
+    f64 = ngb.poisson_desc(12, 12, 12, "f64", 1.0)
+    assert L.ngb_mg_apply(ctypes.byref(f64), ctypes.c_void_p(16), ctypes.c_void_p(32), None) == -1
+    assert b"FP32" in L.ngb_last_error()
+    box = ngb.poisson_desc(12, 12, 12, "f32", 1.0)
+    assert L.ngb_mg_jacobi(ctypes.byref(box), None, ctypes.c_void_p(16), ctypes.c_void_p(32), 2.5, None) == -1
+    assert b"omega" in L.ngb_last_error()
+    assert L.ngb_fcg_direction(0, None, None, None, None, None, None, None, None, None, None) == -1
+    assert L.ngb_fcg_direction(10, ctypes.c_void_p(16), ctypes.c_void_p(32), None, None, ctypes.c_void_p(48),
+                               ctypes.c_void_p(64), None, ctypes.c_void_p(80), ctypes.c_void_p(96), None) == -1
+    assert b"zq given" in L.ngb_last_error()
+    assert L.ngb_fcg_update(10, None, None, None, None, None, None, None, None) == -1
+    assert L.ngb_unet_input(0, None, None, None, 16, None) == -1
+    assert L.ngb_unet_output(8, 8, 8, None, 16, None, 1.0, None, None) == -1
+    assert L.ngb_scale_by_ratio(0, None, None, None, None) == -1
+    assert L.ngb_fcg_scratch_doubles(1000) >= 3
