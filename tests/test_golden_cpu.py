@@ -66,3 +66,18 @@ def test_golden_fixture_regenerates(tmp_path, kat):
             assert np.allclose(fresh[k], kat[k], rtol=1e-13, atol=0), k
         else:
             assert np.array_equal(fresh[k], kat[k]), k
+
+
+@pytest.mark.parametrize("n,steps", [(6, 1), (9, 7), (14, 25)])
+def test_oracle_cavity_matches_numpy_restatement(orc, n, steps):
+    """The C++ oracle's reference-arithmetic D3Q19 cavity against the numpy
+    restatement that made the golden vectors, at other sizes and step counts."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(GOLDEN), "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    ref, omega = mod.cavity_d3q19_f64(n, steps)
+    pops, _, omega2 = oracle_cavity(orc, n, 19, 0, steps)
+    assert abs(omega - omega2) <= 1e-15
+    assert rel_max(pops, ref) <= 1e-13
