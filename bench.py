@@ -153,9 +153,14 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.t.join(timeout=2)
+        return self.summarise(self.lines)
+
+    @staticmethod
+    def summarise(lines):
+        """Median SM clock under the samples, the maximum clock and the throttle reasons seen active."""
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue

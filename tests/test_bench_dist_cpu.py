@@ -51,3 +51,17 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.max_over_ranks(3.5, 1, None) == 3.5
     assert bench.whole_job_mlups(1, 10 ** 6, 10, 2.0) == 5000.0
+
+
+def test_clock_summary_reads_nvidia_smi_samples():
+    """The clocks record of the bench line: median SM clock, maximum, and the
+    throttle reasons that were active in any sample (nvidia-smi csv lines)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    lines = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+             "0, 1980, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active",
+             "0, 2070, 2070, 1200.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+             "garbage line"]
+    got = bench.ClockSampler.summarise(lines)
+    assert got == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert bench.ClockSampler.summarise([])["sm_mhz"] is None
