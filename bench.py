@@ -119,21 +119,41 @@ def profiled_traffic(name):
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+    """Samples nvidia-smi clocks and throttle reasons while the GPU runs the
+    timed work. The GPU is selected by its UUID (nvidia-smi numbers GPUs
+    its own way and ignores CUDA_VISIBLE_DEVICES); each sample carries
+    nvidia-smi's own timestamp, so the summary can keep only the samples
+    taken inside a window of host wall-clock time."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
-        self.gpu = gpu_index
+    def __init__(self, device, period_ms=50):
+        self.gpu = self.gpu_selector(device)
+        self.period_ms = period_ms
         self.proc = None
         self.lines = []
 
-    def start(self):
+    @staticmethod
+    def gpu_selector(device):
+        """nvidia-smi -i argument of a torch CUDA device: GPU-<uuid>, else the PCI bus id."""
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+            import torch
+            p = torch.cuda.get_device_properties(device)
+            u = str(getattr(p, "uuid", "") or "")
+            if u:
+                return u if u.startswith("GPU-") else "GPU-" + u
+            return "%08x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+        except Exception:
+            return None
+
+    def start(self):
+        if self.gpu is None:
+            return
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu, "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -144,32 +164,51 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def stop(self, window=None):
+        """Summary of the samples whose timestamp lies in window = (t0, t1) (time.time() values)."""
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(2.0 * self.period_ms / 1000.0)  # let the last samples of the window arrive
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.t.join(timeout=2)
-        return self.summarise(self.lines)
+        out = self.summarise(self.lines, window)
+        out["gpu"] = self.gpu
+        return out
 
     @staticmethod
-    def summarise(lines):
-        """Median SM clock under the samples, the maximum clock and the throttle reasons seen active."""
+    def parse_time(stamp):
+        """Seconds since the epoch of an nvidia-smi timestamp ("2026/12/04 14:01:02.123", local time)."""
+        import datetime
+        try:
+            return datetime.datetime.strptime(stamp.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
+    @staticmethod
+    def summarise(lines, window=None):
+        """Median SM clock over the samples (inside `window` when given), the
+        maximum clock, and the throttle reasons active in any of them."""
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in lines:
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
+            if window is not None:
+                t = ClockSampler.parse_time(parts[0])
+                if t is None or not (window[0] <= t <= window[1]):
+                    continue
             try:
-                sm.append(float(parts[1]))
-                smax = float(parts[2])
+                clk = float(parts[2])
+                smax = float(parts[3])
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
+            sm.append(clk)
+            for nm, v in zip(names, parts[6:10]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
         sm.sort()

@@ -97,9 +97,16 @@ int ngb_lbm_dense_step(const ngb_lbm_dense_desc* desc, const void* fin, void* fo
 
 /* `nsteps` steps ping-ponging fa -> fb -> fa ...; after an odd count the
  * newest populations are in fb. Launches are captured once into a CUDA graph
- * per (desc, pointers) and replayed. Replaces the host loop of
+ * per (desc, pointers) and replayed; the library keeps the 8 most recently
+ * used graphs and destroys older ones. Replaces the host loop of
  * RunCavityTwoPop.cu:257-273 over LbmIterationD3Q19::run (LbmIteration.h:56-61). */
 int ngb_lbm_dense_run(const ngb_lbm_dense_desc* desc, void* fa, void* fb, const uint32_t* flags, int32_t nsteps, void* stream);
+
+/* Destroys every step graph ngb_lbm_dense_run keeps (a graph still running
+ * is freed when its launch completes). Call before freeing population
+ * buffers for good, or to return the graphs' memory. No reference
+ * counterpart (the reference launches without graphs). */
+int ngb_lbm_release_graphs(void);
 
 /* Kernel launches one step of `desc` issues (1, or 2 where the analytic
  * cavity runs as a core + wall-shell kernel pair): launch accounting for
@@ -109,8 +116,9 @@ int ngb_lbm_dense_kernels_per_step(const ngb_lbm_dense_desc* desc);
 
 /* Host-buffer form of ngb_lbm_dense_run for callers whose populations live
  * in host memory: copies host_in (pinned or pageable, q*plane_stride
- * elements) into fa, runs nsteps, and copies the newest populations back to
- * host_out; fa/fb are caller-provided device buffers. Stream-ordered; the
+ * elements) into fa (and, for an odd nsteps, on into fb, whose non-bulk
+ * nodes the steps never write), runs nsteps, and copies the newest
+ * populations back to host_out; fa/fb are caller-provided device buffers. Stream-ordered; the
  * host buffers must stay valid until the stream reaches this point.
  * Replaces Field::updateDeviceData / run loop / Field::updateHostData
  * (dField_imp.h, RunCavityTwoPop.cu:226-273). */
@@ -313,8 +321,10 @@ int ngb_fcg_update(int64_t n, double* x, const void* p, void* r, const void* q, 
  * as ngb_dot up to summation order; the per-CTA partials live in a fixed
  * 256 KiB array inside this library (held on every GPU that loads it until
  * exit), so n is limited to 2^28 elements (NGB_ERR_RANGE beyond). Calls no
- * cudaMalloc/cudaFree. The first call on a device looks up the array's
- * device address (make it before any stream capture on that device). All
+ * cudaMalloc/cudaFree. Each call looks up the array's device address in the
+ * CUDA context current on the calling thread (primary or driver-API context);
+ * a call under stream capture reuses the address the last uncaptured call saw
+ * in that context, so make one call in a context before capturing there. All
  * calls share the array: calls whose kernels overlap on the GPU race. */
 #define NGB_DOT_NOALLOC_MAX_N (268435456LL)
 int ngb_dot_noalloc(int64_t n, int32_t field, const void* a, const void* b, double* result, void* stream);

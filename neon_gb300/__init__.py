@@ -97,6 +97,7 @@ _EXTRA_SIGNATURES = {
     "ngb_bgrid_flags_from_dense": ([_bd, _i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_bgrid_laplace_i64": ([_bd, _vp, _vp, _vp], ctypes.c_int),
     "ngb_dense_laplace_i64": ([_i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_lbm_release_graphs": ([], ctypes.c_int),
 }
 
 

@@ -21,12 +21,20 @@
 // on the partials.
 //
 // Host code cannot use the array's name as a device address (in host code it
-// names a host-side stand-in), so the first call on each device looks up the
-// device address with cudaGetSymbolAddress while that device is current and
-// keeps it. That first call may load the module lazily; make it before any
-// stream capture on that device.
+// names a host-side stand-in), so each call looks up the device address with
+// cudaGetSymbolAddress in the CUDA context current on the calling thread: the
+// array exists once per context (the device's primary context, or a context
+// a driver-API host made current), and an address taken in one context is not
+// mapped in another, nor after cudaDeviceReset. A call made while its stream
+// is being captured cannot do that lookup, so it uses the address that the
+// last uncaptured call saw in the same context (kept per context handle). The
+// first call in a context may load the module lazily: make it before any
+// stream capture in that context.
 #include "common.cuh"
+#include <cuda.h>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 namespace ngb {
 namespace {
@@ -40,9 +48,11 @@ constexpr int64_t kNoallocMaxN = int64_t(kNoallocMaxPartials) * kChunk;    // 2^
 // partials[0 .. kNoallocMaxPartials), then the ticket word in the last slot.
 static __device__ __align__(256) double g_dot_noalloc_scratch[kNoallocMaxPartials + 1];
 
-constexpr int kMaxDevices = 64;
-std::mutex    g_setup_mutex;
-double*       g_scratch_addr[kMaxDevices] = {nullptr};
+// (context handle, device address) of the lookups made outside stream capture.
+std::mutex                                  g_setup_mutex;
+std::vector<std::pair<CUcontext, double*>>  g_scratch_addr;
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn                             g_ctx_get_current = nullptr;
 
 template <typename T>
 __global__ void __launch_bounds__(kNoallocThreads) dot_noalloc_kernel(int64_t n, const T* __restrict__ a, const T* __restrict__ b,
@@ -86,19 +96,50 @@ __global__ void __launch_bounds__(kNoallocThreads) dot_noalloc_kernel(int64_t n,
     }
 }
 
-// Device address of the scratch array on the current device (set up once per device).
-int scratch_address(double** out)
+// Device address of the scratch array in the calling thread's current
+// context. Outside capture: looked up afresh and remembered for the context;
+// under capture: the remembered address of the same context.
+int scratch_address(cudaStream_t s, double** out)
 {
-    int dev = 0;
-    NGB_CUDA_TRY(cudaGetDevice(&dev));
-    NGB_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "device ordinal %d beyond %d", dev, kMaxDevices);
+    // first runtime call: binds the device's primary context to the thread
+    // unless the caller made another context current
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    NGB_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        NGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_dot_noalloc_scratch));
-        g_scratch_addr[dev] = static_cast<double*>(p);
+    if (!g_ctx_get_current) {
+        void*                           fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        NGB_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("ngb_dot_noalloc: cuCtxGetCurrent not available from the driver");
+            return NGB_ERR_CUDA;
+        }
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
     }
-    *out = g_scratch_addr[dev];
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) {
+        set_error("ngb_dot_noalloc: no current CUDA context");
+        return NGB_ERR_CUDA;
+    }
+    for (auto& e : g_scratch_addr) {
+        if (e.first != ctx) continue;
+        if (cap == cudaStreamCaptureStatusNone) {
+            void* p = nullptr;
+            NGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_dot_noalloc_scratch));
+            e.second = static_cast<double*>(p);
+        }
+        *out = e.second;
+        return NGB_OK;
+    }
+    if (cap != cudaStreamCaptureStatusNone) {
+        set_error("ngb_dot_noalloc: first call in this CUDA context made under stream capture; "
+                  "call it once outside capture first");
+        return NGB_ERR_INVALID;
+    }
+    void* p = nullptr;
+    NGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_dot_noalloc_scratch));
+    g_scratch_addr.emplace_back(ctx, static_cast<double*>(p));
+    *out = static_cast<double*>(p);
     return NGB_OK;
 }
 
@@ -119,10 +160,10 @@ int ngb_dot_noalloc(int64_t n, int32_t field, const void* a, const void* b, doub
                   (long long)n, (long long)kNoallocMaxN, kNoallocMaxPartials);
         return NGB_ERR_RANGE;
     }
-    double* scratch = nullptr;
-    int     rc = scratch_address(&scratch);
-    if (rc) return rc;
     cudaStream_t s = as_stream(stream);
+    double*      scratch = nullptr;
+    int          rc = scratch_address(s, &scratch);
+    if (rc) return rc;
     if (n == 0) {
         NGB_CUDA_TRY(cudaMemsetAsync(result, 0, sizeof(double), s));
         return NGB_OK;

@@ -1,6 +1,7 @@
 // Dense LBM: FP32-compute step instantiations and the C-ABI entry points
 // (step, graph-captured run, wall mask, cavity set-up, macroscopic fields).
 #include "lbm_kernels.cuh"
+#include <list>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -69,15 +70,32 @@ struct RunKey {
     int                steps;
     bool operator<(const RunKey& o) const { return std::memcmp(this, &o, sizeof(RunKey)) < 0; }
 };
-std::mutex                         g_run_mutex;
-std::map<RunKey, cudaGraphExec_t>  g_run_graphs;
-constexpr int                      kStepsPerGraph = 32;  // even: the graph ends on the buffer it started from
+// Least-recently-used cache of instantiated step graphs, bounded so that
+// callers that reallocate their population buffers do not accumulate graphs.
+// An evicted graph may still be running on a stream: cudaGraphExecDestroy
+// then frees it once that launch completes.
+struct RunCache {
+    std::list<std::pair<RunKey, cudaGraphExec_t>>                                    lru;  // front = newest
+    std::map<RunKey, std::list<std::pair<RunKey, cudaGraphExec_t>>::iterator>        index;
+};
+std::mutex    g_run_mutex;
+RunCache      g_run_graphs;
+constexpr int kStepsPerGraph = 32;  // even: the graph ends on the buffer it started from
+constexpr int kMaxRunGraphs = 8;
+
+void release_run_graphs_locked()
+{
+    for (auto& e : g_run_graphs.lru) cudaGraphExecDestroy(e.second);
+    g_run_graphs.lru.clear();
+    g_run_graphs.index.clear();
+}
 
 int get_run_graph(const RunKey& k, cudaGraphExec_t& exec)
 {
-    auto it = g_run_graphs.find(k);
-    if (it != g_run_graphs.end()) {
-        exec = it->second;
+    auto it = g_run_graphs.index.find(k);
+    if (it != g_run_graphs.index.end()) {
+        g_run_graphs.lru.splice(g_run_graphs.lru.begin(), g_run_graphs.lru, it->second);
+        exec = it->second->second;
         return NGB_OK;
     }
     cudaStream_t cs;
@@ -105,7 +123,13 @@ int get_run_graph(const RunKey& k, cudaGraphExec_t& exec)
         set_error("graph instantiate failed: %s", cudaGetErrorString(e));
         return NGB_ERR_CUDA;
     }
-    g_run_graphs[k] = exec;
+    g_run_graphs.lru.emplace_front(k, exec);
+    g_run_graphs.index[k] = g_run_graphs.lru.begin();
+    while (int(g_run_graphs.lru.size()) > kMaxRunGraphs) {
+        cudaGraphExecDestroy(g_run_graphs.lru.back().second);
+        g_run_graphs.index.erase(g_run_graphs.lru.back().first);
+        g_run_graphs.lru.pop_back();
+    }
     return NGB_OK;
 }
 
@@ -269,9 +293,20 @@ int ngb_lbm_dense_run_host(const ngb_lbm_dense_desc* d, const void* host_in, voi
     const size_t bytes = size_t(d->q) * size_t(stride_of(d)) * storage_bytes(d->storage);
     cudaStream_t s = as_stream(stream);
     NGB_CUDA_TRY(cudaMemcpyAsync(fa, host_in, bytes, cudaMemcpyHostToDevice, s));
+    // After an odd count the result is fb, whose non-bulk nodes no step
+    // writes: give fb the uploaded state first (both ping-pong buffers start
+    // identical, as RunCavityTwoPop.cu:168-206 initialises them).
+    if (nsteps % 2 == 1) NGB_CUDA_TRY(cudaMemcpyAsync(fb, fa, bytes, cudaMemcpyDeviceToDevice, s));
     rc = ngb_lbm_dense_run(d, fa, fb, flags, nsteps, stream);
     if (rc) return rc;
     NGB_CUDA_TRY(cudaMemcpyAsync(host_out, nsteps % 2 == 0 ? fa : fb, bytes, cudaMemcpyDeviceToHost, s));
+    return NGB_OK;
+}
+
+int ngb_lbm_release_graphs(void)
+{
+    std::lock_guard<std::mutex> lock(g_run_mutex);
+    release_run_graphs_locked();
     return NGB_OK;
 }
 

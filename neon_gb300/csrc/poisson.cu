@@ -813,12 +813,17 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
         set_error("CG graph instantiate failed: %s", cudaGetErrorString(e));
         return NGB_ERR_CUDA;
     }
-    int32_t* flag = nullptr;
-    e = cudaMallocHost(&flag, sizeof(int32_t));
-    if (e != cudaSuccess) {
-        cudaGraphExecDestroy(exec);
-        set_error("cudaMallocHost failed: %s", cudaGetErrorString(e));
-        return NGB_ERR_CUDA;
+    // pinned 4-byte landing slot of the stop-flag polls: one per host thread,
+    // allocated on its first solve and kept
+    static thread_local int32_t* flag = nullptr;
+    if (!flag) {
+        e = cudaMallocHost(&flag, sizeof(int32_t));
+        if (e != cudaSuccess) {
+            flag = nullptr;
+            cudaGraphExecDestroy(exec);
+            set_error("cudaMallocHost failed: %s", cudaGetErrorString(e));
+            return NGB_ERR_CUDA;
+        }
     }
     int rc = NGB_OK;
     const int max_launches = (prm->max_iter + per - 1) / per + 1;
@@ -839,7 +844,6 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
         }
     }
     const auto t1 = std::chrono::steady_clock::now();
-    cudaFreeHost(flag);
     cudaGraphExecDestroy(exec);
     if (rc) return rc;
     CgState out;

@@ -16,6 +16,7 @@ training loop (the learned-preconditioner case of the Poisson benchmark).
   `stall` iterations the solve continues with Jacobi-PCG (ngb_cg_solve) from
   the current x.
 """
+import math
 import time
 
 import torch
@@ -285,6 +286,14 @@ def _fcg(precondition, ops, mask, b, x, tol, max_iter, refresh, stall, fallback,
                 break
         else:
             rel = float(scal[1].item()) ** 0.5 / bn
+        if not math.isfinite(rel):
+            # breakdown (p.q zero or not finite): Jacobi-PCG takes over from
+            # x if it is still finite, else from zero
+            used_fallback = True
+            if not bool(torch.isfinite(x).all()):
+                x.zero_()
+            rel = float("inf")
+            break
     if check_net is not None:
         check_net()
     torch.cuda.synchronize()

@@ -55,13 +55,19 @@ def test_single_rank_needs_no_process_group():
 
 def test_clock_summary_reads_nvidia_smi_samples():
     """The clocks record of the bench line: median SM clock, maximum, and the
-    throttle reasons that were active in any sample (nvidia-smi csv lines)."""
+    throttle reasons that were active in any sample (nvidia-smi csv lines,
+    timestamp first); with a window, only the samples taken inside it."""
     sys.path.insert(0, ROOT)
     import bench
-    lines = ["0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
-             "0, 1980, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active",
-             "0, 2070, 2070, 1200.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+    lines = ["2026/12/04 14:00:01.000, 0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+             "2026/12/04 14:00:01.050, 0, 1980, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active",
+             "2026/12/04 14:00:01.100, 0, 2070, 2070, 1200.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+             "2026/12/04 14:00:05.000, 0, 1200, 2070, 300.0, 0x0, Not Active, Active, Not Active, Not Active",
              "garbage line"]
     got = bench.ClockSampler.summarise(lines)
-    assert got == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert got == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["hw_thermal_slowdown", "sw_power_cap"],
+                   "samples": 4}
+    t0 = bench.ClockSampler.parse_time("2026/12/04 14:00:01.000")
+    got = bench.ClockSampler.summarise(lines, window=(t0 + 0.04, t0 + 0.2))
+    assert got == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 2}
     assert bench.ClockSampler.summarise([])["sm_mhz"] is None

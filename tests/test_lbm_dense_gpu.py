@@ -260,3 +260,33 @@ def test_cavity_profiles_match_oracle(ngb, orc, cuda):
     xg, yg = ngb.cavity_profiles(u, n, n, n, 0.1)
     xo, yo = ngb.cavity_profiles(uo, n, n, n, 0.1)
     assert xg == xo and yg == yo
+
+
+@pytest.mark.parametrize("steps", [3, 4, 37])
+def test_run_host_matches_device_run(ngb, cuda, steps):
+    """ngb_lbm_dense_run_host (host buffers in and out) returns the same
+    populations as the device-resident run, for odd counts too (the result
+    then lives in fb, whose wall nodes only the upload initialises)."""
+    import torch
+    n, q = 20, 19
+    desc, ref, _ = gpu_cavity(ngb, cuda, n, q, 1, steps)
+    desc2, start, _ = gpu_cavity(ngb, cuda, n, q, 1, 0)
+    host_in = start.cpu().pin_memory()
+    host_out = torch.full_like(host_in, float("nan")).pin_memory()
+    fa = torch.full_like(start, float("nan"))
+    fb = torch.full_like(start, float("nan"))  # garbage in fb: its walls must come from the upload
+    ngb.lbm_dense_run_host(desc2, host_in, host_out, fa, fb, steps)
+    torch.cuda.synchronize()
+    assert torch.equal(host_out, ref.cpu())
+
+
+def test_release_graphs_then_rerun(ngb, cuda):
+    """Dropping the cached step graphs changes nothing but the next call's set-up."""
+    import torch
+    _, a, _ = gpu_cavity(ngb, cuda, 16, 19, 1, 64)
+    assert ngb.lib().ngb_lbm_release_graphs() == 0
+    _, b, _ = gpu_cavity(ngb, cuda, 16, 19, 1, 64)
+    assert torch.equal(a, b)
+    # more distinct buffer pairs than the cache holds: old graphs are evicted, results unchanged
+    outs = [gpu_cavity(ngb, cuda, 16, 19, 1, 64)[1] for _ in range(10)]
+    assert all(torch.equal(o, a) for o in outs)
