@@ -10,11 +10,17 @@ lattice; MLUPS = N^3 * steps / time (walls counted, as Metrics.h:39-42).
 Prints ONE JSON line. `value` is device-timed with inputs resident in HBM;
 `e2e` is the same metric through the host-buffer C-ABI call
 (ngb_lbm_dense_run_host: H2D of the populations, the steps, D2H of the
-result, all inside the timed region).
+result, all inside the timed region). The same line carries the second half
+of the metric, Poisson seconds to 1e-8 at 512^3 (`poisson`: device
+Jacobi-PCG with its per-pass roofline, and the learned preconditioner's FCG
+with and without its network, training included), the 16-bit storage forms
+of the cavity (`storage_16bit`) and the bGrid flow-over-sphere case
+(`sphere`).
 
 `--impl reference` times the CPU restatement of the reference's per-cell
-D3Q19 FP32 arithmetic (the oracle port; the reference cannot be built
-here) on all host threads, on bounded z-slab samples of the same lattice.
+D3Q19 FP32 arithmetic (the oracle port, bit-exact to the reference's own CPU
+backend where that is built) on all host threads, on the full lattice of the
+same configuration.
 """
 import argparse
 import ctypes
@@ -33,7 +39,8 @@ sys.path.insert(0, ROOT)
 METRIC = "D3Q19 LBM MLUPS"
 UNIT = "MLUPS"
 BYTES_PER_UPDATE = {("d3q19", "f32"): 152, ("d3q19", "f64"): 304, ("d3q19", "f16off"): 76, ("d3q19", "bf16off"): 76,
-                    ("d3q27", "f32"): 216, ("d3q27", "f64"): 432, ("d3q27", "f16off"): 108, ("d3q27", "bf16off"): 108}
+                    ("d3q19", "f16sr"): 76, ("d3q27", "f32"): 216, ("d3q27", "f64"): 432, ("d3q27", "f16off"): 108,
+                    ("d3q27", "bf16off"): 108, ("d3q27", "f16sr"): 108}
 
 
 def parse():
@@ -45,10 +52,12 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=0, help="grid size (default: 384 for the LBM workloads, 512 for poisson/learned, 256 for unet)")
     ap.add_argument("--lattice", default="d3q19", choices=["d3q19", "d3q27"])
-    ap.add_argument("--storage", default="f32", choices=["f64", "f32", "f16off", "bf16off"])
+    ap.add_argument("--storage", default="f32", choices=["f64", "f32", "f16off", "bf16off", "f16sr"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--extra", action="store_true", help="also time the other storage/lattice forms")
+    ap.add_argument("--no-sections", action="store_true",
+                    help="cavity: leave out the poisson, storage_16bit and sphere sections of the line")
     ap.add_argument("--profiles", default="", help="cavity: write the centre-line velocity profiles into this directory")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson", "learned", "unet", "accuracy"],
                     help="cavity: dense LBM (default, the headline); sphere: bGrid flow over a sphere; "
@@ -216,56 +225,78 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(n, seconds=12.0, threads=0):
-    """Oracle port of the reference's D3Q19 FP32 per-cell arithmetic on a z-slab sample of the n^3 lattice."""
-    import numpy as np
-    import oracle
-    import neon_gb300 as ngb
-    L = oracle.lib()
-    threads = threads or L.orc_max_threads()
-    ulb = 0.1
-    omega = ngb.cavity_omega(n, ulb, 100.0)
-    # a slab of the full lattice: all of x and y, a few z planes (+2 walls)
-    nz = max(3, min(n, 2 + int(threads) * 2))
-    V = n * n * nz
-    flags = np.zeros(V, np.uint32)
-    L.orc_cavity_flags(n, n, nz, 19, flags.ctypes.data_as(ctypes.c_void_p))
-    a = np.zeros(19 * V, np.float32)
-    L.orc_cavity_init(n, n, nz, 19, 1, ulb, a.ctypes.data_as(ctypes.c_void_p))
-    b = a.copy()
-    P = lambda x: x.ctypes.data_as(ctypes.c_void_p)
-    us = L.orc_time_d3q19_f32(n, n, nz, 1, threads, omega, P(flags), P(a), P(b))
-    steps = max(1, int(seconds * 1e6 / max(us, 1.0)))
-    us = L.orc_time_d3q19_f32(n, n, nz, steps, threads, omega, P(flags), P(a), P(b))
-    mlups = V * steps / us
-    return mlups, threads, "D3Q19 FP32 reference arithmetic, %dx%dx%d slab of the %d^3 lattice, %d steps (%.1f s)" % (
-        n, n, nz, n, steps, us / 1e6)
+def cavity_config(n, lat, st, q, esz, world):
+    """The `config` object of the cavity line (identical for both arms)."""
+    return {"workload": "%s BGK lid-driven cavity, dense %d^3, %s SoA populations" % (lat.upper(), n, st),
+            "lattice": lat, "storage": st, "n": n, "lid_u": 0.1, "Re": 100.0,
+            "l2": "inputs larger than L2 (2 x %.1f GB population buffers)" % (q * n ** 3 * esz / 1e9),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+class OracleCavity:
+    """The oracle port of the reference's D3Q19 FP32 per-cell arithmetic on
+    the full n^3 lattice (host buffers, all host threads)."""
+
+    def __init__(self, n, threads=0):
+        import numpy as np
+        import oracle
+        import neon_gb300 as ngb
+        self.L = oracle.lib()
+        self.n = n
+        self.threads = threads or self.L.orc_max_threads()
+        self.omega = ngb.cavity_omega(n, 0.1, 100.0)
+        V = n ** 3
+        self.flags = np.zeros(V, np.uint32)
+        self.L.orc_cavity_flags(n, n, n, 19, self.flags.ctypes.data_as(ctypes.c_void_p))
+        self.a = np.zeros(19 * V, np.float32)
+        self.L.orc_cavity_init(n, n, n, 19, 1, 0.1, self.a.ctypes.data_as(ctypes.c_void_p))
+        self.b = self.a.copy()
+
+    def steps(self, k):
+        """Runs k steps; returns MLUPS (N^3 per step, as Metrics.h)."""
+        P = lambda x: x.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        n = self.n
+        us = self.L.orc_time_d3q19_f32(n, n, n, k, self.threads, self.omega, P(self.flags), P(self.a), P(self.b))
+        if k % 2:
+            self.a, self.b = self.b, self.a
+        return n ** 3 * k / us, us / 1e6
+
+
+def cpu_sample(n, steps=6):
+    """cpu_baseline of the cavity line: `steps` full-lattice steps of the oracle port."""
+    oc = OracleCavity(n)
+    oc.steps(2)  # warm-up (first touch of the buffers)
+    mlups, sec = oc.steps(steps)
+    return mlups, oc.threads, "D3Q19 FP32 reference arithmetic, full %d^3 lattice, %d steps (%.1f s)" % (n, steps, sec)
 
 
 def run_reference(args):
+    """The reference arm: the oracle port of the reference's D3Q19 FP32 step
+    (bit-exact to the reference's CPU backend where that is built from its
+    sources) on all host threads, the full lattice of the same config; each
+    of --steps timed steps is one full-lattice step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import oracle
-    L = oracle.lib()
-    threads = L.orc_max_threads()
-    # each step: one timed slab sample (~1 s) of the same workload
-    samples = []
-    for i in range(args.warmup + args.steps):
-        mlups, thr, desc = cpu_sample(args.n, seconds=0.5 if i < args.warmup else 1.0, threads=threads)
-        if i >= args.warmup:
-            samples.append(mlups)
-        if len(samples) >= min(args.steps, 20):
-            break
-    value = sum(samples) / len(samples)
-    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": args.gpus, "steps": len(samples),
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (lid-driven cavity set-up)",
-            "impl": "reference",
-            "config": {"workload": "D3Q19 BGK lid-driven cavity, dense %d^3, FP32 SoA" % args.n,
-                       "lattice": "d3q19", "storage": "f32", "n": args.n},
-            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": thr, "kind": "port",
-                             "sample": desc + "; reference not buildable here (needs spdlog/rapidjson/cmake)"},
+    n = args.n
+    oc = OracleCavity(n)
+    oc.steps(max(1, args.warmup))
+    per = []
+    for _ in range(args.steps):
+        mlups, sec = oc.steps(1)
+        per.append(sec)
+    total = sum(per)
+    value = n ** 3 * len(per) / (total * 1e6)
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": args.gpus, "steps": len(per),
+            "warmup": args.warmup, "ms_per_step": round(1e3 * total / len(per), 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (lid-driven cavity set-up, equilibrium start)", "impl": "reference",
+            "config": cavity_config(n, "d3q19", "f32", 19, 4, world),
+            "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": oc.threads, "kind": "port",
+                             "sample": "D3Q19 FP32 reference arithmetic, full %d^3 lattice, %d timed steps (%.1f s); "
+                                       "the oracle port equals the reference's own CPU backend bit for bit, but that "
+                                       "build needs the reference sources, which are not on this machine" % (
+                                           n, len(per), total)},
             "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -285,7 +316,7 @@ def run_ours(args):
     ulb, re_ = 0.1, 100.0
     omega = ngb.cavity_omega(n, ulb, re_)
     desc = ngb.lbm_dense_desc(n, n, n, q, st, omega, ngb.lid_wall_terms(q, ulb), box_cavity=True)
-    tdt = {"f64": torch.float64, "f32": torch.float32, "f16off": torch.float16, "bf16off": torch.bfloat16}[st]
+    tdt = TORCH_DTYPES[st](torch)
     V = n ** 3
     fa = torch.empty(q * V, dtype=tdt, device=dev)
     fb = torch.empty_like(fa)
@@ -300,17 +331,29 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     # ---------------- device-resident timing (CUDA events on the launching stream)
-    sampler = ClockSampler(local)
+    # The timed steps sit inside a clock window: the same step graph runs for
+    # about a second before and half a second after them, while nvidia-smi
+    # samples the GPU every 50 ms; the clocks record keeps the samples of
+    # that window (the timed region alone is a few milliseconds).
+    sampler = ClockSampler(dev)
     barrier()
     sampler.start()
-    time.sleep(0.3)
+    time.sleep(0.2)
+    ms_step_est = max(0.05, 152.0 * V / 6.0e12 * 1e3)
+    load_steps = 2 * max(1, int(1000.0 / ms_step_est) // 2)
+    w0 = time.time()
+    ngb.lbm_dense_run(desc, fa, fb, load_steps, stream=stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     ngb.lbm_dense_run(desc, fa, fb, args.steps, stream=stream)
     e1.record(stream)
-    e1.synchronize()
+    ngb.lbm_dense_run(desc, fa, fb, load_steps // 2 * 2, stream=stream)
+    stream.synchronize()
+    w1 = time.time()
     barrier()
-    clocks = sampler.stop()
+    clocks = sampler.stop(window=(w0, w1))
+    clocks["window"] = "the timed steps inside %.2f s of the same steps (%d before, %d after)" % (
+        w1 - w0, load_steps, load_steps // 2 * 2)
     ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
     per_step_ms = ms / args.steps
     value = whole_job_mlups(world, V, args.steps, ms)
@@ -319,14 +362,14 @@ def run_ours(args):
     # algorithmic bytes of the cells a step updates (the (n-2)^3 bulk cells; walls are not moved)
     achieved = bpu * (n - 2) ** 3 / (per_step_ms * 1e-3) / 1e9
     traffic = profiled_traffic("lbm_%s_%s_dense_%d.md" % (lat, st, n))
+    done_steps = args.warmup + (args.warmup % 2) + load_steps + args.steps + load_steps // 2 * 2
 
     # ---------------- centre-line velocity profiles (RunCavityTwoPop.cu:110-148)
     if args.profiles and rank == 0:
-        done = args.warmup + (args.warmup % 2) + args.steps
         u = torch.zeros(3 * V, dtype=torch.float64, device=dev)
-        ngb.lbm_dense_macroscopic(desc, fa if args.steps % 2 == 0 else fb, None, u, stream=stream)
+        ngb.lbm_dense_macroscopic(desc, fa if done_steps % 2 == 0 else fb, None, u, stream=stream)
         os.makedirs(args.profiles, exist_ok=True)
-        ngb.write_cavity_profiles(args.profiles, done, *ngb.cavity_profiles(u, n, n, n, ulb))
+        ngb.write_cavity_profiles(args.profiles, done_steps, *ngb.cavity_profiles(u, n, n, n, ulb))
         del u
 
     # ---------------- end to end through the host-buffer C-ABI call
@@ -348,11 +391,15 @@ def run_ours(args):
         e2e = {"value": round(whole_job_mlups(world, V, args.steps, ems), 2), "unit": UNIT,
                "h2d_bytes_per_step": nbytes // args.steps, "d2h_bytes_per_step": nbytes // args.steps,
                "note": "one H2D of the populations, %d steps, one D2H of the result per timed call" % args.steps}
+        del host_in, host_out
+
+    launches = args.steps * ngb.lbm_dense_kernels_per_step(desc)
+    del fa, fb
+    torch.cuda.empty_cache()
 
     extra = {}
     if args.extra and rank == 0:
-        for (l2, s2) in [("d3q19", "f16off"), ("d3q19", "bf16off"), ("d3q27", "f32"), ("d3q27", "f16off"),
-                         ("d3q19", "f64")]:
+        for (l2, s2) in [("d3q19", "bf16off"), ("d3q27", "f32"), ("d3q27", "f16off"), ("d3q19", "f64")]:
             extra["%s_%s" % (l2, s2)] = time_variant(ngb, torch, dev, n if s2 != "f64" else 256, l2, s2, args)
 
     if rank == 0:
@@ -364,17 +411,17 @@ def run_ours(args):
                 "warmup": args.warmup, "ms_per_step": round(per_step_ms, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if st != "f64" else "f64",
                 "data": "synthetic (lid-driven cavity set-up, equilibrium start)",
-                "config": {"workload": "%s BGK lid-driven cavity, dense %d^3, %s SoA populations" % (lat.upper(), n, st),
-                           "lattice": lat, "storage": st, "n": n, "lid_u": ulb, "Re": re_,
-                           "l2": "inputs larger than L2 (2 x %.1f GB population buffers)" % (q * V * fa.element_size() / 1e9),
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "config": cavity_config(n, lat, st, q, TORCH_ITEMSIZE[st], world),
                 "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "traffic": traffic,
                              "peak_kind": peak_kind, "bytes_per_update": bpu, "updated_cells": (n - 2) ** 3,
                              "launches_per_step": ngb.lbm_dense_kernels_per_step(desc),
                              "frac_of_nominal_8TBs": round(achieved / 8000.0, 4)},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps * ngb.lbm_dense_kernels_per_step(desc),
-                "clocks": clocks}
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+        if not args.no_sections and lat == "d3q19" and st == "f32":
+            line["storage_16bit"] = storage_16bit_section(ngb, torch, dev, n, args, per_step_ms)
+            line["poisson"] = poisson_section(args)
+            line["sphere"] = sphere_section(args)
         if extra:
             line["variants"] = extra
         print(json.dumps(line), flush=True)
@@ -382,7 +429,29 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def run_sphere(args):
+TORCH_DTYPES = {"f64": lambda t: t.float64, "f32": lambda t: t.float32, "f16off": lambda t: t.float16,
+                "bf16off": lambda t: t.bfloat16, "f16sr": lambda t: t.float16}
+TORCH_ITEMSIZE = {"f64": 8, "f32": 4, "f16off": 2, "bf16off": 2, "f16sr": 2}
+
+
+def storage_16bit_section(ngb, torch, dev, n, args, f32_ms):
+    """The 16-bit offset storage forms of the same cavity (g = f - w stored in
+    16 bits, FP32 collision): MLUPS, ratio to the FP32 step timed above, and
+    their roofline (76 B per update). f16sr stores with stochastic rounding
+    (the form that meets the accuracy target), f16off rounds to nearest."""
+    out = {}
+    peak, kind = measured_peaks()
+    for st in ("f16sr", "f16off"):
+        v = time_variant(ngb, torch, dev, n, "d3q19", st, args)
+        v["speedup_vs_f32"] = round(f32_ms / v["ms_per_step"], 3)
+        v["roofline_frac"] = round(v["achieved_gbs"] / peak, 4)
+        out[st] = v
+    out["peak_kind"] = kind
+    out["target"] = ">= 1.7x the FP32 MLUPS at <= 1e-3 velocity error vs FP64 (accuracy: --workload accuracy)"
+    return out
+
+
+def run_sphere(args, emit=True):
     """Flow over a sphere on bGrid (8^3 blocks), 512x256x256 box: MLUPS per
     active cell for the chosen storage, and the drag coefficient after
     `--sim-steps` steps against an FP64 run of the same case."""
@@ -462,71 +531,75 @@ def run_sphere(args):
             "drag": {"steps": args.sim_steps, "cd": cd, "cd_f64": cd64,
                      "rel_err": (abs(cd - cd64) / abs(cd64)) if cd is not None and cd64 else None},
             "gpu_launches": args.steps}
+    del grid, flags, act, cls
+    torch.cuda.empty_cache()
+    if not emit:
+        return line
     print(json.dumps(line), flush=True)
 
 
-def run_poisson(args):
-    """Poisson -lap(u) = f, zero Dirichlet box, 8 seeded Gaussians (sigma 8):
-    seconds and iterations of the device Jacobi-PCG (FP32 fields, FP64
-    reductions and solution, true residual every 50 iterations) to 1e-8."""
+def poisson_problem(n, dev):
+    """Config 3's Poisson case at n^3: zero Dirichlet box, f = 8 seeded Gaussians (sigma 8), FP32 fields."""
     import torch
     import neon_gb300 as ngb
-    dev = torch.device("cuda", 0)
-    ngb.lib()
-    n = args.n
     d = ngb.poisson_desc(n, n, n, "f32", 1.0)
     c, a = ngb.gaussian_sources(n, n, n, 2024)
     b = torch.empty(n ** 3, dtype=torch.float32, device=dev)
     ngb.poisson_rhs(d, torch.from_numpy(c).to(dev), torch.from_numpy(a).to(dev), 8.0, b)
+    return d, b
+
+
+def jacobi_pcg_run(d, b, n, dev, reps=1):
+    """Device Jacobi-PCG to 1e-8 (FP32 fields, FP64 reductions and solution,
+    true residual every 50 iterations): the best of `reps` solves, with the
+    per-pass roofline (pass A 16 B/DOF, pass B 24 B/DOF per launch) from
+    CUDA events on 20 launches of each pass."""
+    import torch
+    import neon_gb300 as ngb
     ws = ngb.cg_workspace(d, dev)
     results = []
-    for rep in range(max(1, args.steps)):
+    for _ in range(max(1, reps)):
         x = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
         torch.cuda.synchronize()
-        r = ngb.cg_solve(d, b, x, ws, tol=1e-8, max_iter=20000, refresh_every=50, check_every=50, jacobi=True)
-        results.append(r)
+        results.append(ngb.cg_solve(d, b, x, ws, tol=1e-8, max_iter=20000, refresh_every=50, check_every=50,
+                                    jacobi=True))
     best = min(results, key=lambda r: r["seconds"])
-    it = best["iterations"]
+    x0 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
+    ms_a, ms_b = ngb.cg_time_passes(d, b, x0, ws, reps=20)
     peak, kind = measured_peaks()
-    per_it = best["seconds"] / max(it, 1)
-    achieved = 40.0 * n ** 3 / per_it / 1e9
-    line = {"metric": "Poisson seconds to 1e-8 (Jacobi-PCG)", "value": round(best["seconds"], 4), "unit": "s",
-            "n_gpus": 1, "steps": len(results), "warmup": 0, "higher_is_better": False, "dtype": "f32",
-            "data": "synthetic (8 seeded Gaussians, sigma 8)",
-            "config": {"workload": "Poisson 7-point, zero Dirichlet, %d^3, FP32 fields / FP64 reductions" % n,
-                       "iterations": it, "rel_residual": best["rel_residual"], "refreshes": best["refreshes"],
-                       "converged": best["converged"]},
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "peak_kind": kind,
-                         "bytes_per_dof_iteration": 40,
-                         "note": "whole-solve average incl. polls and refreshes"}}
-    print(json.dumps(line), flush=True)
+    it = best["iterations"]
+    whole = 40.0 * n ** 3 * it / best["seconds"] / 1e9
+    passes = {"pass_a": {"ms": round(ms_a, 4), "bytes_per_dof": 16,
+                         "achieved_gbs": round(16.0 * n ** 3 / (ms_a * 1e-3) / 1e9, 1)},
+              "pass_b": {"ms": round(ms_b, 4), "bytes_per_dof": 24,
+                         "achieved_gbs": round(24.0 * n ** 3 / (ms_b * 1e-3) / 1e9, 1)}}
+    for v in passes.values():
+        v["frac"] = round(v["achieved_gbs"] / peak, 4)
+    out = {"seconds": round(best["seconds"], 4), "iterations": it, "rel_residual": best["rel_residual"],
+           "converged": best["converged"], "refreshes": best["refreshes"], "solves": len(results),
+           "roofline": {"bound": "hbm", "peak": peak, "peak_kind": kind, "unit": "GB/s",
+                        "whole_solve_achieved": round(whole, 1), "whole_solve_frac": round(whole / peak, 4),
+                        "bytes_per_dof_iteration": 40, **passes},
+           "gpu_launches_per_iteration": 4}
+    return out, ws
 
 
-def run_learned(args):
-    """Learned preconditioner: a 3-level U-Net (16/32/64 channels, BF16 tensor-core
-    convolutions) trained on residual/error pairs that CG itself produces on
-    seeded k^-2 Gaussian random fields at --train-n, then used inside flexible
-    CG (with Jacobi-PCG fallback on stagnation) on the Gaussian-source Poisson
-    problem at --n, against device Jacobi-PCG on the same problem; both to a
-    1e-8 relative true residual. For --n > --train-n the network is the
-    coarsest-level solve of a V-cycle (damped-Jacobi smoothing and
-    full-weighting / trilinear transfers on the levels between --n and
-    --train-n); the same cycle without the network is timed beside it. For
-    --n == --train-n the network preconditions the fine grid directly.
-    `value` is the FCG solve time (seconds)."""
+def learned_fcg_run(args, n, dev, b, ws, pcg_seconds):
+    """Learned preconditioner: a 3-level U-Net (16/32/64 channels, BF16
+    tensor-core convolutions) trained on residual/error pairs that CG itself
+    produces on seeded k^-2 Gaussian random fields at --train-n, then used
+    inside flexible CG (Jacobi-PCG fallback on stagnation) to a 1e-8 relative
+    true residual. For n > --train-n the network is the coarsest-level solve
+    of a V-cycle (damped-Jacobi smoothing, full-weighting / trilinear
+    transfers); the same cycle without the network is timed beside it."""
     import torch
     import neon_gb300 as ngb
     from neon_gb300 import fcg
     from neon_gb300.learned import UNet
-    dev = torch.device("cuda", 0)
-    ngb.lib()
-    n = args.n
-    # --- training (or loading) the network
     net = UNet(seed=0, device=dev)
     train = {"pairs": 0, "seconds": 0.0, "loss_first": None, "loss_last": None}
     if args.weights:
-        net.load_state_dict(torch.load(args.weights))
+        net.load_weights(args.weights)
         train["weights"] = os.path.basename(args.weights)
     else:
         captures = (2, 5, 10, 20, 40, 80, 120, 160, 200, 250)
@@ -540,41 +613,35 @@ def run_learned(args):
         t2 = time.perf_counter()
         k = max(1, len(losses) // 10)
         train.update(pairs=len(pairs), seconds=round(t2 - t0, 1), data_seconds=round(t1 - t0, 1),
+                     train_n=args.train_n, epochs=args.epochs,
                      loss_first=round(sum(losses[:k]) / k, 4), loss_last=round(sum(losses[-k:]) / k, 4))
         del pairs
         torch.cuda.empty_cache()
         if args.save_weights:
-            torch.save({k2: v.cpu() for k2, v in net.w.items()}, args.save_weights)
-    # --- the Poisson problem of the Jacobi-PCG benchmark
-    d = ngb.poisson_desc(n, n, n, "f32", 1.0)
-    c, a = ngb.gaussian_sources(n, n, n, 2024)
-    b = torch.empty(n ** 3, dtype=torch.float32, device=dev)
-    ngb.poisson_rhs(d, torch.from_numpy(c).to(dev), torch.from_numpy(a).to(dev), 8.0, b)
-    ws = ngb.cg_workspace(d, dev)
-    x = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
-    pcg = ngb.cg_solve(d, b, x, ws, tol=1e-8, max_iter=20000, refresh_every=50, check_every=50, jacobi=True)
-    # FCG preconditioned by the V-cycle whose coarsest level (--train-n) is the network
+            net.save_weights(args.save_weights)
     levels = max(0, int(round(math.log2(n / args.train_n))))
     if args.train_n << levels != n:
         raise SystemExit("learned: --n must be --train-n times a power of two")
-    vc = fcg.VCycle(n, levels, net, device=dev) if levels > 0 else None
-    if vc is not None:
-        vc(b)  # warm-up (network buffers at the coarsest size)
+    plain = None
+    if levels > 0:
+        # the solve through the C ABI (ngb_learned_solve): V-cycle, network, FCG and FP64 true residual in the library
+        solver = ngb.LearnedSolver(n, levels, net.flat_weights())
+        z = torch.empty_like(b)
+        solver.precondition(b, z)  # warm-up (first launches of every kernel)
         torch.cuda.synchronize()
+        del z
         x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
-        res = fcg.fcg_solve_vcycle(vc, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
-        # the same cycle without the network (coarsest correction zero)
+        res = solver.solve(b, x2, tol=1e-8, max_iter=2000, refresh_every=10, stall=30, fallback=True)
+        solver.close()
         x3 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
         plain = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, coarse="none", device=dev), b, x3, tol=1e-8, max_iter=4000,
                                      fallback=True, ws=ws)
+        del x3
     else:
         net.forward(b)
         torch.cuda.synchronize()
         x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
         res = fcg.fcg_solve(net, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
-        plain = None
-    agree = float((x2 - x).norm() / x.norm())
-    # U-Net forward cost at the size it runs at (device time)
     nn_ = n >> levels
     rc = b[:nn_ ** 3].clone()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -584,22 +651,91 @@ def run_learned(args):
     e1.record()
     e1.synchronize()
     fwd_ms = e0.elapsed_time(e1) / 3
-    cfg = {"workload": "Poisson 7-point, zero Dirichlet, %d^3; FCG(1) with a V-cycle of %d damped-Jacobi levels whose "
-                       "coarsest (%d^3) solve is the U-Net 16/32/64 trained at %d^3" % (n, levels, nn_, args.train_n),
-           "fcg_iterations": res["iterations"], "fcg_fallback": res["fallback"],
-           "fallback_iterations": res["fallback_iterations"], "fcg_rel_residual": res["rel_residual"],
-           "converged": res["converged"], "pcg_seconds": round(pcg["seconds"], 4),
-           "pcg_iterations": pcg["iterations"], "speedup_vs_pcg": round(pcg["seconds"] / res["seconds"], 3),
-           "solution_rel_diff": agree, "unet_forward_ms": round(fwd_ms, 3),
+    out = {"seconds": round(res["seconds"], 4), "iterations": res["iterations"], "fallback": res["fallback"],
+           "fallback_iterations": res["fallback_iterations"], "rel_residual": res["rel_residual"],
+           "converged": res["converged"], "speedup_vs_jacobi_pcg": round(pcg_seconds / res["seconds"], 3),
+           "structure": "FCG(1) with a V-cycle of %d damped-Jacobi levels whose coarsest (%d^3) solve is the U-Net "
+                        "16/32/64 trained at %d^3" % (levels, nn_, args.train_n),
+           "path": "C ABI ngb_learned_solve" if levels > 0 else "Python orchestration of the library kernels",
+           "unet_forward_ms": round(fwd_ms, 3),
            "unet_forward_tflops": round(net.flops_forward(nn_) / fwd_ms / 1e9, 1), "training": train}
     if plain is not None:
-        cfg["without_network"] = {"seconds": round(plain["seconds"], 4), "iterations": plain["iterations"],
-                                  "fallback": plain["fallback"], "fallback_iterations": plain["fallback_iterations"],
-                                  "converged": plain["converged"]}
-    line = {"metric": "Poisson seconds to 1e-8: learned FCG vs Jacobi-PCG", "value": round(res["seconds"], 4), "unit": "s",
-            "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "dtype": "bf16",
-            "data": "synthetic (8 seeded Gaussians, sigma 8; training on seeded k^-2 fields)", "config": cfg}
+        out["without_network"] = {"seconds": round(plain["seconds"], 4), "iterations": plain["iterations"],
+                                  "fallback": plain["fallback"], "converged": plain["converged"],
+                                  "speedup_vs_jacobi_pcg": round(pcg_seconds / plain["seconds"], 3)}
+        out["network_gain"] = round(plain["seconds"] / res["seconds"], 3)
+    return out, x2
+
+
+def poisson_cpu_baseline(n=128):
+    """The oracle's Jacobi-PCG (FP32 fields, FP64 dots, true residual every
+    50 iterations) to 1e-8 at n^3 on one host core (the reference's CPU
+    backend runs its grid loops serially)."""
+    from oracle import cpu_baselines
+    import oracle
+    r = cpu_baselines.poisson_pcg(oracle.lib(), n)
+    return {"value": r["seconds"], "unit": "s", "cores": 1, "kind": "port",
+            "sample": "Jacobi-PCG to 1e-8 at %d^3 (%d iterations), the oracle's CG restatement" % (n, r["iterations"])}
+
+
+def poisson_section(args, n=512):
+    """Poisson -lap(u) = f at n^3 to 1e-8: Jacobi-PCG and the learned FCG, both on the device."""
+    import torch
+    dev = torch.device("cuda", 0)
+    d, b = poisson_problem(n, dev)
+    pcg, ws = jacobi_pcg_run(d, b, n, dev, reps=1)
+    learned, _ = learned_fcg_run(args, n, dev, b, ws, pcg["seconds"])
+    del ws, b
+    torch.cuda.empty_cache()
+    out = {"metric": "Poisson seconds to 1e-8 (512^3, zero Dirichlet, 8 seeded Gaussians)", "n": n,
+           "jacobi_pcg": pcg, "learned_fcg": learned,
+           "speedup_learned_vs_jacobi_pcg": learned["speedup_vs_jacobi_pcg"]}
+    if not args.no_cpu:
+        out["cpu_baseline"] = poisson_cpu_baseline()
+    return out
+
+
+def run_poisson(args):
+    """Standalone Jacobi-PCG line (config 3) at --n."""
+    import torch
+    import neon_gb300 as ngb
+    dev = torch.device("cuda", 0)
+    ngb.lib()
+    n = args.n
+    d, b = poisson_problem(n, dev)
+    pcg, _ = jacobi_pcg_run(d, b, n, dev, reps=args.steps)
+    line = {"metric": "Poisson seconds to 1e-8 (Jacobi-PCG)", "value": pcg["seconds"], "unit": "s",
+            "n_gpus": 1, "steps": pcg["solves"], "warmup": 0, "higher_is_better": False, "dtype": "f32",
+            "data": "synthetic (8 seeded Gaussians, sigma 8)",
+            "config": {"workload": "Poisson 7-point, zero Dirichlet, %d^3, FP32 fields / FP64 reductions" % n},
+            "jacobi_pcg": pcg, "roofline": pcg["roofline"]}
     print(json.dumps(line), flush=True)
+
+
+def run_learned(args):
+    """Standalone learned-preconditioner line (config 4) at --n; `value` is the FCG solve time."""
+    import torch
+    import neon_gb300 as ngb
+    dev = torch.device("cuda", 0)
+    ngb.lib()
+    n = args.n
+    d, b = poisson_problem(n, dev)
+    pcg, ws = jacobi_pcg_run(d, b, n, dev, reps=1)
+    learned, x2 = learned_fcg_run(args, n, dev, b, ws, pcg["seconds"])
+    line = {"metric": "Poisson seconds to 1e-8: learned FCG vs Jacobi-PCG", "value": learned["seconds"], "unit": "s",
+            "n_gpus": 1, "steps": 1, "warmup": 1, "higher_is_better": False, "dtype": "bf16",
+            "data": "synthetic (8 seeded Gaussians, sigma 8; training on seeded k^-2 fields)",
+            "config": {"workload": "Poisson 7-point, zero Dirichlet, %d^3" % n}, "jacobi_pcg": pcg,
+            "learned_fcg": learned}
+    print(json.dumps(line), flush=True)
+
+
+def sphere_section(args):
+    """Config 2 on bGrid (FP16 storage, the config's own): MLUPS over active cells and roofline."""
+    import copy
+    a2 = copy.copy(args)
+    a2.storage, a2.lattice, a2.steps, a2.warmup, a2.sim_steps, a2.scale = "f16off", "d3q19", 200, 10, 0, 1
+    return run_sphere(a2, emit=False)
 
 
 def bf16_peak():
@@ -668,9 +804,9 @@ def run_accuracy(args):
     steps = args.sim_steps or 2000
     ulb, re_ = 0.1, 100.0
     V = n ** 3
-    tdts = {"f64": torch.float64, "f32": torch.float32, "f16off": torch.float16, "bf16off": torch.bfloat16}
+    tdts = {k: v(torch) for k, v in TORCH_DTYPES.items()}
     u_ref, out = None, {}
-    for st in ("f64", "f32", "f16off", "bf16off"):
+    for st in ("f64", "f32", "f16sr", "f16off", "bf16off"):
         desc = ngb.lbm_dense_desc(n, n, n, q, st, ngb.cavity_omega(n, ulb, re_), ngb.lid_wall_terms(q, ulb))
         fa = torch.empty(q * V, dtype=tdts[st], device=dev)
         fb = torch.empty_like(fa)
@@ -695,12 +831,13 @@ def run_accuracy(args):
             err = float(du.norm() / u_ref.view(3, n, n, n)[:, 1:-1, 1:-1, 1:-1].norm())
             out[st] = {"mlups": round(V / (ms * 1e3), 1), "velocity_l2_rel_err_vs_f64": err}
             del u
-    line = {"metric": "%s cavity velocity L2 error vs FP64" % args.lattice.upper(), "value": out["f16off"]["velocity_l2_rel_err_vs_f64"],
+    line = {"metric": "%s cavity velocity L2 error vs FP64" % args.lattice.upper(), "value": out["f16sr"]["velocity_l2_rel_err_vs_f64"],
             "unit": "relative L2", "n_gpus": 1, "steps": steps, "warmup": 0, "higher_is_better": False, "dtype": "f32",
             "data": "synthetic (lid-driven cavity set-up, equilibrium start)",
             "config": {"workload": "%s BGK lid-driven cavity, dense %d^3, %d steps" % (args.lattice.upper(), n, steps),
                        "lid_u": ulb, "Re": re_, "forms": out,
-                       "f16_speedup_vs_f32": round(out["f16off"]["mlups"] / out["f32"]["mlups"], 3)}}
+                       "value_form": "f16sr (FP16 offsets, stochastic rounding)",
+                       "f16_speedup_vs_f32": round(out["f16sr"]["mlups"] / out["f32"]["mlups"], 3)}}
     print(json.dumps(line), flush=True)
 
 
@@ -708,7 +845,7 @@ def time_variant(ngb, torch, dev, n, lat, st, args):
     q = 19 if lat == "d3q19" else 27
     ulb = 0.1
     desc = ngb.lbm_dense_desc(n, n, n, q, st, ngb.cavity_omega(n, ulb, 100.0), ngb.lid_wall_terms(q, ulb))
-    tdt = {"f64": torch.float64, "f32": torch.float32, "f16off": torch.float16, "bf16off": torch.bfloat16}[st]
+    tdt = TORCH_DTYPES[st](torch)
     V = n ** 3
     fa = torch.empty(q * V, dtype=tdt, device=dev)
     fb = torch.empty_like(fa)

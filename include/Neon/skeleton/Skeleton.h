@@ -18,6 +18,7 @@
 // launches as the standard one.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdlib>
 #include <fstream>
@@ -95,9 +96,13 @@ class Skeleton {
             sig.insert(sig.end(), launches.back().signature.begin(), launches.back().signature.end());
         }
         cudaStream_t s = mBackend.stream(streamIdx);
+        // the "Skeleton" range of Skeleton.h:56-65, around the graph launch
+        nvtxRangePushA("Skeleton");
         if (!mExec || sig != mSignature) capture(launches);
         mSignature = std::move(sig);
-        NEON_CUDA_CHECK(cudaGraphLaunch(mExec, s));
+        const cudaError_t e = cudaGraphLaunch(mExec, s);
+        nvtxRangePop();
+        NEON_CUDA_CHECK(e);
     }
 
     void ioToDot(const std::string& fname, const std::string& graphname = "", bool = false) const

@@ -40,23 +40,51 @@ int ngb_version(void);
 /* How populations are held in HBM. The *_OFF forms hold g_q = f_q - w_q:
  * BF16OFF as bf16(g_q); F16OFF as fp16(2^14 g_q) (NGB_F16OFF_SCALE), which
  * keeps the small offsets of slow flow regions out of FP16's subnormal range
- * (2^14 is exact, so the FP32 collision computes the same values either way). */
+ * (2^14 is exact, so the FP32 collision computes the same values either way).
+ * F16SR holds the same fp16(2^14 g_q) values but stores them with stochastic
+ * rounding: the FP32 result is rounded up in magnitude with probability
+ * equal to its remainder, so the rounding errors of a quasi-steady flow do
+ * not add up to a systematic drift (round-to-nearest repeats the same error
+ * every step). The random bits are a hash of the cell, the population and
+ * the step seed: for cell index i (x + nx (y + ny z)), population q and seed s,
+ *   h  = mix32(lo32(i >> 1) ^ (hi32(i >> 1) * 0x9E3779B1) ^ (s * 0x85EBCA77)),
+ *   hq = (h ^ (q * 0x9E3779B9)) * 0xC2B2AE35,
+ *   r  = i odd ? (hq >> 6) & 0x1FFF : hq >> 19        (13 bits)
+ * with mix32(x) = x ^= x >> 16, x *= 0x7FEB352D, x ^= x >> 15,
+ * x *= 0x846CA68B, x ^= x >> 16 (Wellons' "lowbias32"); the stored value is
+ * fp16_round_toward_zero(bits_f32(2^14 g) + r). ngb_lbm_dense_step uses
+ * s = dither_seed; the t-th step of ngb_lbm_dense_run uses
+ * s = dither_seed + (t mod 32). */
 #define NGB_F16OFF_SCALE 16384.0f
 typedef enum {
     NGB_STORE_F64 = 0,
     NGB_STORE_F32 = 1,
     NGB_STORE_F16OFF = 2,
-    NGB_STORE_BF16OFF = 3
+    NGB_STORE_BF16OFF = 3,
+    NGB_STORE_F16SR = 4
 } ngb_storage;
 
 /* Cell classification, values of benchmarks/lbm-lid-driven-cavity-flow/src/CellType.h:5-11
- * plus OUTLET (zero-gradient outflow node, new). */
+ * plus OUTLET (zero-gradient outflow node, new) and the Zou-He pressure /
+ * velocity boundary nodes of benchmarks/lbm-flow-over-sphere/src/CellType.h
+ * (PRESSURE, VELOCITY; D3Q19 on dense grids with a flag array, FP64 and FP32
+ * storage). A Zou-He node lies on a face of the box and is updated every step:
+ * with n its inward normal (the first face it lies on, in the order x = 0,
+ * x = nx-1, y = 0, y = ny-1, z = 0, z = nz-1), the 5 populations with
+ * c.n = +1 are unknown; M and K are the sums of the known populations with
+ * c.n = 0 and c.n = -1; PRESSURE nodes take rho = zouhe_rho, u.n =
+ * 1 - (M + 2K) / rho and zero tangential velocity, VELOCITY nodes take u =
+ * zouhe_u and rho = (M + 2K) / (1 - u.n); the unknowns are
+ * f_q = f_opp(q) + eq_q - eq_opp(q) (non-equilibrium bounce-back, Zou & He
+ * 1997) and the node collides with eq(rho, u) of those boundary values. */
 typedef enum {
     NGB_CELL_BOUNCEBACK = 0,
     NGB_CELL_MOVINGWALL = 1,
     NGB_CELL_BULK = 2,
     NGB_CELL_UNDEFINED = 3,
-    NGB_CELL_OUTLET = 4
+    NGB_CELL_OUTLET = 4,
+    NGB_CELL_PRESSURE = 5,
+    NGB_CELL_VELOCITY = 6
 } ngb_cell_class;
 
 /* Packed cell flag (uint32 per cell): bits 0..26 = wall-neighbour mask
@@ -84,6 +112,10 @@ typedef struct ngb_lbm_dense_desc {
      * -6 w_k u_lb (c_k . u_lid) on the lid, 0 elsewhere). Rounded to the
      * storage precision (F64/F32) or kept in FP32 (*_OFF) by the library. */
     double wall_term[2][27];
+    double   zouhe_rho;   /* density of the PRESSURE nodes */
+    double   zouhe_u[3];  /* velocity of the VELOCITY nodes */
+    uint32_t dither_seed; /* F16SR: seed of the stochastic rounding (see ngb_storage) */
+    uint32_t pad;
 } ngb_lbm_dense_desc;
 
 /* One pull stream-collide step over every bulk cell: fout <- step(fin).
@@ -101,6 +133,18 @@ int ngb_lbm_dense_step(const ngb_lbm_dense_desc* desc, const void* fin, void* fo
  * used graphs and destroys older ones. Replaces the host loop of
  * RunCavityTwoPop.cu:257-273 over LbmIterationD3Q19::run (LbmIteration.h:56-61). */
 int ngb_lbm_dense_run(const ngb_lbm_dense_desc* desc, void* fa, void* fb, const uint32_t* flags, int32_t nsteps, void* stream);
+
+/* Checkpoint / resume (no reference counterpart; the reference exports
+ * VTK/VTI only, FieldBase.h:137). save writes the population buffer f (the
+ * newest state, q * plane_stride elements) after a header with the lattice
+ * dims, q, storage, plane stride, omega and the caller's step number
+ * ("NGBLBM01", little-endian). load checks the header against desc, fills fa
+ * and, when fb is non-NULL, fb with the saved state (both ping-pong buffers
+ * equal, as a fresh run starts, so the continued run is bit-identical) and
+ * returns the step number. Both are synchronous (file IO through a pinned
+ * 64 MiB staging buffer). */
+int ngb_lbm_dense_save(const char* path, const ngb_lbm_dense_desc* desc, const void* f, int64_t step, void* stream);
+int ngb_lbm_dense_load(const char* path, const ngb_lbm_dense_desc* desc, void* fa, void* fb, int64_t* step, void* stream);
 
 /* Destroys every step graph ngb_lbm_dense_run keeps (a graph still running
  * is freed when its launch completes). Call before freeing population
@@ -361,6 +405,16 @@ size_t ngb_cg_workspace_bytes(const ngb_poisson_desc* desc);
 int ngb_cg_solve(const ngb_poisson_desc* desc, const void* b, double* x, void* workspace, size_t workspace_bytes,
                  const ngb_cg_params* params, ngb_cg_result* result, void* stream);
 
+/* Measurement aid (no reference counterpart): CUDA-event time per launch of
+ * the solver's two fused passes, each launched `reps` times back to back
+ * from the state after x's initial residual (pass A: p = z + beta p,
+ * s = A p, <p, s>; pass B: x += alpha p, r -= alpha s, <r, z>, <r, r>).
+ * ms[0] = pass A, ms[1] = pass B (milliseconds per launch). Overwrites the
+ * workspace and adds the timed increments to x's low part only (x itself is
+ * read, not changed). Synchronous. */
+int ngb_cg_time_passes(const ngb_poisson_desc* desc, const void* b, double* x, void* workspace, size_t workspace_bytes,
+                       int32_t reps, float* ms, void* stream);
+
 /* Right-hand side of the Poisson case: f = sum of 8 Gaussians
  * A_k exp(-|x - c_k|^2 / (2 sigma^2)), centres (8x3) and amplitudes from the
  * caller (see ngb_gaussian_sources), written in `field` precision. */
@@ -469,6 +523,57 @@ int ngb_mg_restrict(const ngb_poisson_desc* fine, const void* res, void* rc, dou
 /* u += P ec on the fine Free nodes, P the trilinear interpolation from the
  * coarse grid (dims/2) that ngb_mg_restrict's weights are the transpose of. */
 int ngb_mg_prolong_add(const ngb_poisson_desc* fine, const void* ec, void* u, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Learned-preconditioner Poisson solver (no reference counterpart:
+ * libNeonSolver has plain CG only, CG.h:70-76; this is its learned sibling
+ * with the same solve(b, x) -> result shape). FCG(1) on A x = b for the
+ * zero-Dirichlet n^3 box (A as ngb_laplacian_apply, h = 1), preconditioned
+ * by a V-cycle of `levels` damped-Jacobi levels whose coarsest-level solve is
+ * the 3-level U-Net (16/32/64 channels, BF16 tensor-core convolutions) on the
+ * (n / 2^levels)^3 grid; x accumulates in FP64, the true residual b - A x is
+ * recomputed in FP64 every refresh_every iterations, and Jacobi-PCG
+ * (ngb_cg_solve) takes over from x when that residual fails to halve over
+ * `stall` iterations or the iteration breaks down. The solver owns its
+ * device buffers. */
+typedef struct ngb_learned_solver ngb_learned_solver;
+
+typedef struct ngb_learned_params {
+    double  tol;           /* stop when |b - A x| / |b| <= tol (FP64 true residual) */
+    int32_t max_iter;      /* FCG iterations before giving up (fallback excluded) */
+    int32_t refresh_every; /* true-residual period, >= 1 (10 in the benchmark) */
+    int32_t stall;         /* fallback when the true residual does not halve over this many iterations */
+    int32_t fallback;      /* 1: Jacobi-PCG takes over on stagnation or breakdown */
+} ngb_learned_params;
+
+typedef struct ngb_learned_result {
+    int32_t iterations;          /* FCG iterations */
+    int32_t fallback;            /* 1 if Jacobi-PCG took over */
+    int32_t fallback_iterations; /* its iterations */
+    int32_t converged;
+    double  rel_residual;        /* final true relative residual */
+    double  seconds;             /* wall time of the solve */
+} ngb_learned_result;
+
+/* Number of FP32 weights of the network (10 layers [cout][27][cin] in the
+ * order c0a c0b c1a c1b c2a c2b c1c c1d c0c c0d). */
+int64_t ngb_unet_weight_count(void);
+/* Weight file: "NGBUNET1", version 1, 10 layers of (cout, cin, BF16 values).
+ * write rounds FP32 to BF16 (nearest even); read returns exact FP32 values. */
+int ngb_unet_write_weights(const char* path, const float* weights, int64_t count);
+int ngb_unet_read_weights(const char* path, float* weights, int64_t count);
+
+/* Creates the solver for an n^3 grid: n a multiple of 2^levels, the coarsest
+ * grid n / 2^levels >= 8 and a multiple of 4 (two poolings); weights: host
+ * FP32 array of ngb_unet_weight_count() values. Allocates device memory. */
+int ngb_learned_create(int32_t n, int32_t levels, const float* weights, int64_t count, ngb_learned_solver** solver);
+int ngb_learned_destroy(ngb_learned_solver* solver);
+/* z = M(r): one application of the preconditioner (FP32 n^3 fields). */
+int ngb_learned_precondition(ngb_learned_solver* solver, const float* r, float* z, void* stream);
+/* Solves A x = b (b FP32, zero on the faces; x FP64 initial guess and
+ * solution). Synchronous; reads one double from the device per iteration. */
+int ngb_learned_solve(ngb_learned_solver* solver, const float* b, double* x, const ngb_learned_params* params,
+                      ngb_learned_result* result, void* stream);
 
 #ifdef __cplusplus
 }

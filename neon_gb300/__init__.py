@@ -14,10 +14,11 @@ from . import build as _build
 LIB_PATH = _build.LIB_PATH
 
 NGB_OK = 0
-STORE_F64, STORE_F32, STORE_F16OFF, STORE_BF16OFF = 0, 1, 2, 3
-STORAGE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "f16off": STORE_F16OFF, "bf16off": STORE_BF16OFF}
+STORE_F64, STORE_F32, STORE_F16OFF, STORE_BF16OFF, STORE_F16SR = 0, 1, 2, 3, 4
+STORAGE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "f16off": STORE_F16OFF, "bf16off": STORE_BF16OFF,
+                 "f16sr": STORE_F16SR}
 STORAGE_BYTES = {STORE_F64: 8, STORE_F32: 4, STORE_F16OFF: 2, STORE_BF16OFF: 2}
-CELL_BOUNCEBACK, CELL_MOVINGWALL, CELL_BULK, CELL_UNDEFINED, CELL_OUTLET = 0, 1, 2, 3, 4
+CELL_BOUNCEBACK, CELL_MOVINGWALL, CELL_BULK, CELL_UNDEFINED, CELL_OUTLET, CELL_PRESSURE, CELL_VELOCITY = 0, 1, 2, 3, 4, 5, 6
 
 _lib = None
 
@@ -30,7 +31,8 @@ class LbmDenseDesc(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
                 ("q", ctypes.c_int32), ("storage", ctypes.c_int32), ("box_cavity", ctypes.c_int32),
                 ("plane_stride", ctypes.c_int64), ("omega", ctypes.c_double),
-                ("wall_term", (ctypes.c_double * 27) * 2)]
+                ("wall_term", (ctypes.c_double * 27) * 2), ("zouhe_rho", ctypes.c_double),
+                ("zouhe_u", ctypes.c_double * 3)]
 
 
 def build(force=False):
@@ -98,7 +100,27 @@ _EXTRA_SIGNATURES = {
     "ngb_bgrid_laplace_i64": ([_bd, _vp, _vp, _vp], ctypes.c_int),
     "ngb_dense_laplace_i64": ([_i32, _i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_lbm_release_graphs": ([], ctypes.c_int),
+    "ngb_unet_weight_count": ([], ctypes.c_int64),
+    "ngb_lbm_dense_save": ([ctypes.c_char_p, ctypes.POINTER(LbmDenseDesc), _vp, ctypes.c_int64, _vp], ctypes.c_int),
+    "ngb_lbm_dense_load": ([ctypes.c_char_p, ctypes.POINTER(LbmDenseDesc), _vp, _vp, ctypes.POINTER(ctypes.c_int64), _vp],
+                           ctypes.c_int),
+    "ngb_unet_write_weights": ([ctypes.c_char_p, _vp, ctypes.c_int64], ctypes.c_int),
+    "ngb_unet_read_weights": ([ctypes.c_char_p, _vp, ctypes.c_int64], ctypes.c_int),
+    "ngb_learned_create": ([_i32, _i32, _vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "ngb_learned_destroy": ([_vp], ctypes.c_int),
+    "ngb_learned_precondition": ([_vp, _vp, _vp, _vp], ctypes.c_int),
+    "ngb_learned_solve": ([_vp, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
 }
+
+
+class LearnedParams(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("max_iter", ctypes.c_int32), ("refresh_every", ctypes.c_int32),
+                ("stall", ctypes.c_int32), ("fallback", ctypes.c_int32)]
+
+
+class LearnedResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("fallback", ctypes.c_int32), ("fallback_iterations", ctypes.c_int32),
+                ("converged", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
 
 
 class PoissonDesc(ctypes.Structure):
@@ -124,6 +146,7 @@ _EXTRA_SIGNATURES.update({
     "ngb_cg_workspace_bytes": ([_pd], ctypes.c_size_t),
     "ngb_cg_solve": ([_pd, _vp, _vp, _vp, ctypes.c_size_t, ctypes.POINTER(CgParams), ctypes.POINTER(CgResult), _vp],
                      ctypes.c_int),
+    "ngb_cg_time_passes": ([_pd, _vp, _vp, _vp, ctypes.c_size_t, _i32, _vp, _vp], ctypes.c_int),
     "ngb_poisson_rhs": ([_pd, _vp, _vp, _dbl, _vp, _vp], ctypes.c_int),
     "ngb_gaussian_sources": ([_i32, _i32, _i32, ctypes.c_uint64, _vp, _vp], ctypes.c_int),
     "ngb_dot_noalloc": ([ctypes.c_int64, _i32, _vp, _vp, _vp, _vp], ctypes.c_int),
@@ -193,8 +216,11 @@ def lid_wall_terms(q, ulb, ulid=(1.0, 0.0, 0.0)):
 
 
 def lbm_dense_desc(nx, ny, nz, q, storage, omega, moving_wall_terms=None, box_cavity=True, plane_stride=0,
-                   bounce_back_terms=None):
+                   bounce_back_terms=None, zouhe_rho=1.0, zouhe_u=(0.0, 0.0, 0.0)):
     d = LbmDenseDesc()
+    d.zouhe_rho = zouhe_rho
+    for a in range(3):
+        d.zouhe_u[a] = zouhe_u[a]
     d.nx, d.ny, d.nz, d.q = nx, ny, nz, q
     d.storage = STORAGE_NAMES[storage] if isinstance(storage, str) else storage
     d.box_cavity = 1 if box_cavity else 0
@@ -234,6 +260,19 @@ def lbm_dense_run(desc, fa, fb, nsteps, flags=None, stream=None):
 def lbm_dense_run_host(desc, host_in, host_out, fa, fb, nsteps, flags=None, stream=None):
     return check(lib().ngb_lbm_dense_run_host(ctypes.byref(desc), _ptr(host_in), _ptr(host_out), _ptr(fa), _ptr(fb),
                                               _ptr(flags), int(nsteps), _stream(stream)))
+
+
+def lbm_dense_save(path, desc, f, step, stream=None):
+    """Checkpoint of the population buffer f (the newest state) with its step number."""
+    check(lib().ngb_lbm_dense_save(str(path).encode(), ctypes.byref(desc), _ptr(f), int(step), _stream(stream)))
+
+
+def lbm_dense_load(path, desc, fa, fb=None, stream=None):
+    """Resume: fills fa (and fb) with the checkpoint's state; returns its step number."""
+    step = ctypes.c_int64(0)
+    check(lib().ngb_lbm_dense_load(str(path).encode(), ctypes.byref(desc), _ptr(fa), _ptr(fb) if fb is not None else None,
+                                   ctypes.byref(step), _stream(stream)))
+    return step.value
 
 
 def lbm_wall_mask(nx, ny, nz, q, flags, stream=None):
@@ -471,6 +510,14 @@ def cg_solve(desc, b, x, workspace, tol=1e-8, max_iter=10000, refresh_every=50, 
             "rel_residual": r.rel_residual, "seconds": r.seconds}
 
 
+def cg_time_passes(desc, b, x, workspace, reps=20, stream=None):
+    """CUDA-event milliseconds per launch of the CG passes A and B (measurement aid)."""
+    ms = (ctypes.c_float * 2)()
+    check(lib().ngb_cg_time_passes(ctypes.byref(desc), _ptr(b), _ptr(x), _ptr(workspace), workspace.numel(), int(reps),
+                                   ctypes.cast(ms, ctypes.c_void_p), _stream(stream)))
+    return float(ms[0]), float(ms[1])
+
+
 def gaussian_sources(nx, ny, nz, seed):
     import numpy as np
     c = np.zeros(24)
@@ -484,3 +531,45 @@ def poisson_rhs(desc, centres, amps, sigma, f, stream=None):
     """centres/amps: float64 cuda tensors (24 and 8 values)."""
     return check(lib().ngb_poisson_rhs(ctypes.byref(desc), _ptr(centres), _ptr(amps), float(sigma), _ptr(f),
                                        _stream(stream)))
+
+
+class LearnedSolver:
+    """The learned-preconditioner Poisson solver of the C ABI (ngb_learned_*):
+    FCG(1) with a V-cycle whose coarsest solve is the U-Net, FP64 true
+    residual, Jacobi-PCG fallback. `weights`: a weight-file path or an FP32
+    host tensor of ngb_unet_weight_count() values."""
+
+    def __init__(self, n, levels, weights):
+        import torch
+        L = lib()
+        if isinstance(weights, (str, bytes, os.PathLike)):
+            from .learned import read_weights
+            weights = read_weights(weights)
+        w = weights.detach().to("cpu", torch.float32).contiguous()
+        self._keep = w
+        h = ctypes.c_void_p()
+        check(L.ngb_learned_create(int(n), int(levels), ctypes.c_void_p(w.data_ptr()), w.numel(), ctypes.byref(h)))
+        self.handle, self.n, self.levels = h, n, levels
+
+    def precondition(self, r, z, stream=None):
+        check(lib().ngb_learned_precondition(self.handle, _ptr(r), _ptr(z), _stream(stream)))
+        return z
+
+    def solve(self, b, x, tol=1e-8, max_iter=2000, refresh_every=10, stall=30, fallback=True, stream=None):
+        p = LearnedParams()
+        p.tol, p.max_iter, p.refresh_every, p.stall, p.fallback = tol, max_iter, refresh_every, stall, int(fallback)
+        r = LearnedResult()
+        check(lib().ngb_learned_solve(self.handle, _ptr(b), _ptr(x), ctypes.byref(p), ctypes.byref(r), _stream(stream)))
+        return {"iterations": r.iterations, "fallback": bool(r.fallback), "fallback_iterations": r.fallback_iterations,
+                "converged": bool(r.converged), "rel_residual": r.rel_residual, "seconds": r.seconds}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().ngb_learned_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdarg>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/neon_gb300.h"
 
@@ -45,6 +46,16 @@ void clear_error();
     } while (0)
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// NVTX range over a host entry point (the counterpart of the reference's
+// "Skeleton" / "Graph Iteration" ranges, Skeleton.h:56-65, Graph.cpp:1001-1029):
+// visible to Nsight tools, a no-op without one.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ------------------------------------------------------------------ lattices
 // D3Q19 in Neon's order (benchmarks/lbm-lid-driven-cavity-flow/src/D3Q19.h:23-44):
@@ -105,7 +116,8 @@ __host__ __device__ inline int      flag_class(uint32_t f) { return int(f >> 28)
 __host__ __device__ inline uint32_t make_flag(uint32_t mask, int cls) { return (mask & 0x07ffffffu) | (uint32_t(cls) << 28); }
 
 // A node other cells stream from normally (no bounce-back across it).
-__host__ __device__ inline bool is_fluid_class(int c) { return c == NGB_CELL_BULK || c == NGB_CELL_OUTLET; }
+__host__ __device__ inline bool is_zouhe_class(int c) { return c == NGB_CELL_PRESSURE || c == NGB_CELL_VELOCITY; }
+__host__ __device__ inline bool is_fluid_class(int c) { return c == NGB_CELL_BULK || c == NGB_CELL_OUTLET || is_zouhe_class(c); }
 
 // ------------------------------------------------------------------ storage
 // The 16-bit "off" forms hold g = f - w_q; FP16 holds it scaled by 2^14
@@ -118,6 +130,36 @@ template <>
 struct StoreScale<__half> {
     static constexpr int log2 = 14;
 };
+// FP16 offsets stored with stochastic rounding (NGB_STORE_F16SR): the same
+// 2-byte values as __half, a distinct type so that the kernels pick the store.
+struct f16sr_t {
+    __half h;
+};
+template <>
+struct StoreScale<f16sr_t> {
+    static constexpr int log2 = 14;
+};
+
+// Random bits of the F16SR store (the definition in neon_gb300.h, ngb_storage).
+__host__ __device__ inline uint32_t mix32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+// h of the cell pair (i >> 1) in step seed s
+__host__ __device__ inline uint32_t dither_hash(int64_t cell, uint32_t seed)
+{
+    const uint64_t pr = uint64_t(cell) >> 1;
+    return mix32(uint32_t(pr) ^ (uint32_t(pr >> 32) * 0x9E3779B1u) ^ (seed * 0x85EBCA77u));
+}
+__host__ __device__ inline uint32_t dither_word(uint32_t h, int q) { return (h ^ (uint32_t(q) * 0x9E3779B9u)) * 0xC2B2AE35u; }
+// 13 bits for the even (lo) / odd (hi) cell of the pair
+__host__ __device__ inline uint32_t dither_lo(uint32_t hq) { return hq >> 19; }
+__host__ __device__ inline uint32_t dither_hi(uint32_t hq) { return (hq >> 6) & 0x1fffu; }
 static_assert(float(1 << StoreScale<__half>::log2) == NGB_F16OFF_SCALE, "FP16 storage scale");
 
 inline size_t storage_bytes(int storage)

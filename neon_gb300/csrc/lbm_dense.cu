@@ -15,7 +15,7 @@ int validate(const ngb_lbm_dense_desc* d)
 {
     NGB_CHECK_ARG(d != nullptr, "desc is NULL");
     NGB_CHECK_ARG(d->q == 19 || d->q == 27, "q must be 19 or 27 (got %d)", d->q);
-    NGB_CHECK_ARG(d->storage >= NGB_STORE_F64 && d->storage <= NGB_STORE_BF16OFF, "bad storage %d", d->storage);
+    NGB_CHECK_ARG(d->storage >= NGB_STORE_F64 && d->storage <= NGB_STORE_F16SR, "bad storage %d", d->storage);
     NGB_CHECK_ARG(d->nx >= 3 && d->ny >= 3 && d->nz >= 3, "dims must be >= 3 (got %d %d %d)", d->nx, d->ny, d->nz);
     NGB_CHECK_ARG(d->ny <= 65535 && d->nz <= 65535, "ny and nz must be <= 65535");
     const int64_t V = int64_t(d->nx) * d->ny * d->nz;
@@ -35,13 +35,16 @@ C round_through(double v)
     return C(S(v));
 }
 
-DenseParams<float> params_f32(const ngb_lbm_dense_desc* d)
+DenseParams<float> params_f32(const ngb_lbm_dense_desc* d, uint32_t step = 0)
 {
     DenseParams<float> p{};
+    p.seed = d->dither_seed + step;
     p.nx = d->nx, p.ny = d->ny, p.nz = d->nz, p.box = d->box_cavity ? 1 : 0, p.stride = stride_of(d);
     p.omega = float(d->omega);
     for (int c = 0; c < 2; c++)
         for (int q = 0; q < 27; q++) p.wall[c][q] = float(d->wall_term[c][q]);
+    p.zh_rho = float(d->zouhe_rho - 1.0);  // the shifted form works on rho - 1
+    for (int a = 0; a < 3; a++) p.zh_u[a] = float(d->zouhe_u[a]);
     return p;
 }
 
@@ -52,13 +55,16 @@ DenseParams<double> params_f64(const ngb_lbm_dense_desc* d)
     p.omega = d->omega;
     for (int c = 0; c < 2; c++)
         for (int q = 0; q < 27; q++) p.wall[c][q] = d->wall_term[c][q];
+    p.zh_rho = d->zouhe_rho;
+    for (int a = 0; a < 3; a++) p.zh_u[a] = d->zouhe_u[a];
     return p;
 }
 
-int step_impl(const ngb_lbm_dense_desc* d, const void* fin, void* fout, const uint32_t* flags, cudaStream_t s)
+// `step`: index of the step within a run (its dither seed is dither_seed + step).
+int step_impl(const ngb_lbm_dense_desc* d, const void* fin, void* fout, const uint32_t* flags, cudaStream_t s, uint32_t step = 0)
 {
     if (d->storage == NGB_STORE_F64) return launch_lbm_dense_f64(d->q, fin, fout, flags, params_f64(d), s);
-    return launch_lbm_dense_f32(d->q, d->storage, fin, fout, flags, params_f32(d), s);
+    return launch_lbm_dense_f32(d->q, d->storage, fin, fout, flags, params_f32(d, step), s);
 }
 
 // ---------------------------------------------------------------- graph cache for ngb_lbm_dense_run
@@ -105,7 +111,8 @@ int get_run_graph(const RunKey& k, cudaGraphExec_t& exec)
     int         rc = NGB_OK;
     if (e == cudaSuccess) {
         for (int t = 0; t < k.steps && rc == NGB_OK; t++)
-            rc = step_impl(&k.desc, t % 2 == 0 ? k.fa : k.fb, const_cast<void*>(t % 2 == 0 ? k.fb : k.fa), k.flags, cs);
+            rc = step_impl(&k.desc, t % 2 == 0 ? k.fa : k.fb, const_cast<void*>(t % 2 == 0 ? k.fb : k.fa), k.flags, cs,
+                           uint32_t(t));
         e = cudaStreamEndCapture(cs, &graph);
     }
     cudaStreamDestroy(cs);
@@ -141,8 +148,9 @@ __global__ void wall_mask_kernel(uint32_t* flags, int nx, int ny, int nz)
     if (x >= nx) return;
     const int64_t  sy = nx, sz = int64_t(nx) * ny, cell = x + sy * y + sz * z;
     const uint32_t f = flags[cell];
-    if (flag_class(f) != NGB_CELL_BULK) {
-        flags[cell] = make_flag(0, flag_class(f));
+    const int      cls = flag_class(f);
+    if (cls != NGB_CELL_BULK && !is_zouhe_class(cls)) {  // Zou-He nodes are updated and need the mask too
+        flags[cell] = make_flag(0, cls);
         return;
     }
     uint32_t mask = 0;
@@ -156,7 +164,7 @@ __global__ void wall_mask_kernel(uint32_t* flags, int nx, int ny, int nz)
             wall = !is_fluid_class(flag_class(flags[sx + sy * syy + sz * szz]));
         if (wall) mask |= 1u << q;
     }
-    flags[cell] = make_flag(mask, NGB_CELL_BULK);
+    flags[cell] = make_flag(mask, cls);
 }
 
 template <int Q, typename S>
@@ -258,6 +266,7 @@ int ngb_lbm_dense_kernels_per_step(const ngb_lbm_dense_desc* d)
 
 int ngb_lbm_dense_run(const ngb_lbm_dense_desc* d, void* fa, void* fb, const uint32_t* flags, int32_t nsteps, void* stream)
 {
+    NvtxRange nvtx("ngb_lbm_dense_run");
     int rc = validate(d);
     if (rc) return rc;
     NGB_CHECK_ARG(fa && fb && fa != fb, "fa/fb must be distinct non-NULL device pointers");
@@ -277,8 +286,8 @@ int ngb_lbm_dense_run(const ngb_lbm_dense_desc* d, void* fa, void* fb, const uin
         if (rc) return rc;
         for (int i = 0; i < full; i++) NGB_CUDA_TRY(cudaGraphLaunch(exec, s));
     }
-    for (int t = 0; t < rest; t++) {
-        rc = step_impl(d, t % 2 == 0 ? fa : fb, t % 2 == 0 ? fb : fa, flags, s);
+    for (int t = 0; t < rest; t++) {  // steps 32 full + t: seed offset t (mod 32)
+        rc = step_impl(d, t % 2 == 0 ? fa : fb, t % 2 == 0 ? fb : fa, flags, s, uint32_t(t));
         if (rc) return rc;
     }
     return NGB_OK;
@@ -342,6 +351,7 @@ int ngb_lbm_cavity_init(const ngb_lbm_dense_desc* d, double ulb, void* fa, void*
             if (q19) NGB_INIT(19, float, 0); else NGB_INIT(27, float, 0);
             break;
         case NGB_STORE_F16OFF:
+        case NGB_STORE_F16SR:
             if (q19) NGB_INIT(19, __half, 1); else NGB_INIT(27, __half, 1);
             break;
         default:
@@ -378,6 +388,7 @@ int ngb_lbm_dense_macroscopic(const ngb_lbm_dense_desc* d, const void* fin, cons
             if (q19) NGB_MAC(19, float); else NGB_MAC(27, float);
             break;
         case NGB_STORE_F16OFF:
+        case NGB_STORE_F16SR:
             if (q19) NGB_MAC(19, __half); else NGB_MAC(27, __half);
             break;
         default:

@@ -19,7 +19,27 @@ struct DenseParams {
     int64_t stride;   // elements between planes
     C       omega;
     C       wall[2][27];  // wall term by wall class (bounce-back, moving wall), compute type
+    C        zh_rho;      // Zou-He PRESSURE nodes: rho (FP64 compute) or rho - 1 (FP32 shifted compute)
+    C        zh_u[3];     // Zou-He VELOCITY nodes: u
+    uint32_t seed;        // F16SR: dither seed of this step
 };
+
+// Inward normal of a Zou-He node: the first box face it lies on, in the order
+// x = 0, x = nx-1, y = 0, y = ny-1, z = 0, z = nz-1 (axis a, sign s).
+__host__ __device__ inline void zouhe_normal(int x, int y, int z, int nx, int ny, int nz, int& a, int& s)
+{
+    if (x == 0) a = 0, s = 1;
+    else if (x == nx - 1) a = 0, s = -1;
+    else if (y == 0) a = 1, s = 1;
+    else if (y == ny - 1) a = 1, s = -1;
+    else if (z == 0) a = 2, s = 1;
+    else a = 2, s = -1;
+}
+template <int Q>
+__host__ __device__ constexpr int lattice_c(int q, int a)
+{
+    return a == 0 ? Lattice<Q>::cx(q) : (a == 1 ? Lattice<Q>::cy(q) : Lattice<Q>::cz(q));
+}
 
 // Classification and wall mask of cell (x,y,z) for the analytic lid-driven
 // cavity (RunCavityTwoPop.cu:208-224 + LbmTools.h:327-376): faces are walls,
@@ -61,6 +81,19 @@ __device__ __forceinline__ int cell_setup(const DenseParams<C>& p, const uint32_
     const int      cls = flag_class(f);
     mask = flag_mask(f);
     lidbits = 0;
+    if (is_zouhe_class(cls)) {
+        // Zou-He nodes lie on the box faces: moving-wall sources are looked
+        // up inside the box only (an out-of-box source is a resting wall)
+        const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny;
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            if (!(mask & (1u << q))) continue;
+            const int sx = x - Lattice<Q>::cx(q), syy = y - Lattice<Q>::cy(q), szz = z - Lattice<Q>::cz(q);
+            if (sx < 0 || syy < 0 || szz < 0 || sx >= p.nx || syy >= p.ny || szz >= p.nz) continue;
+            if (source_class(flags, sx + sy * syy + sz * szz) == NGB_CELL_MOVINGWALL) lidbits |= 1u << q;
+        }
+        return cls;
+    }
     if (cls == NGB_CELL_BULK) {
         // A bulk cell on the domain face has sources outside the domain: it is
         // not updated (keeps every access inside the arrays).
@@ -151,6 +184,63 @@ __device__ __forceinline__ void bgk_f64_ref(const S (&pop)[Q], double omega_, S 
     }
 }
 
+// Zou-He node (D3Q19) in the reference's FP64 arithmetic: the pull of the
+// known populations (wall rule for masked directions), M and K, the boundary
+// rho and u, the equilibria of collideBgkUnrolled's shapes (LbmTools.h:198-282),
+// the unknowns f_q = f_opp(q) + eq_q - eq_opp(q), and the BGK relaxation
+// towards eq(rho, u).
+template <typename S>
+__device__ __forceinline__ void zouhe_node_f64(const S* __restrict__ fin, S* __restrict__ fout, int64_t cell, int x, int y,
+                                               int z, int cls, uint32_t mask, uint32_t lidbits, const DenseParams<double>& p)
+{
+    using L = Lattice<19>;
+    const int64_t sy = p.nx, sz = int64_t(p.nx) * p.ny, stride = p.stride;
+    int           a, s;
+    zouhe_normal(x, y, z, p.nx, p.ny, p.nz, a, s);
+    double pop[19];
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        pop[q] = 0.0;
+        if (lattice_c<19>(q, a) * s == 1) continue;  // unknown: arrives from outside the box
+        if (mask & (1u << q)) {
+            const int o = L::opp(q);
+            pop[q] = double(__ldg(fin + o * stride + cell)) + ((lidbits & (1u << q)) ? p.wall[1][o] : p.wall[0][o]);
+        } else {
+            pop[q] = double(__ldg(fin + q * stride + cell - L::cx(q) - L::cy(q) * sy - L::cz(q) * sz));
+        }
+    }
+    double M = 0.0, K = 0.0;
+#pragma unroll
+    for (int q = 0; q < 19; q++) {
+        const int ca = lattice_c<19>(q, a);
+        if (ca == 0) M = M + pop[q];
+        else if (ca * s == -1) K = K + pop[q];
+    }
+    double rho, u[3] = {0.0, 0.0, 0.0};
+    if (cls == NGB_CELL_PRESSURE) {
+        rho = p.zh_rho;
+        u[a] = double(s) * (1.0 - (M + 2.0 * K) / rho);
+    } else {
+        for (int d = 0; d < 3; d++) u[d] = p.zh_u[d];
+        rho = (M + 2.0 * K) / (1.0 - double(s) * u[a]);
+    }
+    const double usqr = 1.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    const double cu[9] = {u[0], u[1], u[2], u[0] + u[1], u[0] - u[1], u[0] + u[2], u[0] - u[2], u[1] + u[2], u[1] - u[2]};
+    double       eq[19];
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+        const double wk = k < 3 ? (1. / 18.) : (1. / 36.);
+        eq[k] = rho * wk * (1. - 3. * cu[k] + 4.5 * cu[k] * cu[k] - usqr);
+        eq[k + 10] = eq[k] + rho * wk * 6. * cu[k];
+    }
+    eq[9] = rho * (1. / 3.) * (1. - usqr);
+#pragma unroll
+    for (int q = 0; q < 19; q++)
+        if (lattice_c<19>(q, a) * s == 1) pop[q] = pop[L::opp(q)] + eq[q] - eq[L::opp(q)];
+#pragma unroll
+    for (int q = 0; q < 19; q++) fout[q * stride + cell] = S((1. - p.omega) * pop[q] + p.omega * eq[q]);
+}
+
 template <int Q, typename S>
 __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __restrict__ fin, S* __restrict__ fout,
                                                                    const uint32_t* __restrict__ flags, DenseParams<double> p)
@@ -165,6 +255,10 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __re
     const int     cls = cell_setup<Q>(p, flags, x, y, z, cell, mask, lidbits);
     if (cls == NGB_CELL_OUTLET) {
         outlet_copy<Q>(fin, fout, stride, cell, x, flags);
+        return;
+    }
+    if (is_zouhe_class(cls)) {
+        if constexpr (Q == 19) zouhe_node_f64<S>(fin, fout, cell, x, y, z, cls, mask, lidbits, p);
         return;
     }
     if (cls != NGB_CELL_BULK) return;

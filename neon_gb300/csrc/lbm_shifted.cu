@@ -1,8 +1,25 @@
-// Instantiations of the two-cells-per-thread dense LBM kernel. Compiled with
+// Launches of the dense LBM kernels with FP32 compute (FP32 and 16-bit storage). Compiled with
 // --fmad=false: the kernel writes every fused multiply-add explicitly.
 #include "lbm_shifted.cuh"
 
 namespace ngb {
+namespace {
+
+// Core kernel of the analytic cavity: the x-pair form for 16-bit D3Q19 when rows start on a word.
+template <int Q, typename T>
+void launch_core(bool pair, dim3 gpair, dim3 gcore, dim3 block, const T* fi, T* fo, const DenseParams<float>& ps,
+                 const DirOffsets& o, cudaStream_t s)
+{
+    if constexpr (Q == 19 && sizeof(T) == 2) {
+        if (pair) {
+            lbm_box_core_pair_kernel<Q, T><<<gpair, kPairBlock, 0, s>>>(fi, fo, ps, o);
+            return;
+        }
+    }
+    lbm_box_core_kernel<Q, T><<<gcore, block, 0, s>>>(fi, fo, ps, o);
+}
+
+}  // namespace
 
 int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const uint32_t* flags, const DenseParams<float>& p,
                          cudaStream_t s)
@@ -19,12 +36,15 @@ int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const 
     }
     // FP16 values are 2^14 g: the wall terms added to them scale alike
     DenseParams<float> ps = p;
-    if (storage == NGB_STORE_F16OFF)
+    if (storage == NGB_STORE_F16OFF || storage == NGB_STORE_F16SR)
         for (int c = 0; c < 2; c++)
             for (int q = 0; q < 27; q++) ps.wall[c][q] = p.wall[c][q] * NGB_F16OFF_SCALE;
     // Analytic cavity of at least 4 x 6 x 6 cells: core + shell kernels; otherwise one kernel over every
     // cell. D3Q27 with 16-bit storage keeps the one-kernel form (measured faster: 39.4 vs 36.3 GLUPS at 384^3).
     const bool split = lbm_dense_split(Q, storage, p);
+    // 16-bit D3Q19 with even rows and planes: the x-pair core kernel (32-bit accesses)
+    const bool pair = split && Q == 19 && storage != NGB_STORE_F32 && p.nx % 2 == 0 && p.stride % 2 == 0;
+    const dim3 gpair((p.nx / 2 + kPairBlock - 1) / kPairBlock, p.ny - 4, p.nz - 4);
     const dim3 gcore((p.nx - 1 + kLbmBlockX - 1) / kLbmBlockX, p.ny - 4, p.nz - 4);
     const dim3 gshell((p.nx - 1 + kLbmBlockX - 1) / kLbmBlockX, 2 * (p.ny - 2) + 2 * (p.nz - 4));
 #define NGB_ONE(QQ, T)                                                                                                        \
@@ -32,7 +52,7 @@ int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const 
         const T* fi = static_cast<const T*>(fin);                                                                             \
         T*       fo = static_cast<T*>(fout);                                                                                  \
         if (split) {                                                                                                          \
-            lbm_box_core_kernel<QQ, T><<<gcore, block, 0, s>>>(fi, fo, ps, o);                                                \
+            launch_core<QQ, T>(pair, gpair, gcore, block, fi, fo, ps, o, s);                                                  \
             lbm_box_shell_kernel<QQ, T><<<gshell, block, 0, s>>>(fi, fo, ps, o);                                              \
         } else {                                                                                                              \
             lbm_dense_single_kernel<QQ, T><<<grid, block, 0, s>>>(fi, fo, flags, ps, o);                                      \
@@ -45,6 +65,9 @@ int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const 
             break;
         case NGB_STORE_F16OFF:
             if (q19) NGB_ONE(19, __half); else NGB_ONE(27, __half);
+            break;
+        case NGB_STORE_F16SR:
+            if (q19) NGB_ONE(19, f16sr_t); else NGB_ONE(27, f16sr_t);
             break;
         case NGB_STORE_BF16OFF:
             if (q19) NGB_ONE(19, __nv_bfloat16); else NGB_ONE(27, __nv_bfloat16);

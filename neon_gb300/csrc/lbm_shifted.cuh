@@ -47,7 +47,9 @@ struct PairIO;
 
 template <>
 struct PairIO<float> {
+    static constexpr bool kStochastic = false;
     using Word = float2;
+    __device__ __forceinline__ static float ldg1(const char* p, float w) { return __ldg(reinterpret_cast<const float*>(p)) - w; }
     __device__ __forceinline__ static Word load(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
     // (a.hi, b.lo)
     __device__ __forceinline__ static Word mid(Word a, Word b) { return make_float2(a.y, b.x); }
@@ -62,7 +64,9 @@ struct PairIO<float> {
 
 template <>
 struct PairIO<__half> {
+    static constexpr bool kStochastic = false;
     using Word = __half2;
+    __device__ __forceinline__ static float ldg1(const char* p, float) { return __half2float(__ldg(reinterpret_cast<const __half*>(p))); }
     __device__ __forceinline__ static Word load(const __half* p) { return __ldg(reinterpret_cast<const __half2*>(p)); }
     __device__ __forceinline__ static Word mid(Word a, Word b) { return __halves2half2(__high2half(a), __low2half(b)); }
     __device__ __forceinline__ static float2 to_g(Word v, float) { return __half22float2(v); }
@@ -76,7 +80,12 @@ struct PairIO<__half> {
 
 template <>
 struct PairIO<__nv_bfloat16> {
+    static constexpr bool kStochastic = false;
     using Word = __nv_bfloat162;
+    __device__ __forceinline__ static float ldg1(const char* p, float)
+    {
+        return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p)));
+    }
     __device__ __forceinline__ static Word load(const __nv_bfloat16* p)
     {
         return __ldg(reinterpret_cast<const __nv_bfloat162*>(p));
@@ -90,6 +99,57 @@ struct PairIO<__nv_bfloat16> {
     }
     __device__ __forceinline__ static void store1(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
 };
+
+// FP16 stores with stochastic rounding: r (13 random bits) is added to the
+// FP32 bit pattern, which the round-toward-zero conversion then truncates, so
+// the value rounds up in magnitude with probability = its remainder / ulp.
+__device__ __forceinline__ __half f16_sr(float v, uint32_t r) { return __float2half_rz(__uint_as_float(__float_as_uint(v) + r)); }
+__device__ __forceinline__ uint32_t f16x2_sr(float lo, float hi, uint32_t rlo, uint32_t rhi)
+{
+    uint32_t w;
+    asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(w) : "f"(__uint_as_float(__float_as_uint(hi) + rhi)),
+        "f"(__uint_as_float(__float_as_uint(lo) + rlo)));
+    return w;
+}
+
+template <>
+struct PairIO<f16sr_t> {
+    static constexpr bool kStochastic = true;
+    __device__ __forceinline__ static float ldg1(const char* p, float) { return __half2float(__ldg(reinterpret_cast<const __half*>(p))); }
+    __device__ __forceinline__ static void  store1(f16sr_t* p, float g, float, uint32_t r)
+    {
+        *reinterpret_cast<__half*>(p) = f16_sr(g, r);
+    }
+};
+
+// Store of one computed value (the dither bits r are used by stochastic storage only).
+template <typename S>
+__device__ __forceinline__ void store_g(S* p, float g, float w, uint32_t r)
+{
+    if constexpr (PairIO<S>::kStochastic)
+        PairIO<S>::store1(p, g, w, r);
+    else
+        PairIO<S>::store1(p, g, w);
+}
+// 13 dither bits of population q of `cell` (stochastic storage only)
+template <typename S>
+__device__ __forceinline__ uint32_t dither_of(uint32_t h, int q, int64_t cell)
+{
+    if constexpr (PairIO<S>::kStochastic) {
+        const uint32_t hq = dither_word(h, q);
+        return (cell & 1) ? dither_hi(hq) : dither_lo(hq);
+    } else {
+        return 0u;
+    }
+}
+template <typename S>
+__device__ __forceinline__ uint32_t dither_base(int64_t cell, uint32_t seed)
+{
+    if constexpr (PairIO<S>::kStochastic)
+        return dither_hash(cell, seed);
+    else
+        return 0u;
+}
 
 // Byte offsets, relative to a cell's own element of plane 0, of each
 // direction's pull source (q * stride - c_q . (1, nx, nx ny)) and of each of
@@ -111,7 +171,7 @@ __device__ __forceinline__ void pull_one(const S* __restrict__ fin, int64_t cell
     const char* P = reinterpret_cast<const char*>(fin + cell);
     if (mask == 0) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
+        for (int q = 0; q < Q; q++) g[q] = PairIO<S>::ldg1(P + o.pull[q], float(L::w(q)));
         return;
     }
 #pragma unroll
@@ -119,9 +179,9 @@ __device__ __forceinline__ void pull_one(const S* __restrict__ fin, int64_t cell
         if (mask & (1u << q)) {
             const int   oq = L::opp(q);
             const float wt = (lidbits & (1u << q)) ? p.wall[1][oq] : p.wall[0][oq];
-            g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.own[oq])), float(L::w(oq))) + wt;
+            g[q] = PairIO<S>::ldg1(P + o.own[oq], float(L::w(oq))) + wt;
         } else {
-            g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
+            g[q] = PairIO<S>::ldg1(P + o.pull[q], float(L::w(q)));
         }
     }
 }
@@ -169,6 +229,9 @@ __device__ __forceinline__ V cdot(int q, V u3x, V u3y, V u3z)
     return t;
 }
 
+template <int Q, typename V, int SH>
+__device__ __forceinline__ void bgk_relax(V (&g)[Q], V drho, V rho, V ux, V uy, V uz, float omega);
+
 // Shifted BGK on V = float (one cell) or float2 (a cell pair): g -> g' in place.
 // SH: the values are G = 2^SH g (FP16 storage). Every quantity of the
 // sequence below is then exactly 2^SH times its unscaled value (power-of-two
@@ -205,6 +268,15 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
     V       inv = recip(rho);
     if constexpr (SH != 0) inv = mul2(inv, splat<V>(kDown));
     const V ux = mul2(jx, inv), uy = mul2(jy, inv), uz = mul2(jz, inv);
+    bgk_relax<Q, V, SH>(g, drho, rho, ux, uy, uz, omega);
+}
+
+// The relaxation part of the shifted BGK: g <- g + omega (eq_g(drho, u) - g)
+// with the values of g held as 2^SH g; drho, rho and u are unscaled.
+template <int Q, typename V, int SH>
+__device__ __forceinline__ void bgk_relax(V (&g)[Q], V drho, V rho, V ux, V uy, V uz, float omega)
+{
+    constexpr float kUp = float(1u << SH);
     const V usq = fma2(uz, uz, fma2(uy, uy, mul2(ux, ux)));
     const V rus = mul2(rho, mul2(splat<V>(1.5f), usq));
     const V base = sub2(drho, rus);
@@ -227,6 +299,54 @@ __device__ __forceinline__ void bgk_shifted(V (&g)[Q], float omega)
     }
 }
 
+// Zou-He node (D3Q19) in the shifted FP32 form, on its pulled populations
+// (the unknown ones are overwritten): M and K of the known populations (float
+// adds, q ascending, taken back to unscaled values), mk = M + (K + K);
+// PRESSURE: drho = rho_b - 1, rho = 1 + drho, s u_a = (drho - mk) / rho;
+// VELOCITY: u = u_b, un = s u_a, drho = (mk + un) / (1 - un), rho = 1 + drho;
+// unknowns g_q = fma((2 w_q) rho, c_q . 3u, g_opp(q)) (f_q - f_opp(q) =
+// eq_q - eq_opp(q) = 6 w_q rho c_q . u); then the shifted relaxation.
+template <int Q, typename S>
+__device__ __forceinline__ void zouhe_node_shifted(float (&g)[Q], int cls, int x, int y, int z, const DenseParams<float>& p)
+{
+    using L = Lattice<Q>;
+    constexpr int   SH = StoreScale<S>::log2;
+    constexpr float kUp = float(1u << SH), kDown = 1.0f / kUp;
+    int             a, s;
+    zouhe_normal(x, y, z, p.nx, p.ny, p.nz, a, s);
+    float M = 0.f, K = 0.f;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int ca = lattice_c<Q>(q, a);
+        if (ca == 0) M = M + g[q];
+        else if (ca * s == -1) K = K + g[q];
+    }
+    if constexpr (SH != 0) {
+        M = M * kDown;
+        K = K * kDown;
+    }
+    const float mk = M + (K + K);
+    float       u[3] = {0.f, 0.f, 0.f}, drho, rho;
+    if (cls == NGB_CELL_PRESSURE) {
+        drho = p.zh_rho;
+        rho = 1.f + drho;
+        u[a] = float(s) * ((drho - mk) / rho);
+    } else {
+        for (int d = 0; d < 3; d++) u[d] = p.zh_u[d];
+        const float un = float(s) * u[a];
+        drho = (mk + un) / (1.f - un);
+        rho = 1.f + drho;
+    }
+    const float u3x = 3.f * u[0], u3y = 3.f * u[1], u3z = 3.f * u[2];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (lattice_c<Q>(q, a) * s != 1) continue;
+        const float coef = ((2.f * float(L::w(q))) * kUp) * rho;
+        g[q] = __fmaf_rn(coef, cdot<Q, float>(q, u3x, u3y, u3z), g[L::opp(q)]);
+    }
+    bgk_relax<Q, float, SH>(g, drho, rho, u[0], u[1], u[2], p.omega);
+}
+
 // One cell (x, y, z): classification, pull, collision, stores.
 template <int Q, typename S>
 __device__ __forceinline__ void lbm_cell(const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* __restrict__ flags,
@@ -240,13 +360,20 @@ __device__ __forceinline__ void lbm_cell(const S* __restrict__ fin, S* __restric
         outlet_copy<Q>(fin, fout, p.stride, cell, x, flags);
         return;
     }
-    if (cls != NGB_CELL_BULK) return;
+    const bool zh = is_zouhe_class(cls);
+    if (cls != NGB_CELL_BULK && !(Q == 19 && zh)) return;
     float g[Q];
+    // a Zou-He node's unknown directions come from outside the box: masked,
+    // so the pull reads the node's own opposite populations there (replaced below)
     pull_one<Q, S>(fin, cell, mask, lidbits, p, o, g);
-    bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
-    char* D = reinterpret_cast<char*>(fout + cell);
+    if (zh)
+        zouhe_node_shifted<Q, S>(g, cls, x, y, z, p);
+    else
+        bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
+    const uint32_t h = dither_base<S>(cell, p.seed);
+    char*          D = reinterpret_cast<char*>(fout + cell);
 #pragma unroll
-    for (int q = 0; q < Q; q++) PairIO<S>::store1(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)));
+    for (int q = 0; q < Q; q++) store_g<S>(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)), dither_of<S>(h, q, cell));
 }
 
 // One cell per thread, every cell of the grid.
@@ -285,28 +412,162 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_box_core_kernel(const S* __res
     float         g[Q];
     if (edge_warp == 0) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
+        for (int q = 0; q < Q; q++) g[q] = PairIO<S>::ldg1(P + o.pull[q], float(L::w(q)));
     } else {
 #pragma unroll
         for (int q = 0; q < Q; q++) {
             const int cx = L::cx(q);
             if (cx == 0) {
-                g[q] = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + o.pull[q])), float(L::w(q)));
+                g[q] = PairIO<S>::ldg1(P + o.pull[q], float(L::w(q)));
             } else {
                 const int     oq = L::opp(q);
                 const bool    wall = cx > 0 ? lo : hi;
                 const int64_t off = wall ? o.own[oq] : o.pull[q];
                 const float   wt = wall ? p.wall[0][oq] : 0.f;
                 const float   w = float(wall ? L::w(oq) : L::w(q));
-                const float   v = PairIO<S>::to_g1(__ldg(reinterpret_cast<const S*>(P + off)), w);
+                const float   v = PairIO<S>::ldg1(P + off, w);
                 g[q] = wall ? v + wt : v;
             }
         }
     }
     bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
-    char* D = reinterpret_cast<char*>(fout + cell);
+    const uint32_t h = dither_base<S>(cell, p.seed);
+    char*          D = reinterpret_cast<char*>(fout + cell);
 #pragma unroll
-    for (int q = 0; q < Q; q++) PairIO<S>::store1(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)));
+    for (int q = 0; q < Q; q++) store_g<S>(reinterpret_cast<S*>(D + o.own[q]), g[q], float(L::w(q)), dither_of<S>(h, q, cell));
+}
+
+// ------------------------------------------------------------------ x-pair core kernel (16-bit storage)
+// The core region of the analytic cavity with one thread per aligned pair of
+// cells (2t, 2t+1) of a row: every population plane is read with one 32-bit
+// load per thread (128 bytes per warp instruction instead of 64) and written
+// with one 32-bit store. A direction with c_x = 0 reads its pair directly; for
+// c_x = +1 the pair (2t-1, 2t) is the high half of the left neighbour's word
+// (warp shuffle) and the low half of the own word, for c_x = -1 the pair
+// (2t+1, 2t+2) is the own high half and the right neighbour's low half; the
+// first / last lane of a warp fetches the missing half with a 16-bit load.
+// The collision runs on FP32x2 pairs (per lane the scalar sequence, so the
+// stored bits equal the one-cell kernels'). The pairs holding x = 1 and
+// x = nx-2 take the resting-wall bounce-back per half; x = 0 and x = nx-1 are
+// wall nodes and are not written. Requires nx even (rows start on a word).
+constexpr int kPairBlock = 64;
+
+__device__ __forceinline__ uint32_t ldg_u32(const char* p) { return __ldg(reinterpret_cast<const unsigned int*>(p)); }
+__device__ __forceinline__ uint32_t ldg_u16(const char* p) { return __ldg(reinterpret_cast<const unsigned short*>(p)); }
+
+template <typename S>
+struct PairBits;
+template <>
+struct PairBits<__half> {
+    __device__ __forceinline__ static float2 to_g(uint32_t w)
+    {
+        __half2 h;
+        memcpy(&h, &w, 4);
+        return __half22float2(h);
+    }
+    __device__ __forceinline__ static uint32_t from_g(float2 g)
+    {
+        const __half2 h = __floats2half2_rn(g.x, g.y);
+        uint32_t      w;
+        memcpy(&w, &h, 4);
+        return w;
+    }
+};
+template <>
+struct PairBits<__nv_bfloat16> {
+    __device__ __forceinline__ static float2 to_g(uint32_t w)
+    {
+        __nv_bfloat162 h;
+        memcpy(&h, &w, 4);
+        return __bfloat1622float2(h);
+    }
+    __device__ __forceinline__ static uint32_t from_g(float2 g)
+    {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(g.x, g.y);
+        uint32_t             w;
+        memcpy(&w, &h, 4);
+        return w;
+    }
+};
+
+template <>
+struct PairBits<f16sr_t> {
+    __device__ __forceinline__ static float2 to_g(uint32_t w) { return PairBits<__half>::to_g(w); }
+    // the pair's cells are even (lo) and odd (hi): their dither bits come from one word
+    __device__ __forceinline__ static uint32_t from_g_sr(float2 g, uint32_t hq)
+    {
+        return f16x2_sr(g.x, g.y, dither_lo(hq), dither_hi(hq));
+    }
+};
+
+template <int Q, typename S>
+__device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
+                                               const DirOffsets& o)
+{
+    using L = Lattice<Q>;
+    constexpr unsigned kFull = 0xffffffffu;
+    const int          np = p.nx >> 1;  // pairs per row
+    const int          t = blockIdx.x * kPairBlock + threadIdx.x;
+    const int          lane = threadIdx.x & 31;
+    const bool         live = t < np;
+    const int          tp = live ? t : np - 1;  // idle lanes read the last pair (in the row, results unused)
+    const int          y = 2 + blockIdx.y, z = 2 + blockIdx.z;
+    const int64_t      cell = 2 * int64_t(tp) + int64_t(p.nx) * (y + int64_t(p.ny) * z);
+    const char*        P = reinterpret_cast<const char*>(fin + cell);
+    const bool         first = tp == 0, last = tp == np - 1;  // the pairs holding x = 1 and x = nx - 2
+    const unsigned     edge = __ballot_sync(kFull, live && (first || last));
+    float2             g[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int   cx = L::cx(q);
+        const char* src = P + o.pull[q];  // the pull source of the pair's first cell
+        uint32_t    w;
+        if (cx == 0) {
+            w = ldg_u32(src);
+        } else if (cx > 0) {  // sources 2t-1, 2t
+            const uint32_t own = ldg_u32(src + 2);
+            uint32_t       left = __shfl_up_sync(kFull, own, 1);
+            if (lane == 0) left = ldg_u16(src) << 16;
+            w = __byte_perm(left, own, 0x5432);
+        } else {  // sources 2t+1, 2t+2
+            const uint32_t own = ldg_u32(src - 2);
+            uint32_t       right = __shfl_down_sync(kFull, own, 1);
+            if (lane == 31) right = ldg_u16(src + 2);
+            w = __byte_perm(own, right, 0x5432);
+        }
+        g[q] = PairBits<S>::to_g(w);
+        if (edge && cx != 0) {  // warp-uniform: the warp holds a row end
+            const int oq = L::opp(q);
+            if (cx > 0 && first) g[q].y = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).y + p.wall[0][oq];
+            if (cx < 0 && last) g[q].x = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).x + p.wall[0][oq];
+        }
+    }
+    bgk_shifted<Q, float2, StoreScale<S>::log2>(g, p.omega);
+    if (!live) return;
+    char*          D = reinterpret_cast<char*>(fout + cell);
+    const uint32_t h = dither_base<S>(cell, p.seed);  // one hash per pair (cell is even)
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        uint32_t w;
+        if constexpr (PairIO<S>::kStochastic)
+            w = PairBits<S>::from_g_sr(g[q], dither_word(h, q));
+        else
+            w = PairBits<S>::from_g(g[q]);
+        if (!(first || last)) {
+            *reinterpret_cast<unsigned int*>(D + o.own[q]) = w;
+        } else if (first) {  // x = 0 is a wall node
+            *reinterpret_cast<unsigned short*>(D + o.own[q] + 2) = static_cast<unsigned short>(w >> 16);
+        } else {  // x = nx - 1 is a wall node
+            *reinterpret_cast<unsigned short*>(D + o.own[q]) = static_cast<unsigned short>(w & 0xffffu);
+        }
+    }
+}
+
+template <int Q, typename S>
+__global__ void __launch_bounds__(kPairBlock) lbm_box_core_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                      DenseParams<float> p, const __grid_constant__ DirOffsets o)
+{
+    core_pair_body<Q, S>(fin, fout, p, o);
 }
 
 // The rest of the analytic cavity's bulk cells: the planes z = 1 and

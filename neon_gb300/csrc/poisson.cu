@@ -859,6 +859,54 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
     return NGB_OK;
 }
 
+template <typename T>
+int time_passes_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace& w, int reps, float* ms, cudaStream_t s)
+{
+    const Dom d = make_dom(desc);
+    const int grid = grid_for(d.segs);
+    CgState   init{};
+    init.tol = 0.0;                  // never converged while timing
+    init.refresh_every = 1 << 30;    // no refresh inside the timed passes
+    init.max_iter = 1 << 30;
+    init.jacobi = 1;
+    NGB_CUDA_TRY(cudaMemcpyAsync(w.st, &init, sizeof(CgState), cudaMemcpyHostToDevice, s));
+    T *r = static_cast<T*>(w.r), *p0 = static_cast<T*>(w.p0), *p1 = static_cast<T*>(w.p1), *sv = static_cast<T*>(w.s),
+      *xlo = static_cast<T*>(w.xlo);
+    cg_init_kernel<T><<<grid, kBX, 0, s>>>(d, w.st, b, x, r, p0, xlo, w.partials);
+    NGB_LAUNCH_CHECK("cg_init_kernel");
+    NGB_CUDA_TRY(cudaMemsetAsync(p1, 0, size_t(desc->nx) * desc->ny * desc->nz * sizeof(T), s));
+    const int   grid_a = std::min(grid, pass_a_items(d)), grid_b = std::min(grid, pass_b_items(d));
+    cudaEvent_t ev[3];
+    for (auto& e : ev) NGB_CUDA_TRY(cudaEventCreate(&e));
+    NGB_CUDA_TRY(cudaEventRecord(ev[0], s));
+    for (int it = 0; it < reps; it++) {
+        T* pa = (it % 2 == 0) ? p0 : p1;
+        T* pb = (it % 2 == 0) ? p1 : p0;
+        if (d.bd)
+            cg_pass_a_kernel<T, false><<<grid_a, kBX, 0, s>>>(d, w.st, r, pa, pb, sv, w.partials);
+        else
+            cg_pass_a_kernel<T, true><<<grid_a, kBX, 0, s>>>(d, w.st, r, pa, pb, sv, w.partials);
+    }
+    NGB_CUDA_TRY(cudaEventRecord(ev[1], s));
+    for (int it = 0; it < reps; it++) {
+        T* pb = (it % 2 == 0) ? p1 : p0;
+        if (d.bd)
+            cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, s>>>(d, w.st, xlo, pb, r, sv, w.partials);
+        else
+            cg_pass_b_kernel<T, true><<<grid_b, kBX, 0, s>>>(d, w.st, xlo, pb, r, sv, w.partials);
+    }
+    NGB_CUDA_TRY(cudaEventRecord(ev[2], s));
+    NGB_LAUNCH_CHECK("cg_pass_a/b_kernel");
+    NGB_CUDA_TRY(cudaEventSynchronize(ev[2]));
+    float a = 0.f, bb = 0.f;
+    NGB_CUDA_TRY(cudaEventElapsedTime(&a, ev[0], ev[1]));
+    NGB_CUDA_TRY(cudaEventElapsedTime(&bb, ev[1], ev[2]));
+    for (auto& e : ev) cudaEventDestroy(e);
+    ms[0] = a / float(reps);
+    ms[1] = bb / float(reps);
+    return NGB_OK;
+}
+
 }  // namespace
 }  // namespace ngb
 
@@ -953,6 +1001,7 @@ size_t ngb_cg_workspace_bytes(const ngb_poisson_desc* d)
 int ngb_cg_solve(const ngb_poisson_desc* d, const void* b, double* x, void* workspace, size_t workspace_bytes,
                  const ngb_cg_params* prm, ngb_cg_result* res, void* stream)
 {
+    NvtxRange nvtx("ngb_cg_solve");
     int rc = validate(d);
     if (rc) return rc;
     NGB_CHECK_ARG(b && x && workspace && prm, "NULL argument");
@@ -964,6 +1013,20 @@ int ngb_cg_solve(const ngb_poisson_desc* d, const void* b, double* x, void* work
     NGB_CUDA_TRY(cudaMemsetAsync(&w.st->ticket, 0, sizeof(unsigned int), as_stream(stream)));
     if (d->field == NGB_STORE_F64) return solve_t<double>(d, static_cast<const double*>(b), x, w, prm, res, as_stream(stream));
     return solve_t<float>(d, static_cast<const float*>(b), x, w, prm, res, as_stream(stream));
+}
+
+int ngb_cg_time_passes(const ngb_poisson_desc* d, const void* b, double* x, void* workspace, size_t workspace_bytes,
+                       int32_t reps, float* ms, void* stream)
+{
+    int rc = validate(d);
+    if (rc) return rc;
+    NGB_CHECK_ARG(b && x && workspace && ms && reps >= 1, "bad argument");
+    NGB_CHECK_ARG((reinterpret_cast<uintptr_t>(workspace) & 255) == 0, "workspace must be 256-byte aligned");
+    const Workspace w = layout(d, workspace);
+    NGB_CHECK_ARG(workspace_bytes >= w.bytes, "workspace too small (%zu < %zu)", workspace_bytes, w.bytes);
+    NGB_CUDA_TRY(cudaMemsetAsync(&w.st->ticket, 0, sizeof(unsigned int), as_stream(stream)));
+    if (d->field == NGB_STORE_F64) return time_passes_t<double>(d, static_cast<const double*>(b), x, w, reps, ms, as_stream(stream));
+    return time_passes_t<float>(d, static_cast<const float*>(b), x, w, reps, ms, as_stream(stream));
 }
 
 int ngb_poisson_rhs(const ngb_poisson_desc* d, const double* centres, const double* amps, double sigma, void* f, void* stream)

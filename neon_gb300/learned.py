@@ -283,8 +283,36 @@ class UNet:
     def state_dict(self):
         return {k: v.cpu() for k, v in self.w.items()}
 
+    def flat_weights(self):
+        """The FP32 master weights as one host array in the layer order of the weight file."""
+        return torch.cat([self.w[name].reshape(-1).cpu() for name, _, _ in LAYERS]).contiguous()
+
+    def save_weights(self, path):
+        """Writes the weight file (BF16 values, the precision the network computes in)."""
+        w = self.flat_weights()
+        check(lib().ngb_unet_write_weights(str(path).encode(), ctypes.c_void_p(w.data_ptr()), w.numel()))
+
+    def load_weights(self, path):
+        """Reads a weight file written by save_weights (or by ngb_unet_write_weights)."""
+        w = read_weights(path)
+        off = 0
+        for name, cin, cout in LAYERS:
+            cnt = cout * 27 * cin
+            self.w[name].copy_(w[off:off + cnt].reshape(cout, 27, cin).to(self.dev))
+            self.wb[name].copy_(self.w[name].to(torch.bfloat16))
+            off += cnt
+        self._refresh_flipped()
+
     def load_state_dict(self, sd):
         for k, v in sd.items():
             self.w[k].copy_(v.to(self.dev))
             self.wb[k].copy_(self.w[k].to(torch.bfloat16))
         self._refresh_flipped()
+
+
+def read_weights(path):
+    """FP32 host tensor of a U-Net weight file (ngb_unet_read_weights)."""
+    L = lib()
+    w = torch.empty(int(L.ngb_unet_weight_count()), dtype=torch.float32)
+    check(L.ngb_unet_read_weights(str(path).encode(), ctypes.c_void_p(w.data_ptr()), w.numel()))
+    return w

@@ -58,6 +58,10 @@ def lib():
                                    c_void_p]
         L.orc_time_d3q19_f32.argtypes = [c_int, c_int, c_int, c_int, c_int, c_double, c_void_p, c_void_p, c_void_p]
         L.orc_time_d3q19_f32.restype = c_double
+        L.orc_set_zouhe.argtypes = [c_double, c_double, c_double, c_double]
+        L.orc_set_dither_seed.argtypes = [ctypes.c_uint32]
+        L.orc_f32_to_f16_sr.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t]
+        L.orc_dither_bits.argtypes = [c_void_p, c_void_p, ctypes.c_uint32, c_void_p, c_size_t]
         for f in ("orc_f32_to_f16", "orc_f16_to_f32", "orc_f32_to_bf16", "orc_bf16_to_f32"):
             getattr(L, f).argtypes = [c_void_p, c_void_p, c_size_t]
         L.orc_bgrid_build.argtypes = [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p]

@@ -63,9 +63,44 @@ inline double w27(int q)
 
 // ---------------------------------------------------------------- cell type
 // CellType.h:3-35: {uint32 wallNghBitflag; classification}.
-// outlet (zero-gradient outflow: copies the x-1 neighbour) is the project's own addition.
-enum Classification : int { bounceBack = 0, movingWall = 1, bulk = 2, undefined = 3, outlet = 4 };
-inline bool is_fluid(int c) { return c == bulk || c == outlet; }
+// outlet (zero-gradient outflow: copies the x-1 neighbour) is the project's own addition;
+// pressure / velocity are Zou-He boundary nodes (the classes of
+// benchmarks/lbm-flow-over-sphere/src/CellType.h), defined below.
+enum Classification : int { bounceBack = 0, movingWall = 1, bulk = 2, undefined = 3, outlet = 4, pressure = 5, velocity = 6 };
+inline bool is_zouhe(int c) { return c == pressure || c == velocity; }
+inline bool is_fluid(int c) { return c == bulk || c == outlet || is_zouhe(c); }
+
+// ---------------------------------------------------------------- Zou-He boundary nodes
+// The project's definition of the pressure / velocity boundary of the
+// flow-over-sphere benchmark (LbmContainers.h:53-290 there), as the
+// non-equilibrium bounce-back of Zou & He (1997) on D3Q19:
+// * a Zou-He node lies on a face of the box; its inward normal n is that of
+//   the first face it lies on, in the order x = 0, x = nx-1, y = 0, y = ny-1,
+//   z = 0, z = nz-1 (axis a, sign s = +1 on the low face, -1 on the high one);
+// * it is updated every step: the 5 populations with s c_a = +1 arrive from
+//   outside the box and are unknown; the others stream (pull, with the wall
+//   rule for masked directions; an out-of-box source counts as a resting wall);
+// * M = sum of the known populations with c_a = 0, K = sum of those with
+//   s c_a = -1 (q ascending); pressure nodes take rho = rho_b and the normal
+//   velocity s u_a = 1 - (M + 2K) / rho_b, tangential velocity 0 (as the
+//   reference's streamAndZouhe); velocity nodes take u = u_b and
+//   rho = (M + 2K) / (1 - s u_b,a);
+// * the unknowns follow f_q = f_opp(q) + eq_q - eq_opp(q), and the node
+//   collides with eq(rho, u) of the boundary values (the reference collides
+//   its Zou-He nodes with the boundary rho and u, not with re-summed moments).
+struct ZouHe {
+    double rho = 1.0;
+    double u[3] = {0.0, 0.0, 0.0};
+};
+inline void zouhe_normal(int x, int y, int z, int nx, int ny, int nz, int& a, int& s)
+{
+    if (x == 0) a = 0, s = 1;
+    else if (x == nx - 1) a = 0, s = -1;
+    else if (y == 0) a = 1, s = 1;
+    else if (y == ny - 1) a = 1, s = -1;
+    else if (z == 0) a = 2, s = 1;
+    else a = 2, s = -1;
+}
 struct CellType {
     uint32_t wallNghBitflag = 0;
     int      classification = bulk;
@@ -122,6 +157,58 @@ inline float f16_to_f32(uint16_t h)
     std::memcpy(&f, &x, 4);
     return f;
 }
+// IEEE binary16 with round toward zero (truncation of the dropped bits).
+inline uint16_t f32_to_f16_rz(float f)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t ax = x & 0x7fffffffu;
+    if (ax >= 0x7f800000u) return uint16_t(sign | 0x7c00u | (ax > 0x7f800000u ? 0x200u : 0u));
+    if (ax >= 0x47800000u) return uint16_t(sign | 0x7bffu);  // |f| >= 65536: largest finite (toward zero)
+    if (ax < 0x38800000u) {                                   // half subnormal or zero
+        const int e = int(ax >> 23);
+        if (e == 0) return uint16_t(sign);
+        const uint32_t m = (ax & 0x7fffffu) | 0x800000u;
+        const int      shift = 126 - e;
+        if (shift >= 32) return uint16_t(sign);
+        return uint16_t(sign | (m >> shift));
+    }
+    return uint16_t(sign | ((((ax >> 23) - 127u + 15u) << 10) | ((ax & 0x7fffffu) >> 13)));
+}
+
+// Stochastic rounding of FP16 offset storage (the library's F16SR): the random
+// bits r of cell i, population q, step seed s, added to the FP32 bit pattern
+// of the (scaled) value, then truncated:
+//   h = mix32(lo32(i >> 1) ^ (hi32(i >> 1) * 0x9E3779B1) ^ (s * 0x85EBCA77))
+//   hq = (h ^ (q * 0x9E3779B9)) * 0xC2B2AE35;  r = i odd ? (hq >> 6) & 0x1FFF : hq >> 19
+// mix32 is Wellons' lowbias32 integer hash.
+inline uint32_t dither_mix32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+inline uint32_t dither_bits(uint64_t cell, int q, uint32_t seed)
+{
+    const uint64_t pr = cell >> 1;
+    const uint32_t h = dither_mix32(uint32_t(pr) ^ (uint32_t(pr >> 32) * 0x9E3779B1u) ^ (seed * 0x85EBCA77u));
+    const uint32_t hq = (h ^ (uint32_t(q) * 0x9E3779B9u)) * 0xC2B2AE35u;
+    return (cell & 1) ? ((hq >> 6) & 0x1fffu) : (hq >> 19);
+}
+inline uint16_t f32_to_f16_sr(float f, uint32_t r)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    x += r;
+    float g;
+    std::memcpy(&g, &x, 4);
+    return f32_to_f16_rz(g);
+}
+
 inline uint16_t f32_to_bf16(float f)
 {
     uint32_t x;
@@ -210,7 +297,7 @@ inline void compute_wall_mask(int nx, int ny, int nz, int Q, CellType* flag)
             for (int x = 0; x < nx; x++) {
                 CellType c = in[lin(x, y, z, nx, ny)];
                 c.wallNghBitflag = 0;
-                if (c.classification != bulk) continue;
+                if (c.classification != bulk && !is_zouhe(c.classification)) continue;
                 for (int q = 0; q < Q; q++) {
                     const int cx = Q == 19 ? kC19[q][0] : c27(q, 0);
                     const int cy = Q == 19 ? kC19[q][1] : c27(q, 1);
@@ -228,17 +315,83 @@ inline void compute_wall_mask(int nx, int ny, int nz, int Q, CellType* flag)
 // ---------------------------------------------------------------- D3Q19 step (reference arithmetic)
 // One pull stream-collide step over every bulk cell (LbmTools.h:284-325).
 // S = storage type, C = compute type.
+// Reference-shape equilibria of D3Q19 (collideBgkUnrolled, LbmTools.h:198-282):
+// eq[k] for the go directions k = 0..8, eq[k+10] = eq[k] + rho w 6 (c_{k+10}.u), eq[9].
+template <typename C>
+void d3q19_eq(C rho, C u0, C u1, C u2, C usqr, C* eq)
+{
+    const C cu[9] = {u0, u1, u2, u0 + u1, u0 - u1, u0 + u2, u0 - u2, u1 + u2, u1 - u2};
+    for (int k = 0; k < 9; k++) {
+        const double wk = k < 3 ? (1. / 18.) : (1. / 36.);
+        eq[k] = rho * wk * (1. - 3. * cu[k] + 4.5 * cu[k] * cu[k] - usqr);
+        eq[k + 10] = eq[k] + rho * wk * 6. * cu[k];
+    }
+    eq[9] = rho * (1. / 3.) * (1. - usqr);
+}
+
+// Zou-He node in the reference's arithmetic (FP64 / FP32 compute C).
+// `wall` gives the wall term of a masked direction by the source's class.
+template <typename S, typename C, typename At, typename WallTerm>
+void zouhe_node_ref(int x, int y, int z, int nx, int ny, int nz, const CellType& cell, C omega, const ZouHe& zh, At at,
+                    WallTerm wall, C* out)
+{
+    int a, s;
+    zouhe_normal(x, y, z, nx, ny, nz, a, s);
+    C pop[19];
+    for (int q = 0; q < 19; q++) {
+        if (kC19[q][a] * s == 1) continue;  // unknown
+        const int sx = x - kC19[q][0], sy = y - kC19[q][1], sz = z - kC19[q][2];
+        if (cell.wallNghBitflag & (uint32_t(1) << q)) {
+            const bool inside = sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz;
+            pop[q] = static_cast<C>(at(x, y, z, opp19(q))) + C(wall(inside, sx, sy, sz, opp19(q)));
+        } else {
+            pop[q] = static_cast<C>(at(sx, sy, sz, q));
+        }
+    }
+    C M = 0, K = 0;
+    for (int q = 0; q < 19; q++) {
+        if (kC19[q][a] == 0) M = M + pop[q];
+        else if (kC19[q][a] * s == -1) K = K + pop[q];
+    }
+    C rho, u[3] = {0, 0, 0};
+    if (cell.classification == pressure) {
+        rho = C(zh.rho);
+        u[a] = C(s) * (C(1) - (M + C(2) * K) / rho);
+    } else {
+        for (int d = 0; d < 3; d++) u[d] = C(zh.u[d]);
+        rho = (M + C(2) * K) / (C(1) - C(s) * u[a]);
+    }
+    const C usqr = 1.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    C       eq[19];
+    d3q19_eq<C>(rho, u[0], u[1], u[2], usqr, eq);
+    for (int q = 0; q < 19; q++)
+        if (kC19[q][a] * s == 1) pop[q] = pop[opp19(q)] + eq[q] - eq[opp19(q)];
+    for (int q = 0; q < 19; q++) out[q] = (1. - omega) * pop[q] + omega * eq[q];
+}
+
 template <typename S, typename C>
 void d3q19_step(int nx, int ny, int nz, const S* fin, S* fout, const CellType* flag, C omega,
-                int z_begin = 0, int z_end = -1)
+                int z_begin = 0, int z_end = -1, const ZouHe* zh = nullptr, const double (*wallt)[27] = nullptr)
 {
     const size_t V = size_t(nx) * ny * nz;
     if (z_end < 0) z_end = nz;
     auto at = [&](int x, int y, int z, int q) -> S { return fin[size_t(q) * V + lin(x, y, z, nx, ny)]; };
+    auto zwall = [&](bool inside, int sx, int sy, int sz, int q) -> double {
+        if (!wallt) return 0.0;
+        if (!inside) return wallt[0][q];  // out of the box: a resting wall
+        return flag[lin(sx, sy, sz, nx, ny)].classification == movingWall ? wallt[1][q] : wallt[0][q];
+    };
     for (int z = z_begin; z < z_end; z++)
         for (int y = 0; y < ny; y++)
             for (int x = 0; x < nx; x++) {
                 const CellType cell = flag[lin(x, y, z, nx, ny)];
+                if (is_zouhe(cell.classification)) {
+                    if (!zh) continue;
+                    C out[19];
+                    zouhe_node_ref<S, C>(x, y, z, nx, ny, nz, cell, omega, *zh, at, zwall, out);
+                    for (int q = 0; q < 19; q++) fout[size_t(q) * V + lin(x, y, z, nx, ny)] = static_cast<S>(out[q]);
+                    continue;
+                }
                 if (cell.classification == outlet) {
                     if (x > 0 && flag[lin(x - 1, y, z, nx, ny)].classification != undefined)
                         for (int q = 0; q < 19; q++) fout[size_t(q) * V + lin(x, y, z, nx, ny)] = at(x - 1, y, z, q);
@@ -375,9 +528,70 @@ void bgk_step_generic(int nx, int ny, int nz, const CellType* flag, C omega, Loa
 //   per q: t = c_q . u3 (signed adds in x, y, z order); a = fma(0.5 * t, t, t)
 //          eqg = fma(wr, a, wb); g' = fma(omega, eqg - g, g)
 // Wall rule as the reference step: bit q set -> g(x, opp q) + wall term.
+// Zou-He node in the shifted FP32 form (see ZouHe above), g = f - w:
+//   M, K as above on g (float adds, q ascending), mk = M + (K + K);
+//   pressure: drho = float(rho_b - 1), rho = 1 + drho, s u_a = (drho - mk) / rho;
+//   velocity: u = float(u_b), un = s u_a, drho = (mk + un) / (1 - un), rho = 1 + drho;
+//   unknowns: g_q = fma((2 w_q) rho, t_q, g_opp(q)) with t_q = c_q . 3u
+//   (f_q - f_opp(q) = eq_q - eq_opp(q) = 6 w rho c_q.u); then the relaxation
+//   of the shifted BGK with these drho and u.
+template <int Q>
+void zouhe_node_shifted(int x, int y, int z, int nx, int ny, int nz, const CellType& cell, float omega, float zh_drho,
+                        const float* zh_u, const float* g_known, float* out)
+{
+    int a, s;
+    zouhe_normal(x, y, z, nx, ny, nz, a, s);
+    float g[19];
+    for (int q = 0; q < 19; q++) g[q] = g_known[q];
+    float M = 0.f, K = 0.f;
+    for (int q = 0; q < 19; q++) {
+        if (kC19[q][a] == 0) M = M + g[q];
+        else if (kC19[q][a] * s == -1) K = K + g[q];
+    }
+    const float mk = M + (K + K);
+    float       u[3] = {0.f, 0.f, 0.f}, drho, rho;
+    if (cell.classification == pressure) {
+        drho = zh_drho;
+        rho = 1.f + drho;
+        u[a] = float(s) * ((drho - mk) / rho);
+    } else {
+        for (int d = 0; d < 3; d++) u[d] = zh_u[d];
+        const float un = float(s) * u[a];
+        drho = (mk + un) / (1.f - un);
+        rho = 1.f + drho;
+    }
+    const float u3[3] = {3.f * u[0], 3.f * u[1], 3.f * u[2]};
+    auto        tdot = [&](int q) {
+        float t = 0.f;
+        bool  started = false;
+        for (int d = 0; d < 3; d++) {
+            if (kC19[q][d] == 0) continue;
+            if (!started) {
+                t = kC19[q][d] > 0 ? u3[d] : -u3[d];
+                started = true;
+            } else {
+                t = kC19[q][d] > 0 ? t + u3[d] : t - u3[d];
+            }
+        }
+        return t;
+    };
+    for (int q = 0; q < 19; q++)
+        if (kC19[q][a] * s == 1) g[q] = std::fmaf((2.f * float(kW19[q])) * rho, tdot(q), g[opp19(q)]);
+    const float usq = std::fmaf(u[2], u[2], std::fmaf(u[1], u[1], u[0] * u[0]));
+    const float rus = rho * (1.5f * usq);
+    const float base = drho - rus;
+    for (int q = 0; q < 19; q++) {
+        const float w = float(kW19[q]), wr = w * rho, wb = w * base;
+        const float t = tdot(q);
+        const float aa = std::fmaf(0.5f * t, t, t);
+        const float eqg = std::fmaf(wr, aa, wb);
+        out[q] = std::fmaf(omega, eqg - g[q], g[q]);
+    }
+}
+
 template <int Q, typename LoadG, typename StoreG, typename WallTerm>
 void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega, LoadG loadg, StoreG storeg, WallTerm wall,
-                      int z_begin = 0, int z_end = -1)
+                      int z_begin = 0, int z_end = -1, const ZouHe* zh = nullptr)
 {
     if (z_end < 0) z_end = nz;
     int   c[Q][3], op[Q];
@@ -394,6 +608,27 @@ void bgk_step_shifted(int nx, int ny, int nz, const CellType* flag, float omega,
                 if (cell.classification == outlet) {
                     if (x > 0 && flag[lin(x - 1, y, z, nx, ny)].classification != undefined)
                         for (int q = 0; q < Q; q++) storeg(x, y, z, q, loadg(x - 1, y, z, q));
+                    continue;
+                }
+                if (Q == 19 && is_zouhe(cell.classification)) {
+                    if (!zh) continue;
+                    int za, zs;
+                    zouhe_normal(x, y, z, nx, ny, nz, za, zs);
+                    float gk[19] = {}, zo[19];
+                    for (int q = 0; q < 19; q++) {
+                        if (c[q][za] * zs == 1) continue;
+                        const int sx = x - c[q][0], sy = y - c[q][1], sz = z - c[q][2];
+                        if (cell.wallNghBitflag & (uint32_t(1) << q)) {
+                            int cls = undefined;
+                            if (sx >= 0 && sy >= 0 && sz >= 0 && sx < nx && sy < ny && sz < nz) cls = flag[lin(sx, sy, sz, nx, ny)].classification;
+                            gk[q] = loadg(x, y, z, op[q]) + float(wall(cls, op[q]));
+                        } else {
+                            gk[q] = loadg(sx, sy, sz, q);
+                        }
+                    }
+                    const float zu[3] = {float(zh->u[0]), float(zh->u[1]), float(zh->u[2])};
+                    zouhe_node_shifted<19>(x, y, z, nx, ny, nz, cell, omega, float(zh->rho - 1.0), zu, gk, zo);
+                    for (int q = 0; q < 19; q++) storeg(x, y, z, q, zo[q]);
                     continue;
                 }
                 if (cell.classification != bulk) continue;

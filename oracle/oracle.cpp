@@ -23,7 +23,7 @@ using namespace oracle;
 
 namespace {
 
-enum Storage { ST_F64 = 0, ST_F32 = 1, ST_F16OFF = 2, ST_BF16OFF = 3 };
+enum Storage { ST_F64 = 0, ST_F32 = 1, ST_F16OFF = 2, ST_BF16OFF = 3, ST_F16SR = 4 };
 // FP16 offset storage holds fp16(2^14 g) (the library's NGB_F16OFF_SCALE); both factors are exact
 constexpr float kF16Up = 16384.0f, kF16Down = 1.0f / 16384.0f;
 enum ComputeMode { CM_REFERENCE = 0, CM_GENERIC = 1, CM_SHIFTED = 2 };
@@ -39,7 +39,9 @@ inline CellType unpack(uint32_t f)
 }
 inline uint32_t pack(const CellType& c) { return (c.wallNghBitflag & 0x07ffffffu) | (uint32_t(c.classification) << 28); }
 
-double g_wall[4][27];  // wall terms by classification (set per run)
+double   g_wall[4][27];  // wall terms by classification (set per run)
+uint32_t g_dither_seed = 0;  // F16SR: step t of a run uses seed g_dither_seed + (t mod 32)
+ZouHe  g_zh;           // Zou-He boundary values (orc_set_zouhe)
 
 double weight(int Q, int q) { return Q == 19 ? kW19[q] : w27(q); }
 
@@ -66,10 +68,14 @@ void shifted_run(int nx, int ny, int nz, const CellType* flag, float omega, S* a
         const S* fin = (t % 2 == 0) ? a : b;
         S*       fout = (t % 2 == 0) ? b : a;
         auto     loadg = [&](int x, int y, int z, int q) -> float { return toG(fin[size_t(q) * V + lin(x, y, z, nx, ny)], q); };
-        auto     storeg = [&](int x, int y, int z, int q, float g) { fout[size_t(q) * V + lin(x, y, z, nx, ny)] = fromG(g, q); };
+        const uint32_t seed = g_dither_seed + uint32_t(t % 32);
+        auto           storeg = [&](int x, int y, int z, int q, float g) {
+            const size_t i = lin(x, y, z, nx, ny);
+            fout[size_t(q) * V + i] = fromG(g, q, i, seed);
+        };
         auto     wall = [&](int cls, int q) -> double { return cls == movingWall ? g_wall[1][q] : g_wall[0][q]; };
 #pragma omp parallel for schedule(static) num_threads(threads)
-        for (int z = 0; z < nz; z++) bgk_step_shifted<Q>(nx, ny, nz, flag, omega, loadg, storeg, wall, z, z + 1);
+        for (int z = 0; z < nz; z++) bgk_step_shifted<Q>(nx, ny, nz, flag, omega, loadg, storeg, wall, z, z + 1, &g_zh);
     }
 }
 
@@ -78,6 +84,31 @@ void shifted_run(int nx, int ny, int nz, const CellType* flag, float omega, S* a
 extern "C" {
 
 int orc_version() { return 3; }
+
+// Zou-He boundary values of the following runs: pressure nodes rho, velocity nodes (ux, uy, uz).
+// F16SR: seed of the first step of the following runs (step t uses seed + t mod 32).
+int orc_set_dither_seed(uint32_t seed)
+{
+    g_dither_seed = seed;
+    return 0;
+}
+
+// IEEE binary16 stochastic-rounding store of n values (the random bits given).
+void orc_f32_to_f16_sr(const float* in, const uint32_t* r, uint16_t* out, size_t n)
+{
+    for (size_t i = 0; i < n; i++) out[i] = f32_to_f16_sr(in[i], r[i]);
+}
+void orc_dither_bits(const uint64_t* cell, const int32_t* q, uint32_t seed, uint32_t* out, size_t n)
+{
+    for (size_t i = 0; i < n; i++) out[i] = dither_bits(cell[i], q[i], seed);
+}
+
+int orc_set_zouhe(double rho, double ux, double uy, double uz)
+{
+    g_zh.rho = rho;
+    g_zh.u[0] = ux, g_zh.u[1] = uy, g_zh.u[2] = uz;
+    return 0;
+}
 
 int orc_max_threads()
 {
@@ -150,13 +181,15 @@ int orc_lbm_run(int nx, int ny, int nz, int Q, int storage, int mode, int comput
                 const double* fin = static_cast<const double*>(t % 2 == 0 ? a : b);
                 double*       fout = static_cast<double*>(t % 2 == 0 ? b : a);
 #pragma omp parallel for schedule(static) num_threads(threads)
-                for (int z = 0; z < nz; z++) d3q19_step<double, double>(nx, ny, nz, fin, fout, flag.data(), omega, z, z + 1);
+                for (int z = 0; z < nz; z++)
+                    d3q19_step<double, double>(nx, ny, nz, fin, fout, flag.data(), omega, z, z + 1, &g_zh, g_wall);
             } else if (storage == ST_F32) {
                 const float* fin = static_cast<const float*>(t % 2 == 0 ? a : b);
                 float*       fout = static_cast<float*>(t % 2 == 0 ? b : a);
                 const float  om = float(omega);
 #pragma omp parallel for schedule(static) num_threads(threads)
-                for (int z = 0; z < nz; z++) d3q19_step<float, float>(nx, ny, nz, fin, fout, flag.data(), om, z, z + 1);
+                for (int z = 0; z < nz; z++)
+                    d3q19_step<float, float>(nx, ny, nz, fin, fout, flag.data(), om, z, z + 1, &g_zh, g_wall);
             } else {
                 return -2;
             }
@@ -171,16 +204,21 @@ int orc_lbm_run(int nx, int ny, int nz, int Q, int storage, int mode, int comput
             if (storage == ST_F32) {
                 shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<float*>(a), static_cast<float*>(b), steps,
                                 [](float v, int q) { return v - float(weight(QQ, q)); },
-                                [](float g, int q) { return float(weight(QQ, q)) + g; }, threads);
+                                [](float g, int q, size_t, uint32_t) { return float(weight(QQ, q)) + g; }, threads);
             } else if (storage == ST_F16OFF) {
                 shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
                                 [](uint16_t v, int) { return f16_to_f32(v) * kF16Down; },
-                                [](float g, int) { return f32_to_f16(g * kF16Up); },
+                                [](float g, int, size_t, uint32_t) { return f32_to_f16(g * kF16Up); },
+                                threads);
+            } else if (storage == ST_F16SR) {
+                shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
+                                [](uint16_t v, int) { return f16_to_f32(v) * kF16Down; },
+                                [](float g, int q, size_t i, uint32_t seed) { return f32_to_f16_sr(g * kF16Up, dither_bits(i, q, seed)); },
                                 threads);
             } else if (storage == ST_BF16OFF) {
                 shifted_run<QQ>(nx, ny, nz, flag.data(), om, static_cast<uint16_t*>(a), static_cast<uint16_t*>(b), steps,
-                                [](uint16_t v, int) { return bf16_to_f32(v); }, [](float g, int) { return f32_to_bf16(g); },
-                                threads);
+                                [](uint16_t v, int) { return bf16_to_f32(v); },
+                                [](float g, int, size_t, uint32_t) { return f32_to_bf16(g); }, threads);
             }
         };
         if (storage == ST_F64) return -2;
@@ -239,6 +277,7 @@ int orc_velocity(int nx, int ny, int nz, int Q, int storage, const double* wall,
             case ST_F64: return static_cast<const double*>(pop)[i];
             case ST_F32: return static_cast<const float*>(pop)[i];
             case ST_F16OFF:
+            case ST_F16SR:
                 return double(f16_to_f32(static_cast<const uint16_t*>(pop)[i]) * kF16Down) + double(float(weight(Q, q)));
             default: return double(bf16_to_f32(static_cast<const uint16_t*>(pop)[i])) + double(float(weight(Q, q)));
         }

@@ -11,7 +11,7 @@ def P(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
-STORE_DTYPE = {0: np.float64, 1: np.float32, 2: np.uint16, 3: np.uint16}
+STORE_DTYPE = {0: np.float64, 1: np.float32, 2: np.uint16, 3: np.uint16, 4: np.uint16}
 
 
 def wall_table(q, ulb, storage):
@@ -36,7 +36,7 @@ def oracle_cavity(orc, n, q, storage, steps, ulb=0.1, re=100.0, mode=None, compu
     b = a.copy()
     omega = ngb.cavity_omega(n, ulb, re)
     if mode is None:
-        mode = 0 if (q == 19 and storage in (0, 1)) else (2 if storage in (2, 3) else 1)
+        mode = 0 if (q == 19 and storage in (0, 1)) else (2 if storage in (2, 3, 4) else 1)
     if compute_float is None:
         compute_float = 0 if storage == 0 else 1
     wt = wall_table(q, ulb, storage)

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 def _tdtype(storage):
     import torch
-    return {0: torch.float64, 1: torch.float32, 2: torch.float16, 3: torch.bfloat16}[storage]
+    return {0: torch.float64, 1: torch.float32, 2: torch.float16, 3: torch.bfloat16, 4: torch.float16}[storage]
 
 
 @pytest.mark.parametrize("dims,kind", CASES)

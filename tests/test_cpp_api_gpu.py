@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "tests", "cpp")
 BUILD = os.path.join(CPP, "_build")
-PROGRAMS = ["api_stencil", "api_lbm", "api_poisson", "api_dataview"]
+PROGRAMS = ["api_stencil", "api_lbm", "api_poisson", "api_dataview", "api_learned"]
 
 
 def _compile(name):
@@ -128,3 +128,30 @@ def test_data_views_and_occ(programs):
     internal) and a Skeleton with Occ::standard give the STANDARD result."""
     out = _run(programs["api_dataview"])
     assert out.count("ok=1") == 8 and "ok=0" not in out, out
+
+
+def test_learned_fcg_t(programs, ngb, cuda, tmp_path):
+    """LearnedFCG_t::solve through the C++ API on the 128^3 Gaussian-source
+    problem (weights from a file written by the library): converges to 1e-8
+    with the iteration count of the C-ABI solve (the same calls) and of the
+    Python orchestration within +-2."""
+    import torch
+    from neon_gb300 import fcg
+    from neon_gb300.learned import UNet
+    n, levels = 128, 1
+    net = UNet(seed=0, device=cuda)
+    wpath = tmp_path / "unet.ngbw"
+    net.save_weights(wpath)
+    net.load_weights(wpath)  # the BF16 values the file holds, so both paths run the same network
+    d = ngb.poisson_desc(n, n, n, "f32", 1.0)
+    c, a = ngb.gaussian_sources(n, n, n, 2024)
+    b = torch.empty(n ** 3, dtype=torch.float32, device=cuda)
+    ngb.poisson_rhs(d, torch.from_numpy(c).to(cuda), torch.from_numpy(a).to(cuda), 8.0, b)
+    b.cpu().numpy().tofile(str(tmp_path / "poisson_b.bin"))
+    out = _run(programs["api_learned"], tmp_path, n, wpath, levels)
+    assert "status=0" in out, out
+    its = int(out.split("iterations=")[1].split()[0])
+    x = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
+    ref = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, net, device=cuda), b, x, tol=1e-8, max_iter=2000, fallback=True)
+    assert ref["converged"]
+    assert abs(its - (ref["iterations"] + ref["fallback_iterations"])) <= 2, (out, ref)

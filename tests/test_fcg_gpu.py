@@ -1,9 +1,9 @@
 """Flexible CG with the learned U-Net preconditioner on the fine grid (small
 grids): the training data are solver-generated residual/error pairs, FCG
-reaches the 1e-8 true relative residual (through the Jacobi-PCG fallback if
-it stalls), agrees with Jacobi-PCG's solution, and, when it does not stall,
-needs fewer iterations than Jacobi-PCG; the trained network needs fewer
-iterations than the untrained one. The multilevel form, the one the
+reaches the 1e-8 true relative residual without the Jacobi-PCG fallback,
+agrees with Jacobi-PCG's solution and needs fewer iterations than
+Jacobi-PCG; the trained network needs fewer iterations than the untrained
+one. The multilevel form, the one the
 benchmark uses, is tested in test_mg_gpu.py."""
 import numpy as np
 import pytest
@@ -54,10 +54,11 @@ def test_fcg_converges_and_beats_jacobi_pcg(ngb, orc, cuda, trained):
     n = 32
     b = fcg.grf_k2(n, 999, cuda)
     x = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
-    # the fine-grid form can stall on an unlucky training run (BF16 output
-    # noise amplified by A); the stagnation test then hands over to Jacobi-PCG
+    # at 32^3 the fine-grid form converges without the Jacobi-PCG fallback
+    # (it stalls on larger grids, where the network's BF16 output noise,
+    # amplified by A, grows with n^2; the V-cycle form serves those)
     res = fcg.fcg_solve(net, b, x, tol=1e-8, max_iter=400, fallback=True)
-    assert res["converged"], res
+    assert res["converged"] and not res["fallback"], res
     # Jacobi-PCG on the same system
     d = ngb.poisson_desc(n, n, n, "f32", 1.0)
     ws = ngb.cg_workspace(d, cuda)
@@ -65,11 +66,9 @@ def test_fcg_converges_and_beats_jacobi_pcg(ngb, orc, cuda, trained):
     pcg = ngb.cg_solve(d, b, x2, ws, tol=1e-8, max_iter=5000, refresh_every=50, check_every=10, jacobi=True)
     assert pcg["converged"]
     assert float((x - x2).norm() / x2.norm()) < 1e-6
-    if not res["fallback"]:
-        assert res["iterations"] < pcg["iterations"], (res["iterations"], pcg["iterations"])
+    assert res["iterations"] < pcg["iterations"], (res["iterations"], pcg["iterations"])
     # the untrained network is worse than the trained one
     x3 = torch.zeros_like(x)
     raw = fcg.fcg_solve(UNet(seed=0, device=cuda), b, x3, tol=1e-8, max_iter=400, fallback=True)
     assert raw["converged"], raw
-    if not res["fallback"]:
-        assert res["iterations"] < raw["iterations"] + raw["fallback_iterations"], (res, raw)
+    assert res["iterations"] < raw["iterations"] + raw["fallback_iterations"], (res, raw)

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 def _tdtype(storage):
     import torch
-    return {0: torch.float64, 1: torch.float32, 2: torch.float16, 3: torch.bfloat16}[storage]
+    return {0: torch.float64, 1: torch.float32, 2: torch.float16, 3: torch.bfloat16, 4: torch.float16}[storage]
 
 
 def gpu_cavity(ngb, cuda, n, q, storage, steps, ulb=0.1, re=100.0, box=True, use_run=True):
@@ -150,7 +150,7 @@ def test_single_step_from_developed_state(ngb, orc, cuda, q, storage):
 
 @pytest.mark.parametrize("n", [18, 17])
 @pytest.mark.parametrize("q", [19, 27])
-@pytest.mark.parametrize("storage", [1, 2, 3])
+@pytest.mark.parametrize("storage", [1, 2, 3, 4])
 def test_shifted_forms_bit_exact_over_steps(ngb, orc, cuda, n, q, storage):
     """60 steps from the equilibrium start, even n (two cells per thread) and
     odd n (one cell per thread): bit-identical to the oracle's shifted form."""
@@ -166,7 +166,7 @@ def test_shifted_forms_bit_exact_over_steps(ngb, orc, cuda, n, q, storage):
 
 @pytest.mark.parametrize("dims", [(136, 21, 10), (256, 9, 7)])
 @pytest.mark.parametrize("q", [19, 27])
-@pytest.mark.parametrize("storage", [1, 2, 3])
+@pytest.mark.parametrize("storage", [1, 2, 3, 4])
 @pytest.mark.parametrize("box", [True, False])
 def test_non_cubic_bit_exact(ngb, orc, cuda, dims, q, storage, box):
     """Non-cubic lattices: two or three 128-cell x blocks (one partial), an odd
@@ -290,3 +290,24 @@ def test_release_graphs_then_rerun(ngb, cuda):
     # more distinct buffer pairs than the cache holds: old graphs are evicted, results unchanged
     outs = [gpu_cavity(ngb, cuda, 16, 19, 1, 64)[1] for _ in range(10)]
     assert all(torch.equal(o, a) for o in outs)
+
+
+@pytest.mark.parametrize("storage", [1, 2, 4])
+def test_checkpoint_resume_is_bit_identical(ngb, cuda, tmp_path, storage):
+    """Save after 64 steps, load into fresh buffers, run 36 more: the same bits
+    as 100 uninterrupted steps (the loader fills both ping-pong buffers; with
+    stochastic rounding the step seeds continue, as 64 = 0 mod 32)."""
+    import torch
+    n = 24
+    desc, ref, _ = gpu_cavity(ngb, cuda, n, 19, storage, 100)
+    desc, mid, _ = gpu_cavity(ngb, cuda, n, 19, storage, 64)
+    path = tmp_path / "cavity.ngbl"
+    ngb.lbm_dense_save(path, desc, mid, 64)
+    fa = torch.full_like(mid, float("nan"))
+    fb = torch.full_like(mid, float("nan"))
+    assert ngb.lbm_dense_load(path, desc, fa, fb) == 64
+    bits = (lambda t: t.view(torch.int16)) if storage != 1 else (lambda t: t)
+    assert torch.equal(bits(fa), bits(mid))
+    ngb.lbm_dense_run(desc, fa, fb, 36)
+    torch.cuda.synchronize()
+    assert torch.equal(bits(fa), bits(ref))
