@@ -32,6 +32,10 @@ extern "C" {
 const char* ngb_last_error(void);
 /* ABI version of the loaded library. */
 int ngb_version(void);
+/* sizeof of the ABI structs, for bindings that lay them out themselves:
+ * 0 ngb_lbm_dense_desc, 1 ngb_bgrid_desc, 2 ngb_poisson_desc, 3 ngb_cg_params,
+ * 4 ngb_cg_result, 5 ngb_learned_params, 6 ngb_learned_result; 0 otherwise. */
+size_t ngb_abi_struct_size(int32_t which);
 
 /* ------------------------------------------------------------------------
  * Lattice-Boltzmann populations

@@ -32,7 +32,7 @@ class LbmDenseDesc(ctypes.Structure):
                 ("q", ctypes.c_int32), ("storage", ctypes.c_int32), ("box_cavity", ctypes.c_int32),
                 ("plane_stride", ctypes.c_int64), ("omega", ctypes.c_double),
                 ("wall_term", (ctypes.c_double * 27) * 2), ("zouhe_rho", ctypes.c_double),
-                ("zouhe_u", ctypes.c_double * 3)]
+                ("zouhe_u", ctypes.c_double * 3), ("dither_seed", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
 
 
 def build(force=False):
@@ -216,8 +216,9 @@ def lid_wall_terms(q, ulb, ulid=(1.0, 0.0, 0.0)):
 
 
 def lbm_dense_desc(nx, ny, nz, q, storage, omega, moving_wall_terms=None, box_cavity=True, plane_stride=0,
-                   bounce_back_terms=None, zouhe_rho=1.0, zouhe_u=(0.0, 0.0, 0.0)):
+                   bounce_back_terms=None, zouhe_rho=1.0, zouhe_u=(0.0, 0.0, 0.0), dither_seed=0):
     d = LbmDenseDesc()
+    d.dither_seed = dither_seed
     d.zouhe_rho = zouhe_rho
     for a in range(3):
         d.zouhe_u[a] = zouhe_u[a]

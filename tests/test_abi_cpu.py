@@ -85,3 +85,16 @@ def test_new_entry_points_validate_without_gpu(ngb):
     assert L.ngb_unet_output(8, 8, 8, None, 16, None, 1.0, None, None) == -1
     assert L.ngb_scale_by_ratio(0, None, None, None, None) == -1
     assert L.ngb_fcg_scratch_doubles(1000) >= 3
+
+
+def test_ctypes_structs_match_the_c_layout(ngb):
+    """Every ABI struct the Python helpers lay out has the size the library was compiled with."""
+    import ctypes
+    L = ngb.lib()
+    L.ngb_abi_struct_size.restype = ctypes.c_size_t
+    L.ngb_abi_struct_size.argtypes = [ctypes.c_int32]
+    structs = [ngb.LbmDenseDesc, ngb.BGridDesc, ngb.PoissonDesc, ngb.CgParams, ngb.CgResult, ngb.LearnedParams,
+               ngb.LearnedResult]
+    for i, st in enumerate(structs):
+        assert L.ngb_abi_struct_size(i) == ctypes.sizeof(st), (st.__name__, L.ngb_abi_struct_size(i), ctypes.sizeof(st))
+    assert L.ngb_abi_struct_size(99) == 0
