@@ -459,6 +459,12 @@ int ngb_conv3d_tc(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx
                   const float* bias, void* y, int32_t ldy, int32_t cout, int32_t out_f32, int32_t relu, int32_t accumulate,
                   void* stream);
 int ngb_conv3d_tc_check(void* stream);
+/* Self-test of the kernels' bounded waits: one thread polls, `limit` times at
+ * most (1 .. 2^20), an mbarrier that nothing arrives on, with no copy or MMA
+ * in flight. The wait runs out and raises the same error flag a pipeline
+ * wait of ngb_conv3d_tc does; returns NGB_OK when it gave up as designed (the
+ * next ngb_conv3d_tc_check then returns NGB_ERR_TIMEOUT and clears the flag). */
+int ngb_conv3d_tc_wait_selftest(int32_t limit, void* stream);
 
 /* dw[co][t][ci] += sum_v dy[v][co] x[v+t][ci] (BF16 inputs, FP32 dw). */
 int ngb_conv3d_bwd_weight(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy, int32_t lddy,

@@ -175,6 +175,7 @@ _EXTRA_SIGNATURES.update({
     "ngb_conv3d_pack": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_conv3d_tc": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
     "ngb_conv3d_tc_check": ([_vp], ctypes.c_int),
+    "ngb_conv3d_tc_wait_selftest": ([ctypes.c_int32, _vp], ctypes.c_int),
 })
 
 

@@ -49,15 +49,32 @@ __device__ int g_tc_error;
 
 // Wait for the phase of `parity` to complete; false when this CTA has given up
 // (its own limit ran out, or another role's did).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, volatile int* abort_flag, uint32_t limit)
 {
-    for (uint32_t i = 0; i < kWaitLimit; i++) {
+    for (uint32_t i = 0; i < limit; i++) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
     }
     *abort_flag = 1;
     atomicExch(&g_tc_error, 1);
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
+{
+    return mbar_wait_for(bar, parity, abort_flag, kWaitLimit);
+}
+
+// Self-test of the bounded wait: one thread waits, `limit` polls at most, on
+// a barrier that nothing arrives on (no copy or MMA is issued), so the wait
+// runs out, raises the error flag and returns.
+__global__ void tc_wait_selftest_kernel(uint32_t limit, int* gave_up)
+{
+    __shared__ uint64_t bar;
+    __shared__ int      abort_flag;
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+    mbar_init_fence();
+    *gave_up = mbar_wait_for(&bar, 0, &abort_flag, limit) ? 0 : 1;
 }
 // Drain wait used on the way out: bounded, ignores the abort flag.
 __device__ __forceinline__ void mbar_drain(uint64_t* bar, uint32_t parity)
@@ -492,6 +509,29 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
 #undef NGB_TC
     set_error("unsupported cout %d", cout);
     return NGB_ERR_UNSUPPORTED;
+}
+
+int ngb_conv3d_tc_wait_selftest(int32_t limit, void* stream)
+{
+    NGB_CHECK_ARG(limit >= 1 && limit <= (1 << 20), "limit %d out of [1, 2^20]", limit);
+    int* gave_up = nullptr;
+    NGB_CUDA_TRY(cudaMalloc(&gave_up, sizeof(int)));
+    cudaStream_t s = as_stream(stream);
+    tc_wait_selftest_kernel<<<1, 1, 0, s>>>(uint32_t(limit), gave_up);
+    cudaError_t e = cudaGetLastError();
+    int         host = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&host, gave_up, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(gave_up);
+    if (e != cudaSuccess) {
+        set_error("wait self-test: %s", cudaGetErrorString(e));
+        return NGB_ERR_CUDA;
+    }
+    if (!host) {
+        set_error("wait self-test: the wait completed on a barrier nothing arrived on");
+        return NGB_ERR_CUDA;
+    }
+    return NGB_OK;
 }
 
 int ngb_conv3d_tc_check(void* stream)

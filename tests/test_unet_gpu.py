@@ -262,3 +262,28 @@ def test_unet_tensor_cores_match_mma_path_at_128(ngb, cuda):
     for name in g0:
         rel = float((g1[name] - g0[name]).norm() / max(float(g0[name].norm()), 1e-30))
         assert rel <= 2e-2, (name, rel)
+
+
+def test_bounded_wait_times_out_and_reports(ngb, cuda):
+    """A bounded mbarrier wait on a barrier nothing arrives on (no copy or MMA
+    in flight) gives up after its limit; the flag it raises is what
+    ngb_conv3d_tc_check reports as NGB_ERR_TIMEOUT, once, and the context
+    stays usable (a convolution afterwards still checks clean)."""
+    import torch
+    L = ngb.lib()
+    assert L.ngb_conv3d_tc_wait_selftest(4096, None) == 0, L.ngb_last_error()
+    assert L.ngb_conv3d_tc_check(None) == -5  # NGB_ERR_TIMEOUT
+    assert b"wait ran out" in L.ngb_last_error()
+    assert L.ngb_conv3d_tc_check(None) == 0  # the flag was cleared
+    assert L.ngb_conv3d_tc_wait_selftest(0, None) == -1  # limit out of range
+    nx, ny, nz = 16, 8, 4
+    cin = cout = 16
+    assert L.ngb_conv3d_tc_supported(nx, ny, nz, cin, cin, cout, cout) == 1
+    X = torch.randn(nx * ny * nz, cin, device=cuda).to(torch.bfloat16)
+    W = (torch.randn(cout, 27, cin, device=cuda) * 0.05).to(torch.bfloat16)
+    Wp = torch.empty_like(W)
+    ngb.check(L.ngb_conv3d_pack(cout, cin, ngb._ptr(W), ngb._ptr(Wp), None))
+    Y = torch.zeros(nx * ny * nz, cout, dtype=torch.float32, device=cuda)
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), None, ngb._ptr(Y), cout, cout, 1, 0, 0, None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    assert bool(torch.isfinite(Y).all())
