@@ -155,3 +155,37 @@ def test_learned_fcg_t(programs, ngb, cuda, tmp_path):
     ref = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, net, device=cuda), b, x, tol=1e-8, max_iter=2000, fallback=True)
     assert ref["converged"]
     assert abs(its - (ref["iterations"] + ref["fallback_iterations"])) <= 2, (out, ref)
+
+
+def test_learned_fcg_t_committed_weights(programs, ngb, cuda, tmp_path):
+    """LearnedFCG_t with the committed trained network
+    (neon_gb300/weights/unet_poisson_64.ngbw: trained at 64^3 on solver pairs
+    of k^-2 fields by bench.py --workload learned --train-n 64) on the 128^3
+    Gaussian-source problem, one V-cycle level above the network: reaches
+    1e-8 without the Jacobi-PCG fallback, in the iteration count of the
+    Python orchestration of the same kernels (+-2), and in far fewer
+    iterations than the same cycle without the network."""
+    import torch
+    from neon_gb300 import fcg
+    from neon_gb300.learned import UNet
+    n, levels = 128, 1
+    wpath = os.path.join(ROOT, "neon_gb300", "weights", "unet_poisson_64.ngbw")
+    net = UNet(seed=0, device=cuda)
+    net.load_weights(wpath)
+    d = ngb.poisson_desc(n, n, n, "f32", 1.0)
+    c, a = ngb.gaussian_sources(n, n, n, 2024)
+    b = torch.empty(n ** 3, dtype=torch.float32, device=cuda)
+    ngb.poisson_rhs(d, torch.from_numpy(c).to(cuda), torch.from_numpy(a).to(cuda), 8.0, b)
+    b.cpu().numpy().tofile(str(tmp_path / "poisson_b.bin"))
+    out = _run(programs["api_learned"], tmp_path, n, wpath, levels)
+    assert "status=0" in out and "fallback=0" in out, out
+    its = int(out.split("iterations=")[1].split()[0])
+    res = float(out.split("residual=")[1].split()[0])
+    assert res <= 1e-8, out
+    x = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
+    ref = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, net, device=cuda), b, x, tol=1e-8, max_iter=2000, fallback=True)
+    assert ref["converged"] and not ref["fallback"], ref
+    assert abs(its - ref["iterations"]) <= 2, (out, ref)
+    x0 = torch.zeros_like(x)
+    plain = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, coarse="none", device=cuda), b, x0, tol=1e-8, max_iter=2000, fallback=True)
+    assert its * 3 < plain["iterations"] + plain["fallback_iterations"], (its, plain)

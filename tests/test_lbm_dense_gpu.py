@@ -39,7 +39,7 @@ def gpu_cavity(ngb, cuda, n, q, storage, steps, ulb=0.1, re=100.0, box=True, use
 
 def to_numpy_storage(t, storage):
     import torch
-    if storage in (2, 3):
+    if storage in (2, 3, 4):
         return t.view(torch.int16).cpu().numpy().view(np.uint16)
     return t.cpu().numpy()
 
