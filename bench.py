@@ -580,7 +580,7 @@ def jacobi_pcg_run(d, b, n, dev, reps=1):
            "roofline": {"bound": "hbm", "peak": peak, "peak_kind": kind, "unit": "GB/s",
                         "whole_solve_achieved": round(whole, 1), "whole_solve_frac": round(whole / peak, 4),
                         "bytes_per_dof_iteration": 40, **passes},
-           "gpu_launches_per_iteration": 4}
+           "gpu_launches_per_iteration": 2, "launches_per_refresh": 2}
     return out, ws
 
 

@@ -53,10 +53,12 @@ size_t ngb_abi_struct_size(int32_t which);
  * the step seed: for cell index i (x + nx (y + ny z)), population q and seed s,
  *   h  = mix32(lo32(i >> 1) ^ (hi32(i >> 1) * 0x9E3779B1) ^ (s * 0x85EBCA77)),
  *   hq = (h ^ (q * 0x9E3779B9)) * 0xC2B2AE35,
- *   r  = i odd ? (hq >> 6) & 0x1FFF : hq >> 19        (13 bits)
+ *   r  = i odd ? (hq >> 16) & 0x1FFF : hq & 0x1FFF    (13 bits)
  * with mix32(x) = x ^= x >> 16, x *= 0x7FEB352D, x ^= x >> 15,
  * x *= 0x846CA68B, x ^= x >> 16 (Wellons' "lowbias32"); the stored value is
- * fp16_round_toward_zero(bits_f32(2^14 g) + r). ngb_lbm_dense_step uses
+ * 2^14 g with r / 2^13 of its FP16 ulp added to the magnitude, then
+ * truncated (FP16 subnormals included): the GPU's cvt.rs.f16x2.f32 with hq as
+ * the random word of the pair (2i, 2i+1). ngb_lbm_dense_step uses
  * s = dither_seed; the t-th step of ngb_lbm_dense_run uses
  * s = dither_seed + (t mod 32). */
 #define NGB_F16OFF_SCALE 16384.0f

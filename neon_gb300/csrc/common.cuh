@@ -157,9 +157,10 @@ __host__ __device__ inline uint32_t dither_hash(int64_t cell, uint32_t seed)
     return mix32(uint32_t(pr) ^ (uint32_t(pr >> 32) * 0x9E3779B1u) ^ (seed * 0x85EBCA77u));
 }
 __host__ __device__ inline uint32_t dither_word(uint32_t h, int q) { return (h ^ (uint32_t(q) * 0x9E3779B9u)) * 0xC2B2AE35u; }
-// 13 bits for the even (lo) / odd (hi) cell of the pair
-__host__ __device__ inline uint32_t dither_lo(uint32_t hq) { return hq >> 19; }
-__host__ __device__ inline uint32_t dither_hi(uint32_t hq) { return (hq >> 6) & 0x1fffu; }
+// 13 bits for the even (lo) / odd (hi) cell of the pair: bits 0-12 and 16-28,
+// the bits cvt.rs.f16x2.f32 takes for its low and high result from one word
+__host__ __device__ inline uint32_t dither_lo(uint32_t hq) { return hq & 0x1fffu; }
+__host__ __device__ inline uint32_t dither_hi(uint32_t hq) { return (hq >> 16) & 0x1fffu; }
 static_assert(float(1 << StoreScale<__half>::log2) == NGB_F16OFF_SCALE, "FP16 storage scale");
 
 inline size_t storage_bytes(int storage)

@@ -100,16 +100,21 @@ struct PairIO<__nv_bfloat16> {
     __device__ __forceinline__ static void store1(__nv_bfloat16* p, float g, float) { *p = __float2bfloat16_rn(g); }
 };
 
-// FP16 stores with stochastic rounding: r (13 random bits) is added to the
-// FP32 bit pattern, which the round-toward-zero conversion then truncates, so
-// the value rounds up in magnitude with probability = its remainder / ulp.
-__device__ __forceinline__ __half f16_sr(float v, uint32_t r) { return __float2half_rz(__uint_as_float(__float_as_uint(v) + r)); }
-__device__ __forceinline__ uint32_t f16x2_sr(float lo, float hi, uint32_t rlo, uint32_t rhi)
+// FP16 stores with stochastic rounding, by the hardware's stochastic-rounding
+// conversion (cvt.rs): a 13-bit random number r in [0, 8192) is added, in
+// units of 2^-13 of the result's ulp, to the magnitude, which is then
+// truncated, so the value rounds up in magnitude with probability = its
+// remainder / ulp (FP16 subnormal results included). One 32-bit word carries
+// the bits of a pair: bits 0-12 for the low half, 16-28 for the high half.
+__device__ __forceinline__ uint32_t f16x2_sr(float lo, float hi, uint32_t rbits)
 {
     uint32_t w;
-    asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(w) : "f"(__uint_as_float(__float_as_uint(hi) + rhi)),
-        "f"(__uint_as_float(__float_as_uint(lo) + rlo)));
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(w) : "f"(hi), "f"(lo), "r"(rbits));
     return w;
+}
+__device__ __forceinline__ __half f16_sr(float v, uint32_t r)
+{
+    return __ushort_as_half(static_cast<unsigned short>(f16x2_sr(v, 0.f, r) & 0xffffu));
 }
 
 template <>
@@ -494,28 +499,20 @@ template <>
 struct PairBits<f16sr_t> {
     __device__ __forceinline__ static float2 to_g(uint32_t w) { return PairBits<__half>::to_g(w); }
     // the pair's cells are even (lo) and odd (hi): their dither bits come from one word
-    __device__ __forceinline__ static uint32_t from_g_sr(float2 g, uint32_t hq)
-    {
-        return f16x2_sr(g.x, g.y, dither_lo(hq), dither_hi(hq));
-    }
+    __device__ __forceinline__ static uint32_t from_g_sr(float2 g, uint32_t hq) { return f16x2_sr(g.x, g.y, hq); }
 };
 
-template <int Q, typename S>
-__device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
-                                               const DirOffsets& o)
+// One pair of cells (2 tp, 2 tp + 1). EDGE: the warp holds a row end or an
+// idle lane (pairs past the row end read the last pair and store nothing),
+// so the bounce-back of x = 1 / x = nx - 2 and the partial stores are tested
+// per direction; warps without (the rest of the row) take no such test.
+template <int Q, typename S, bool EDGE>
+__device__ __forceinline__ void core_pair_cells(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
+                                                const DirOffsets& o, int64_t cell, int lane, bool live, bool first, bool last)
 {
     using L = Lattice<Q>;
     constexpr unsigned kFull = 0xffffffffu;
-    const int          np = p.nx >> 1;  // pairs per row
-    const int          t = blockIdx.x * kPairBlock + threadIdx.x;
-    const int          lane = threadIdx.x & 31;
-    const bool         live = t < np;
-    const int          tp = live ? t : np - 1;  // idle lanes read the last pair (in the row, results unused)
-    const int          y = 2 + blockIdx.y, z = 2 + blockIdx.z;
-    const int64_t      cell = 2 * int64_t(tp) + int64_t(p.nx) * (y + int64_t(p.ny) * z);
     const char*        P = reinterpret_cast<const char*>(fin + cell);
-    const bool         first = tp == 0, last = tp == np - 1;  // the pairs holding x = 1 and x = nx - 2
-    const unsigned     edge = __ballot_sync(kFull, live && (first || last));
     float2             g[Q];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -536,14 +533,16 @@ __device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __r
             w = __byte_perm(own, right, 0x5432);
         }
         g[q] = PairBits<S>::to_g(w);
-        if (edge && cx != 0) {  // warp-uniform: the warp holds a row end
-            const int oq = L::opp(q);
-            if (cx > 0 && first) g[q].y = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).y + p.wall[0][oq];
-            if (cx < 0 && last) g[q].x = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).x + p.wall[0][oq];
+        if constexpr (EDGE) {
+            if (cx != 0) {
+                const int oq = L::opp(q);
+                if (cx > 0 && first) g[q].y = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).y + p.wall[0][oq];
+                if (cx < 0 && last) g[q].x = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).x + p.wall[0][oq];
+            }
         }
     }
     bgk_shifted<Q, float2, StoreScale<S>::log2>(g, p.omega);
-    if (!live) return;
+    if (EDGE && !live) return;
     char*          D = reinterpret_cast<char*>(fout + cell);
     const uint32_t h = dither_base<S>(cell, p.seed);  // one hash per pair (cell is even)
 #pragma unroll
@@ -553,7 +552,7 @@ __device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __r
             w = PairBits<S>::from_g_sr(g[q], dither_word(h, q));
         else
             w = PairBits<S>::from_g(g[q]);
-        if (!(first || last)) {
+        if (!EDGE || !(first || last)) {
             *reinterpret_cast<unsigned int*>(D + o.own[q]) = w;
         } else if (first) {  // x = 0 is a wall node
             *reinterpret_cast<unsigned short*>(D + o.own[q] + 2) = static_cast<unsigned short>(w >> 16);
@@ -564,8 +563,28 @@ __device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __r
 }
 
 template <int Q, typename S>
-__global__ void __launch_bounds__(kPairBlock) lbm_box_core_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                      DenseParams<float> p, const __grid_constant__ DirOffsets o)
+__device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
+                                               const DirOffsets& o)
+{
+    const int      np = p.nx >> 1;  // pairs per row
+    const int      t = blockIdx.x * kPairBlock + threadIdx.x;
+    const int      lane = threadIdx.x & 31;
+    const bool     live = t < np;
+    const int      tp = live ? t : np - 1;  // idle lanes read the last pair (in the row, results unused)
+    const int      y = 2 + blockIdx.y, z = 2 + blockIdx.z;
+    const int64_t  cell = 2 * int64_t(tp) + int64_t(p.nx) * (y + int64_t(p.ny) * z);
+    const bool     first = tp == 0, last = tp == np - 1;  // the pairs holding x = 1 and x = nx - 2
+    const unsigned edge = __ballot_sync(0xffffffffu, !live || first || last);
+    if (edge)
+        core_pair_cells<Q, S, true>(fin, fout, p, o, cell, lane, live, first, last);
+    else
+        core_pair_cells<Q, S, false>(fin, fout, p, o, cell, lane, true, false, false);
+}
+
+// 64 registers: sixteen 64-thread CTAs (32 warps) per SM
+template <int Q, typename S>
+__global__ void __launch_bounds__(kPairBlock, 16) lbm_box_core_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
+                                                                          DenseParams<float> p, const __grid_constant__ DirOffsets o)
 {
     core_pair_body<Q, S>(fin, fout, p, o);
 }

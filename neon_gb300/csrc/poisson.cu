@@ -591,7 +591,8 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
 // flight while the current one is updated; BOX as in pass A.
 template <typename T, bool BOX>
 __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* __restrict__ xlo, const T* __restrict__ p,
-                                                        T* __restrict__ r, const T* __restrict__ s, double* partials)
+                                                        T* __restrict__ r, const T* __restrict__ s, double* partials,
+                                                        cudaGraphConditionalHandle refresh_if, int use_if)
 {
     if (st->converged) return;
     const int     jac = st->jacobi;
@@ -636,6 +637,8 @@ __global__ void __launch_bounds__(kBX) cg_pass_b_kernel(Dom d, CgState* st, T* _
         const bool want = (st->iter % st->refresh_every == 0) || (sqrt(out[1]) / st->bnorm <= st->tol);
         st->last = st->iter >= st->max_iter ? 1 : 0;
         st->refresh = (want || st->last) ? 1 : 0;
+        // inside the solve graph: the refresh kernels run only when wanted
+        if (use_if) cudaGraphSetConditional(refresh_if, unsigned(st->refresh));
     }
 }
 
@@ -778,28 +781,62 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
     // the two passes: no more CTAs than work items (partials hold `grid` entries)
     const int grid_a = std::min(grid, pass_a_items(d)), grid_b = std::min(grid, pass_b_items(d));
     // Capture `check_every` iterations (rounded up to even: p ping-pongs) once.
+    // Each iteration is pass A, pass B and an IF node holding the two refresh
+    // kernels, whose condition pass B sets: they launch on refresh iterations only.
     const int    per = std::max(2, (prm->check_every + 1) / 2 * 2);
-    cudaStream_t cs;
+    cudaStream_t cs, cs_body;
     NGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    if (cudaStreamCreateWithFlags(&cs_body, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        set_error("cudaStreamCreateWithFlags failed");
+        return NGB_ERR_CUDA;
+    }
     cudaGraph_t graph = nullptr;
-    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        for (int it = 0; it < per; it++) {
+        for (int it = 0; it < per && e == cudaSuccess; it++) {
             T* pa = (it % 2 == 0) ? p0 : p1;
             T* pb = (it % 2 == 0) ? p1 : p0;
+            cudaGraphConditionalHandle h{};
+            e = cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault);
+            if (e != cudaSuccess) break;
             if (d.bd)
                 cg_pass_a_kernel<T, false><<<grid_a, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
             else
                 cg_pass_a_kernel<T, true><<<grid_a, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
             if (d.bd)
-                cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
+                cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials, h, 1);
             else
-                cg_pass_b_kernel<T, true><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials);
-            cg_refresh1_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, x, xlo);
-            cg_refresh2_kernel<T><<<grid, kBX, 0, cs>>>(d, w.st, b, x, r, w.partials);
+                cg_pass_b_kernel<T, true><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials, h, 1);
+            cudaStreamCaptureStatus cst;
+            const cudaGraphNode_t*  deps = nullptr;
+            size_t                  ndeps = 0;
+            e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &deps, nullptr, &ndeps);
+            if (e != cudaSuccess) break;
+            cudaGraphNodeParams np{};
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = h;
+            np.conditional.type = cudaGraphCondTypeIf;
+            np.conditional.size = 1;
+            cudaGraphNode_t node;
+            e = cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np);
+            if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+            if (e == cudaSuccess)
+                e = cudaStreamBeginCaptureToGraph(cs_body, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                cg_refresh1_kernel<T><<<grid, kBX, 0, cs_body>>>(d, w.st, x, xlo);
+                cg_refresh2_kernel<T><<<grid, kBX, 0, cs_body>>>(d, w.st, b, x, r, w.partials);
+                cudaGraph_t body = nullptr;
+                e = cudaStreamEndCapture(cs_body, &body);
+            }
         }
-        e = cudaStreamEndCapture(cs, &graph);
+        cudaGraph_t captured = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &captured);
+        if (e == cudaSuccess) e = e2;
     }
+    cudaStreamDestroy(cs_body);
     cudaStreamDestroy(cs);
     if (e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -891,9 +928,9 @@ int time_passes_t(const ngb_poisson_desc* desc, const T* b, double* x, const Wor
     for (int it = 0; it < reps; it++) {
         T* pb = (it % 2 == 0) ? p1 : p0;
         if (d.bd)
-            cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, s>>>(d, w.st, xlo, pb, r, sv, w.partials);
+            cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, s>>>(d, w.st, xlo, pb, r, sv, w.partials, cudaGraphConditionalHandle{}, 0);
         else
-            cg_pass_b_kernel<T, true><<<grid_b, kBX, 0, s>>>(d, w.st, xlo, pb, r, sv, w.partials);
+            cg_pass_b_kernel<T, true><<<grid_b, kBX, 0, s>>>(d, w.st, xlo, pb, r, sv, w.partials, cudaGraphConditionalHandle{}, 0);
     }
     NGB_CUDA_TRY(cudaEventRecord(ev[2], s));
     NGB_LAUNCH_CHECK("cg_pass_a/b_kernel");

@@ -178,11 +178,14 @@ inline uint16_t f32_to_f16_rz(float f)
 }
 
 // Stochastic rounding of FP16 offset storage (the library's F16SR): the random
-// bits r of cell i, population q, step seed s, added to the FP32 bit pattern
-// of the (scaled) value, then truncated:
+// bits r of cell i, population q, step seed s,
 //   h = mix32(lo32(i >> 1) ^ (hi32(i >> 1) * 0x9E3779B1) ^ (s * 0x85EBCA77))
-//   hq = (h ^ (q * 0x9E3779B9)) * 0xC2B2AE35;  r = i odd ? (hq >> 6) & 0x1FFF : hq >> 19
-// mix32 is Wellons' lowbias32 integer hash.
+//   hq = (h ^ (q * 0x9E3779B9)) * 0xC2B2AE35;  r = i odd ? (hq >> 16) & 0x1FFF : hq & 0x1FFF
+// (mix32 is Wellons' lowbias32 integer hash) are added, in units of 2^-13 of
+// the FP16 result's ulp, to the magnitude of the (scaled) value, which is
+// then truncated: the conversion the GPU's cvt.rs.f16x2.f32 performs with
+// one random word per pair (bits 0-12 for the low result, 16-28 for the high),
+// pinned bit for bit against that instruction's outputs in the tests.
 inline uint32_t dither_mix32(uint32_t x)
 {
     x ^= x >> 16;
@@ -197,13 +200,29 @@ inline uint32_t dither_bits(uint64_t cell, int q, uint32_t seed)
     const uint64_t pr = cell >> 1;
     const uint32_t h = dither_mix32(uint32_t(pr) ^ (uint32_t(pr >> 32) * 0x9E3779B1u) ^ (seed * 0x85EBCA77u));
     const uint32_t hq = (h ^ (uint32_t(q) * 0x9E3779B9u)) * 0xC2B2AE35u;
-    return (cell & 1) ? ((hq >> 6) & 0x1fffu) : (hq >> 19);
+    return (cell & 1) ? ((hq >> 16) & 0x1fffu) : (hq & 0x1fffu);
 }
+// r in [0, 8192). Normal FP16 results: the FP32 significand keeps 13 bits
+// below the FP16 ulp, so adding r to the FP32 bit pattern (a carry may raise
+// the exponent) and truncating is the rule; a sum of 2^16 or more overflows
+// to infinity (no saturation). FP16 subnormal results (|f| < 2^-14, ulp
+// 2^-24): floor((floor(|f| 2^37) + r) / 2^13) ulps.
 inline uint16_t f32_to_f16_sr(float f, uint32_t r)
 {
     uint32_t x;
     std::memcpy(&x, &f, 4);
-    x += r;
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t ax = x & 0x7fffffffu;
+    if (ax < 0x38800000u) {
+        const int      e = int(ax >> 23);  // |f| = m 2^(e - 150) for e >= 1
+        const int      shift = 113 - e;    // floor(|f| 2^37) = m >> shift
+        const uint32_t m = (ax & 0x7fffffu) | 0x800000u;
+        const uint32_t fx = (e == 0 || shift >= 32) ? 0u : (m >> shift);
+        return uint16_t(sign | ((fx + r) >> 13));
+    }
+    if (ax >= 0x7f800000u) return f32_to_f16_rz(f);  // infinity, NaN
+    x += r;                                           // r < 2^13: may carry into the exponent
+    if ((x & 0x7fffffffu) >= 0x47800000u) return uint16_t(sign | 0x7c00u);  // rounded to 2^16 or beyond: overflow
     float g;
     std::memcpy(&g, &x, 4);
     return f32_to_f16_rz(g);
