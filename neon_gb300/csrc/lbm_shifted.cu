@@ -12,6 +12,7 @@ void launch_core(bool pair, dim3 gpair, dim3 gcore, dim3 block, const T* fi, T* 
 {
     if constexpr (Q == 19 && sizeof(T) == 2) {
         if (pair) {
+            gpair.z = (gpair.z + PairWalk<T>::planes - 1) / PairWalk<T>::planes;
             lbm_box_core_pair_kernel<Q, T><<<gpair, kPairBlock, 0, s>>>(fi, fo, ps, o);
             return;
         }

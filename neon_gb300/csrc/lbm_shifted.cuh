@@ -450,15 +450,18 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_box_core_kernel(const S* __res
 // c_x = +1 the pair (2t-1, 2t) is the high half of the left neighbour's word
 // (warp shuffle) and the low half of the own word, for c_x = -1 the pair
 // (2t+1, 2t+2) is the own high half and the right neighbour's low half; the
-// first / last lane of a warp fetches the missing half with a 16-bit load.
+// first / last lane of a warp loads the aligned word beyond the warp's ends.
 // The collision runs on FP32x2 pairs (per lane the scalar sequence, so the
 // stored bits equal the one-cell kernels'). The pairs holding x = 1 and
 // x = nx-2 take the resting-wall bounce-back per half; x = 0 and x = nx-1 are
-// wall nodes and are not written. Requires nx even (rows start on a word).
+// wall nodes and are not written. Warps that hold such a pair or an idle lane
+// take a separate path; the rest of the row runs without any per-direction
+// test. A thread walks ZC planes in z with the next plane's words loaded
+// before the current plane's collision (ZC = 1: one plane, no prefetch).
+// Requires nx even (rows start on a word).
 constexpr int kPairBlock = 64;
 
 __device__ __forceinline__ uint32_t ldg_u32(const char* p) { return __ldg(reinterpret_cast<const unsigned int*>(p)); }
-__device__ __forceinline__ uint32_t ldg_u16(const char* p) { return __ldg(reinterpret_cast<const unsigned short*>(p)); }
 
 template <typename S>
 struct PairBits;
@@ -502,49 +505,80 @@ struct PairBits<f16sr_t> {
     __device__ __forceinline__ static uint32_t from_g_sr(float2 g, uint32_t hq) { return f16x2_sr(g.x, g.y, hq); }
 };
 
-// One pair of cells (2 tp, 2 tp + 1). EDGE: the warp holds a row end or an
-// idle lane (pairs past the row end read the last pair and store nothing),
-// so the bounce-back of x = 1 / x = nx - 2 and the partial stores are tested
-// per direction; warps without (the rest of the row) take no such test.
-template <int Q, typename S, bool EDGE>
-__device__ __forceinline__ void core_pair_cells(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
-                                                const DirOffsets& o, int64_t cell, int lane, bool live, bool first, bool last)
+// Plane walk and register cap of the pair kernel per storage: FP16 with
+// stochastic rounding spends more instructions per pair, so it hides the
+// load latency with the prefetch of the next plane (16 planes per thread,
+// up to 128 registers); the other 16-bit forms run one plane per thread at
+// 64 registers (32 warps per SM). Measured at 384^3, same process.
+template <typename S>
+struct PairWalk {
+    static constexpr int planes = 1, min_ctas = 16;
+};
+template <>
+struct PairWalk<f16sr_t> {
+    static constexpr int planes = 16, min_ctas = 8;
+};
+
+// The 32-bit words one pair pulls along every direction (w), and for the
+// first / last lane of a warp the word beyond the warp's end along each
+// c_x = +1 (xa) / -1 (xb) direction; for the pairs at x = 1 / x = nx - 2 that
+// slot holds the pair's own word of the opposite direction (bounce-back).
+template <int Q>
+__device__ __forceinline__ void pair_fetch(const char* P, const DirOffsets& o, int lane, bool first, bool last, uint32_t (&w)[Q],
+                                           uint32_t (&xa)[5], uint32_t (&xb)[5])
 {
     using L = Lattice<Q>;
-    constexpr unsigned kFull = 0xffffffffu;
-    const char*        P = reinterpret_cast<const char*>(fin + cell);
-    float2             g[Q];
+    int ia = 0, ib = 0;
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         const int   cx = L::cx(q);
         const char* src = P + o.pull[q];  // the pull source of the pair's first cell
-        uint32_t    w;
         if (cx == 0) {
-            w = ldg_u32(src);
-        } else if (cx > 0) {  // sources 2t-1, 2t
-            const uint32_t own = ldg_u32(src + 2);
-            uint32_t       left = __shfl_up_sync(kFull, own, 1);
-            if (lane == 0) left = ldg_u16(src) << 16;
-            w = __byte_perm(left, own, 0x5432);
-        } else {  // sources 2t+1, 2t+2
-            const uint32_t own = ldg_u32(src - 2);
-            uint32_t       right = __shfl_down_sync(kFull, own, 1);
-            if (lane == 31) right = ldg_u16(src + 2);
-            w = __byte_perm(own, right, 0x5432);
-        }
-        g[q] = PairBits<S>::to_g(w);
-        if constexpr (EDGE) {
-            if (cx != 0) {
-                const int oq = L::opp(q);
-                if (cx > 0 && first) g[q].y = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).y + p.wall[0][oq];
-                if (cx < 0 && last) g[q].x = PairBits<S>::to_g(ldg_u32(P + o.own[oq])).x + p.wall[0][oq];
-            }
+            w[q] = ldg_u32(src);
+        } else if (cx > 0) {
+            w[q] = ldg_u32(src + 2);
+            if (lane == 0) xa[ia] = ldg_u32(first ? P + o.own[L::opp(q)] : src - 2);
+            ia++;
+        } else {
+            w[q] = ldg_u32(src - 2);
+            if (last || lane == 31) xb[ib] = ldg_u32(last ? P + o.own[L::opp(q)] : src + 2);
+            ib++;
         }
     }
-    bgk_shifted<Q, float2, StoreScale<S>::log2>(g, p.omega);
-    if (EDGE && !live) return;
-    char*          D = reinterpret_cast<char*>(fout + cell);
-    const uint32_t h = dither_base<S>(cell, p.seed);  // one hash per pair (cell is even)
+}
+
+// Words -> the pair's pulled values as FP32 pairs (shuffles, byte permutes,
+// bounce-back at the row ends).
+template <int Q, typename S, bool EDGE>
+__device__ __forceinline__ void pair_unpack(const uint32_t (&w)[Q], const uint32_t (&xa)[5], const uint32_t (&xb)[5], int lane,
+                                            bool first, bool last, const DenseParams<float>& p, float2 (&g)[Q])
+{
+    using L = Lattice<Q>;
+    int ia = 0, ib = 0;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int cx = L::cx(q);
+        if (cx == 0) {
+            g[q] = PairBits<S>::to_g(w[q]);
+        } else if (cx > 0) {
+            uint32_t left = __shfl_up_sync(0xffffffffu, w[q], 1);
+            if (lane == 0) left = xa[ia];
+            g[q] = PairBits<S>::to_g(__byte_perm(left, w[q], 0x5432));
+            if (EDGE && first) g[q].y = PairBits<S>::to_g(xa[ia]).y + p.wall[0][L::opp(q)];
+            ia++;
+        } else {
+            uint32_t right = __shfl_down_sync(0xffffffffu, w[q], 1);
+            if (lane == 31) right = xb[ib];
+            g[q] = PairBits<S>::to_g(__byte_perm(w[q], right, 0x5432));
+            if (EDGE && last) g[q].x = PairBits<S>::to_g(xb[ib]).x + p.wall[0][L::opp(q)];
+            ib++;
+        }
+    }
+}
+
+template <int Q, typename S, bool EDGE>
+__device__ __forceinline__ void pair_store(char* D, const DirOffsets& o, const float2 (&g)[Q], uint32_t h, bool first, bool last)
+{
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         uint32_t w;
@@ -552,41 +586,55 @@ __device__ __forceinline__ void core_pair_cells(const S* __restrict__ fin, S* __
             w = PairBits<S>::from_g_sr(g[q], dither_word(h, q));
         else
             w = PairBits<S>::from_g(g[q]);
-        if (!EDGE || !(first || last)) {
+        if (!EDGE || !(first || last))
             *reinterpret_cast<unsigned int*>(D + o.own[q]) = w;
-        } else if (first) {  // x = 0 is a wall node
+        else if (first)  // x = 0 is a wall node
             *reinterpret_cast<unsigned short*>(D + o.own[q] + 2) = static_cast<unsigned short>(w >> 16);
-        } else {  // x = nx - 1 is a wall node
+        else  // x = nx - 1 is a wall node
             *reinterpret_cast<unsigned short*>(D + o.own[q]) = static_cast<unsigned short>(w & 0xffffu);
-        }
+    }
+}
+
+// One pair's column of planes z0 .. z1-1.
+template <int Q, typename S, bool EDGE>
+__device__ __forceinline__ void pair_column(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
+                                            const DirOffsets& o, int64_t cell, int z0, int z1, int lane, bool live, bool first,
+                                            bool last)
+{
+    const int64_t zs = int64_t(p.nx) * p.ny * int64_t(sizeof(S));  // bytes per plane
+    const char*   P = reinterpret_cast<const char*>(fin + cell);
+    char*         D = reinterpret_cast<char*>(fout + cell);
+    uint32_t      w[Q], xa[5] = {0, 0, 0, 0, 0}, xb[5] = {0, 0, 0, 0, 0};
+    pair_fetch<Q>(P, o, lane, first, last, w, xa, xb);
+    for (int z = z0; z < z1; z++) {
+        float2 g[Q];
+        pair_unpack<Q, S, EDGE>(w, xa, xb, lane, first, last, p, g);
+        if (z + 1 < z1) pair_fetch<Q>(P + zs, o, lane, first, last, w, xa, xb);
+        bgk_shifted<Q, float2, StoreScale<S>::log2>(g, p.omega);
+        if (!EDGE || live) pair_store<Q, S, EDGE>(D, o, g, dither_base<S>(cell, p.seed), first, last);
+        P += zs;
+        D += zs;
+        cell += int64_t(p.nx) * p.ny;
     }
 }
 
 template <int Q, typename S>
-__device__ __forceinline__ void core_pair_body(const S* __restrict__ fin, S* __restrict__ fout, const DenseParams<float>& p,
-                                               const DirOffsets& o)
+__global__ void __launch_bounds__(kPairBlock, PairWalk<S>::min_ctas)
+    lbm_box_core_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout, DenseParams<float> p, const __grid_constant__ DirOffsets o)
 {
+    constexpr int  ZC = PairWalk<S>::planes;
     const int      np = p.nx >> 1;  // pairs per row
-    const int      t = blockIdx.x * kPairBlock + threadIdx.x;
-    const int      lane = threadIdx.x & 31;
+    const int      t = blockIdx.x * kPairBlock + threadIdx.x, lane = threadIdx.x & 31;
     const bool     live = t < np;
     const int      tp = live ? t : np - 1;  // idle lanes read the last pair (in the row, results unused)
-    const int      y = 2 + blockIdx.y, z = 2 + blockIdx.z;
-    const int64_t  cell = 2 * int64_t(tp) + int64_t(p.nx) * (y + int64_t(p.ny) * z);
+    const int      y = 2 + blockIdx.y, z0 = 2 + blockIdx.z * ZC, z1 = min(z0 + ZC, p.nz - 2);
     const bool     first = tp == 0, last = tp == np - 1;  // the pairs holding x = 1 and x = nx - 2
     const unsigned edge = __ballot_sync(0xffffffffu, !live || first || last);
+    const int64_t  cell = 2 * int64_t(tp) + int64_t(p.nx) * (y + int64_t(p.ny) * z0);
     if (edge)
-        core_pair_cells<Q, S, true>(fin, fout, p, o, cell, lane, live, first, last);
+        pair_column<Q, S, true>(fin, fout, p, o, cell, z0, z1, lane, live, first, last);
     else
-        core_pair_cells<Q, S, false>(fin, fout, p, o, cell, lane, true, false, false);
-}
-
-// 64 registers: sixteen 64-thread CTAs (32 warps) per SM
-template <int Q, typename S>
-__global__ void __launch_bounds__(kPairBlock, 16) lbm_box_core_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout,
-                                                                          DenseParams<float> p, const __grid_constant__ DirOffsets o)
-{
-    core_pair_body<Q, S>(fin, fout, p, o);
+        pair_column<Q, S, false>(fin, fout, p, o, cell, z0, z1, lane, true, false, false);
 }
 
 // The rest of the analytic cavity's bulk cells: the planes z = 1 and
