@@ -376,7 +376,7 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         host_in = torch.empty(q * V, dtype=tdt, pin_memory=True)
-        host_out = torch.empty_like(host_in)
+        host_out = torch.empty(q * V, dtype=tdt, pin_memory=True)  # empty_like would drop the pinning
         host_in.copy_(fa.cpu())
         ngb.lbm_dense_run_host(desc, host_in, host_out, fa, fb, 2, stream=stream)  # warm the path
         barrier()
