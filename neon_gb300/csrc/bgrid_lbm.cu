@@ -267,34 +267,6 @@ __device__ __forceinline__ __half        hi_of(__half2 w) { return __high2half(w
 __device__ __forceinline__ __nv_bfloat16 lo_of(__nv_bfloat162 w) { return __low2bfloat16(w); }
 __device__ __forceinline__ __nv_bfloat16 hi_of(__nv_bfloat162 w) { return __high2bfloat16(w); }
 
-// One bulk voxel of a pair whose partner is not bulk: scalar pull from the
-// cubes (lane 0 or 1 of the pair), collision, store.
-template <typename S>
-__device__ __forceinline__ void staged_voxel(const S* sp, const S* __restrict__ fin, S* __restrict__ fout, const uint32_t* flags,
-                                             const uint32_t* sconn, const BParams<float>& p, uint32_t b, int v, int i, int j,
-                                             int k, uint32_t m)
-{
-    constexpr int  Q = 19;
-    using L = Lattice<Q>;
-    const uint32_t lid = m ? bgrid_lidbits<Q>(flags, p.mask, sconn, i, j, k, m) : 0u;
-    const S*       own = fin + size_t(b) * Q * kBlockVoxels + v;
-    float          g[Q];
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-        const int o = L::opp(q);
-        if (is_rest<Q>(q))
-            g[q] = PairIO<S>::to_g1(own[q * kBlockVoxels], float(L::w(q)));
-        else if ((m >> q) & 1u)  // w(opp q) == w(q)
-            g[q] = PairIO<S>::to_g1(sp[cube_own<Q>(o)], float(L::w(q))) + ((lid >> q) & 1u ? p.wall[1][o] : p.wall[0][o]);
-        else
-            g[q] = PairIO<S>::to_g1(sp[cube_src<Q>(q)], float(L::w(q)));
-    }
-    bgk_shifted<Q, float, StoreScale<S>::log2>(g, p.omega);
-    S* out = fout + size_t(b) * Q * kBlockVoxels + v;
-#pragma unroll
-    for (int q = 0; q < Q; q++) PairIO<S>::store1(out + q * kBlockVoxels, g[q], float(L::w(q)));
-}
-
 template <typename S>
 constexpr size_t staged_smem()
 {
@@ -373,8 +345,14 @@ __global__ void __launch_bounds__(kStagedThreads, 4)
             if (bgrid_pull_src<Q>(sconn, i + 1, j, k, q, nv) == NGB_BGRID_NO_BLOCK) m1 |= 1u << q;
         }
     }
+    // A voxel that is not bulk is computed beside its partner (from the cube
+    // values at its pull positions, which may be unset) but not stored: a
+    // pair with one bulk voxel takes the same path as a full pair.
+    const bool b0 = c0 == NGB_CELL_BULK, b1 = c1 == NGB_CELL_BULK;
+    if (!b0) m0 = 0u;
+    if (!b1) m1 = 0u;
     const S* sp = st + pc;
-    if (c0 == NGB_CELL_BULK && c1 == NGB_CELL_BULK) {
+    if (b0 || b1) {
         float2 g[Q];
         if ((m0 | m1) == 0) {
 #pragma unroll
@@ -401,14 +379,19 @@ __global__ void __launch_bounds__(kStagedThreads, 4)
         }
         bgk_shifted<Q, float2, StoreScale<S>::log2>(g, p.omega);
         S* out = fout + size_t(b) * Q * kBlockVoxels + v;
+        if (b0 && b1) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) PairIO<S>::store(out + q * kBlockVoxels, g[q], float(L::w(q)));
-        return;
+            for (int q = 0; q < Q; q++) PairIO<S>::store(out + q * kBlockVoxels, g[q], float(L::w(q)));
+        } else if (b0) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) PairIO<S>::store1(out + q * kBlockVoxels, g[q].x, float(L::w(q)));
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q; q++) PairIO<S>::store1(out + q * kBlockVoxels + 1, g[q].y, float(L::w(q)));
+        }
     }
     if (c0 == NGB_CELL_OUTLET) bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v, i, j, k);
     if (c1 == NGB_CELL_OUTLET) bgrid_outlet<Q, S>(fin, fout, p.mask, p.conn, b, v + 1, i + 1, j, k);
-    if (c0 == NGB_CELL_BULK) staged_voxel<S>(sp, fin, fout, flags, sconn, p, b, v, i, j, k, m0);
-    if (c1 == NGB_CELL_BULK) staged_voxel<S>(sp + 1, fin, fout, flags, sconn, p, b, v + 1, i + 1, j, k, m1);
 }
 
 template <typename S>

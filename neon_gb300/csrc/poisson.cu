@@ -585,6 +585,133 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
     }
 }
 
+// pass A for the analytic box with float fields and fewer than 2^31 cells:
+// the tiles, planes and arithmetic of cg_pass_a_kernel<float, true> (so the
+// results are the same bits), with 32-bit cell indices advanced by one plane
+// per step (one wide multiply-add per address instead of 64-bit index
+// arithmetic), one uniform validity test per plane, and columns outside the
+// grid parked on cell 0 (read, never used or written); 48 registers.
+__global__ void __launch_bounds__(kBX, 5) cg_pass_a_box_kernel(Dom d, CgState* st, const float* __restrict__ r,
+                                                                  const float* __restrict__ p_old, float* __restrict__ p_new,
+                                                                  float* __restrict__ s, double* partials)
+{
+    if (st->converged) return;
+    const int    jac = st->jacobi;
+    const double beta = st->rz_prev == 0.0 ? 0.0 : st->rz / st->rz_prev;
+    const float  tb = float(beta);
+    const float  invh2 = 1.0f / (float(d.h) * float(d.h));
+    const float  dg6 = invdiag6<float>(d, jac);
+    __shared__ float planes[2][kTYA + 2][kTX + 2];
+    const int    lx = threadIdx.x % kTX, ly0 = threadIdx.x / kTX;
+    int        hx = 0, hy = 0;
+    const bool halo = threadIdx.x < kHalo;
+    if (threadIdx.x < kTX + 2) {
+        hx = threadIdx.x - 1, hy = -1;
+    } else if (threadIdx.x < 2 * (kTX + 2)) {
+        hx = threadIdx.x - (kTX + 2) - 1, hy = kTYA;
+    } else if (halo) {
+        const int k = threadIdx.x - 2 * (kTX + 2);
+        hx = (k & 1) ? kTX : -1, hy = k >> 1;
+    }
+    const int ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTYA - 1) / kTYA;
+    const int items = pass_a_items(d);
+    const int pl = d.nx * d.ny;
+    DotAcc<float> acc;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int  tx = item % ntx, rest = item / ntx, ty = rest % nty, zc = rest / nty;
+        const int  x = tx * kTX + lx, z0 = zc * d.zc, z1 = min(z0 + d.zc, d.nz);
+        const int  ya = ty * kTYA + ly0, yb = ya + 8;
+        const bool ownA = x < d.nx && ya < d.ny, ownB = x < d.nx && yb < d.ny;
+        const bool fA = x == 0 || x == d.nx - 1 || ya == 0 || ya == d.ny - 1;
+        const bool fB = x == 0 || x == d.nx - 1 || yb == 0 || yb == d.ny - 1;
+        const int  gx = tx * kTX + hx, gy = ty * kTYA + hy;
+        const bool hown = halo && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
+        const bool hface = gx == 0 || gy == 0 || gx == d.nx - 1 || gy == d.ny - 1;
+        // columns outside the grid stay on cell 0 (read, never used or written)
+        const int stA = ownA ? pl : 0, stB = ownB ? pl : 0, sth = hown ? pl : 0;
+        int       iA = (ownA ? x + d.nx * ya : 0) + z0 * stA, iB = (ownB ? x + d.nx * yb : 0) + z0 * stB;
+        int       ih = (hown ? gx + d.nx * gy : 0) + z0 * sth;
+        const float dgA = fA ? 1.f : dg6, dgB = fB ? 1.f : dg6, dgh = hface ? 1.f : dg6;
+        // p' = dgv r + tb p (0 outside the grid); zface: dgv = 1
+        auto pnA = [&](bool zin, bool zface, float rv, float pv) -> float {
+            const float v = float((zface ? 1.f : dgA) * rv) + tb * pv;
+            return (ownA && zin) ? v : 0.f;
+        };
+        auto pnB = [&](bool zin, bool zface, float rv, float pv) -> float {
+            const float v = float((zface ? 1.f : dgB) * rv) + tb * pv;
+            return (ownB && zin) ? v : 0.f;
+        };
+        float pprevA = 0.f, pprevB = 0.f, pcA, pcB, r1A = 0.f, p1A = 0.f, r1B = 0.f, p1B = 0.f, hr, hp;
+        if (z0 >= 1) {
+            pprevA = pnA(true, z0 - 1 == 0, r[iA - stA], p_old[iA - stA]);
+            pprevB = pnB(true, z0 - 1 == 0, r[iB - stB], p_old[iB - stB]);
+        }
+        const bool zf0 = z0 == 0 || z0 == d.nz - 1;
+        pcA = pnA(true, zf0, r[iA], p_old[iA]);
+        pcB = pnB(true, zf0, r[iB], p_old[iB]);
+        hr = r[ih], hp = p_old[ih];
+        if (z0 + 1 < d.nz) {
+            r1A = r[iA + stA], p1A = p_old[iA + stA];
+            r1B = r[iB + stB], p1B = p_old[iB + stB];
+        }
+        __syncthreads();
+        for (int z = z0; z < z1; z++) {
+            float r2A = 0.f, p2A = 0.f, r2B = 0.f, p2B = 0.f, hr2 = 0.f, hp2 = 0.f;
+            if (z + 2 < d.nz) {
+                const int ja = iA + 2 * stA, jb = iB + 2 * stB;
+                r2A = r[ja], p2A = p_old[ja], r2B = r[jb], p2B = p_old[jb];
+            }
+            if (z + 1 < d.nz) hr2 = r[ih + sth], hp2 = p_old[ih + sth];
+            const bool  zn = z + 1 == d.nz - 1;
+            const float pnextA = pnA(z + 1 < d.nz, zn, r1A, p1A), pnextB = pnB(z + 1 < d.nz, zn, r1B, p1B);
+            const bool  zf = z == 0 || z == d.nz - 1;
+            const float hvv = float((zf ? 1.f : dgh) * hr) + tb * hp;
+            float (*plane)[kTX + 2] = planes[z & 1];
+            plane[ly0 + 1][lx + 1] = pcA;
+            plane[ly0 + 9][lx + 1] = pcB;
+            if (halo) plane[hy + 1][hx + 1] = hown ? hvv : 0.f;
+            __syncthreads();
+            {
+                float sum = 0.f;
+                sum = sum + plane[ly0 + 1][lx + 2];
+                sum = sum + plane[ly0 + 1][lx];
+                sum = sum + plane[ly0 + 2][lx + 1];
+                sum = sum + plane[ly0][lx + 1];
+                sum = sum + pnextA;
+                sum = sum + pprevA;
+                const float sc = (fA || zf) ? pcA : (-sum + 6.f * pcA) * invh2;
+                if (ownA) {
+                    p_new[iA] = pcA, s[iA] = sc;
+                    acc.add(pcA, sc);
+                }
+            }
+            {
+                float sum = 0.f;
+                sum = sum + plane[ly0 + 9][lx + 2];
+                sum = sum + plane[ly0 + 9][lx];
+                sum = sum + plane[ly0 + 10][lx + 1];
+                sum = sum + plane[ly0 + 8][lx + 1];
+                sum = sum + pnextB;
+                sum = sum + pprevB;
+                const float sc = (fB || zf) ? pcB : (-sum + 6.f * pcB) * invh2;
+                if (ownB) {
+                    p_new[iB] = pcB, s[iB] = sc;
+                    acc.add(pcB, sc);
+                }
+            }
+            iA += stA, iB += stB, ih += sth;
+            pprevA = pcA, pcA = pnextA, pprevB = pcB, pcB = pnextB;
+            r1A = r2A, p1A = p2A, r1B = r2B, p1B = p2B, hr = hr2, hp = hp2;
+        }
+    }
+    double v[1] = {acc.value()};
+    double out[1];
+    if (grid_sum<1>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
+        st->pAp = out[0];
+        st->alpha = st->rz / out[0];
+    }
+}
+
 // pass B: x_lo += alpha p; r -= alpha s; rz' = <r, z>; rr = <r, r>. Work
 // items of 32 x 8 columns and chunks of d.zc planes: each thread
 // walks its column with a running index, the loads of the next plane in
@@ -759,6 +886,23 @@ Workspace layout(const ngb_poisson_desc* d, void* base)
     return w;
 }
 
+// pass A launch: the 32-bit-index box kernel where it applies
+template <typename T>
+void launch_pass_a(const Dom& d, int grid_a, CgState* st, const T* r, const T* pa, T* pb, T* sv, double* partials, cudaStream_t s)
+{
+    if (d.bd) {
+        cg_pass_a_kernel<T, false><<<grid_a, kBX, 0, s>>>(d, st, r, pa, pb, sv, partials);
+        return;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        if (int64_t(d.nx) * d.ny * d.nz < (int64_t(1) << 31)) {
+            cg_pass_a_box_kernel<<<grid_a, kBX, 0, s>>>(d, st, r, pa, pb, sv, partials);
+            return;
+        }
+    }
+    cg_pass_a_kernel<T, true><<<grid_a, kBX, 0, s>>>(d, st, r, pa, pb, sv, partials);
+}
+
 template <typename T>
 int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace& w, const ngb_cg_params* prm,
             ngb_cg_result* res, cudaStream_t s)
@@ -801,10 +945,7 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
             cudaGraphConditionalHandle h{};
             e = cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault);
             if (e != cudaSuccess) break;
-            if (d.bd)
-                cg_pass_a_kernel<T, false><<<grid_a, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
-            else
-                cg_pass_a_kernel<T, true><<<grid_a, kBX, 0, cs>>>(d, w.st, r, pa, pb, sv, w.partials);
+            launch_pass_a<T>(d, grid_a, w.st, r, pa, pb, sv, w.partials, cs);
             if (d.bd)
                 cg_pass_b_kernel<T, false><<<grid_b, kBX, 0, cs>>>(d, w.st, xlo, pb, r, sv, w.partials, h, 1);
             else
@@ -919,10 +1060,7 @@ int time_passes_t(const ngb_poisson_desc* desc, const T* b, double* x, const Wor
     for (int it = 0; it < reps; it++) {
         T* pa = (it % 2 == 0) ? p0 : p1;
         T* pb = (it % 2 == 0) ? p1 : p0;
-        if (d.bd)
-            cg_pass_a_kernel<T, false><<<grid_a, kBX, 0, s>>>(d, w.st, r, pa, pb, sv, w.partials);
-        else
-            cg_pass_a_kernel<T, true><<<grid_a, kBX, 0, s>>>(d, w.st, r, pa, pb, sv, w.partials);
+        launch_pass_a<T>(d, grid_a, w.st, r, pa, pb, sv, w.partials, s);
     }
     NGB_CUDA_TRY(cudaEventRecord(ev[1], s));
     for (int it = 0; it < reps; it++) {
