@@ -468,9 +468,23 @@ int ngb_conv3d_tc_check(void* stream);
  * next ngb_conv3d_tc_check then returns NGB_ERR_TIMEOUT and clears the flag). */
 int ngb_conv3d_tc_wait_selftest(int32_t limit, void* stream);
 
-/* dw[co][t][ci] += sum_v dy[v][co] x[v+t][ci] (BF16 inputs, FP32 dw). */
+/* dw[co][t][ci] += sum_v dy[v][co] x[v+t][ci] (BF16 inputs, FP32 dw). Runs
+ * on the tcgen05 tensor cores where ngb_conv3d_bwd_weight_tc_supported
+ * allows, on the mma.sync kernel elsewhere. */
 int ngb_conv3d_bwd_weight(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy, int32_t lddy,
                           int32_t cout, float* dw, void* stream);
+/* The tcgen05 form alone: an implicit GEMM per group of 128 / cin taps
+ * (M = 128 rows (tap, ci), N = cout, K = voxels, FP32 accumulators in TMEM),
+ * operands gathered and transposed into shared memory by the CTA; CTAs over
+ * voxel ranges add into dw with FP32 atomics. Shapes: nx % 8 == 0, the
+ * voxel count a multiple of 64, cin % 8 == 0 and <= 128, cout in
+ * {16, 32, 64}, ldx / lddy multiples of 8, x and dy 16-byte aligned. */
+int ngb_conv3d_bwd_weight_tc_supported(int32_t nx, int32_t ny, int32_t nz, int32_t ldx, int32_t cin, int32_t lddy, int32_t cout);
+int ngb_conv3d_bwd_weight_tc(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy,
+                             int32_t lddy, int32_t cout, float* dw, void* stream);
+/* The mma.sync form alone (any shape ngb_conv3d_bwd_weight takes: cin % 16 == 0, cout % 8 == 0, cout <= 64). */
+int ngb_conv3d_bwd_weight_mma(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy,
+                              int32_t lddy, int32_t cout, float* dw, void* stream);
 
 /* out = BF16(dy * (y > 0)) (ReLU backward; y NULL: no mask). */
 int ngb_relu_bwd(int64_t V, int32_t C, const float* dy, int32_t lddy, const void* y, int32_t ldy, void* out, int32_t ldo, void* stream);

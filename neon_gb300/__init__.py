@@ -17,7 +17,7 @@ NGB_OK = 0
 STORE_F64, STORE_F32, STORE_F16OFF, STORE_BF16OFF, STORE_F16SR = 0, 1, 2, 3, 4
 STORAGE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "f16off": STORE_F16OFF, "bf16off": STORE_BF16OFF,
                  "f16sr": STORE_F16SR}
-STORAGE_BYTES = {STORE_F64: 8, STORE_F32: 4, STORE_F16OFF: 2, STORE_BF16OFF: 2}
+STORAGE_BYTES = {STORE_F64: 8, STORE_F32: 4, STORE_F16OFF: 2, STORE_BF16OFF: 2, STORE_F16SR: 2}
 CELL_BOUNCEBACK, CELL_MOVINGWALL, CELL_BULK, CELL_UNDEFINED, CELL_OUTLET, CELL_PRESSURE, CELL_VELOCITY = 0, 1, 2, 3, 4, 5, 6
 
 _lib = None
@@ -175,6 +175,11 @@ _EXTRA_SIGNATURES.update({
     "ngb_conv3d_pack": ([_i32, _i32, _vp, _vp, _vp], ctypes.c_int),
     "ngb_conv3d_tc": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp], ctypes.c_int),
     "ngb_conv3d_tc_check": ([_vp], ctypes.c_int),
+    "ngb_conv3d_bwd_weight_tc_supported": ([ctypes.c_int32] * 7, ctypes.c_int),
+    "ngb_conv3d_bwd_weight_tc": ([ctypes.c_int32] * 3 + [_vp, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp],
+                                 ctypes.c_int),
+    "ngb_conv3d_bwd_weight_mma": ([ctypes.c_int32] * 3 + [_vp, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp],
+                                  ctypes.c_int),
     "ngb_conv3d_tc_wait_selftest": ([ctypes.c_int32, _vp], ctypes.c_int),
 })
 

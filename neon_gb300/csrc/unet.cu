@@ -387,6 +387,15 @@ int ngb_conv3d(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, i
 int ngb_conv3d_bwd_weight(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy, int32_t lddy,
                           int32_t cout, float* dw, void* stream)
 {
+    if (ngb_conv3d_bwd_weight_tc_supported(nx, ny, nz, ldx, cin, lddy, cout) && (reinterpret_cast<uintptr_t>(x) & 15u) == 0 &&
+        (reinterpret_cast<uintptr_t>(dy) & 15u) == 0 && dw)
+        return ngb_conv3d_bwd_weight_tc(nx, ny, nz, x, ldx, cin, dy, lddy, cout, dw, stream);
+    return ngb_conv3d_bwd_weight_mma(nx, ny, nz, x, ldx, cin, dy, lddy, cout, dw, stream);
+}
+
+int ngb_conv3d_bwd_weight_mma(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy,
+                              int32_t lddy, int32_t cout, float* dw, void* stream)
+{
     NGB_CHECK_ARG(nx > 0 && ny > 0 && nz > 0, "bad dims");
     NGB_CHECK_ARG(cin > 0 && cin % 16 == 0 && cout > 0 && cout <= 64 && cout % 8 == 0, "bad channel counts");
     NGB_CHECK_ARG(x && dy && dw, "NULL argument");

@@ -410,6 +410,183 @@ int launch_tc(const CUtensorMap& map, const TcParams& p, cudaStream_t s)
     return NGB_OK;
 }
 
+
+// ---------------------------------------------------------------- weight gradient on tcgen05
+// dw[co][t][ci] += sum_v dy[v][co] x[v + off(t)][ci] as an implicit GEMM per
+// group of taps: M = 128 rows (tap, ci) of the group (128 / Cin taps; rows
+// past the group's taps are zero), N = Cout, K = voxels, accumulated in TMEM
+// over the CTA's range of voxels in steps of 64 (four MMAs of K 16).
+// Operands are K-major (voxels contiguous per row), which the activations'
+// channels-last layout is not: four staging warps gather 8 voxels x 8
+// channels per thread with 16-byte loads (zero outside the grid), transpose
+// the 8 x 8 block in registers (byte permutes) and store it as one 128-byte
+// core matrix; a fifth warp owns TMEM and issues the MMAs. The staging warps
+// then read their 32-lane quarter of the accumulator and add it to dw
+// (FP32 atomics: CTAs over voxel ranges meet there).
+constexpr int kWgThreads = 160;
+constexpr int kWgK = 64;       // voxels per stage
+constexpr int kWgStages = 3;
+
+struct WgParams {
+    int                  nx, ny, nz, cin, ldx, lddy;
+    int                  taps, groups, splits;
+    int64_t              chunks;  // V / kWgK
+    uint32_t             a_bytes, stage_bytes, tmem_cols;
+    const __nv_bfloat16* x;
+    const __nv_bfloat16* dy;
+    float*               dw;
+};
+
+// 8 x 8 BF16 transpose: in[i] holds 8 channels of voxel i; returns, for
+// channel e, the 8 voxels' values as one 16-byte row.
+__device__ __forceinline__ uint4 wg_row(const uint4 (&in)[8], int e)
+{
+    const uint32_t sel = (e & 1) ? 0x7632u : 0x5410u;
+    uint32_t       w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint32_t* a = reinterpret_cast<const uint32_t*>(&in[2 * k]);
+        const uint32_t* b = reinterpret_cast<const uint32_t*>(&in[2 * k + 1]);
+        w[k] = __byte_perm(a[e >> 1], b[e >> 1], sel);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint8_t* p, uint4 v)
+{
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(smem_u32(p)), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
+}
+
+template <int N>
+__global__ void __launch_bounds__(kWgThreads, 1) conv3d_wgrad_tc_kernel(WgParams p)
+{
+    constexpr uint32_t kIdesc = idesc_bf16_f32(kTcM, N);
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* stages = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    __shared__ uint64_t     full_bar[kWgStages], empty_bar[kWgStages], done_bar, drain_bar;
+    __shared__ uint32_t     tmem_base_sh;
+    __shared__ volatile int abort_sh;
+
+    const int     warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int     group = blockIdx.x % p.groups, split = blockIdx.x / p.groups;
+    const int     t0 = group * p.taps, nt = min(p.taps, 27 - t0), rows = nt * p.cin;
+    const int64_t c_begin = int64_t(split) * p.chunks / p.splits, c_end = int64_t(split + 1) * p.chunks / p.splits;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kWgStages; s++) {
+            mbar_init(&full_bar[s], 128);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&done_bar, 1);
+        mbar_init(&drain_bar, 1);
+        abort_sh = 0;
+        mbar_init_fence();
+    }
+    if (warp == 4) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                     "r"(p.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+
+    if (warp < 4) {
+        // ------------------------------------------------ staging, then epilogue
+        const int  tid = threadIdx.x, rg = tid >> 3, vg = tid & 7;  // row group (8 rows), voxel group (8 voxels)
+        const int  m0 = rg * 8;
+        const bool arow = m0 < rows;
+        const int  tap = t0 + (arow ? m0 / p.cin : 0), ci0 = arow ? m0 % p.cin : 0;
+        const int  dxi = tap % 3 - 1, dyi = (tap / 3) % 3 - 1, dzi = tap / 9 - 1;
+        const bool brow = rg < N / 8;
+        uint32_t   k = 0;
+        bool       ok = true;
+        for (int64_t c = c_begin; c < c_end; c++, k++) {
+            const uint32_t s = k % kWgStages;
+            if (!(ok = mbar_wait(&empty_bar[s], ((k / kWgStages) & 1u) ^ 1u, &abort_sh))) break;
+            uint8_t*      st = stages + size_t(s) * p.stage_bytes;
+            const int64_t v0 = c * kWgK + vg * 8;  // x of v0 is a multiple of 8 (nx % 8 == 0)
+            const int     x0 = int(v0 % p.nx);
+            const int64_t yz = v0 / p.nx;
+            const int     y = int(yz % p.ny), z = int(yz / p.ny);
+            uint4         in[8];
+            {
+                const int  yy = y + dyi, zz = z + dzi;
+                const bool yzok = arow && yy >= 0 && yy < p.ny && zz >= 0 && zz < p.nz;
+                const int64_t rowv = (int64_t(zz) * p.ny + yy) * p.nx;
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const int xx = x0 + i + dxi;
+                    in[i] = (yzok && xx >= 0 && xx < p.nx)
+                                ? __ldg(reinterpret_cast<const uint4*>(p.x + (rowv + xx) * p.ldx + ci0))
+                                : make_uint4(0u, 0u, 0u, 0u);
+                }
+            }
+            uint8_t* dA = st + (vg >> 1) * 4096 + (vg & 1) * 2048 + rg * 128;
+#pragma unroll
+            for (int e = 0; e < 8; e++) st_shared_v4(dA + e * 16, wg_row(in, e));
+            if (brow) {
+#pragma unroll
+                for (int i = 0; i < 8; i++) in[i] = __ldg(reinterpret_cast<const uint4*>(p.dy + (v0 + i) * p.lddy + rg * 8));
+                uint8_t* dB = st + p.a_bytes + (vg >> 1) * (N * 32) + (vg & 1) * (N * 16) + rg * 128;
+#pragma unroll
+                for (int e = 0; e < 8; e++) st_shared_v4(dB + e * 16, wg_row(in, e));
+            }
+            // generic-proxy stores made visible to the tensor core (async proxy)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&full_bar[s]);
+        }
+        if (ok && c_end > c_begin && mbar_wait(&done_bar, 0, &abort_sh)) {
+            tc_fence_after();
+            float acc[N];
+#pragma unroll
+            for (int c = 0; c < N; c += 16) tmem_ld16(tmem + ((uint32_t(warp) * 32u) << 16) + uint32_t(c), acc + c);
+            const int m = warp * 32 + lane;
+            if (m < rows) {
+                const int t = t0 + m / p.cin, ci = m % p.cin;
+#pragma unroll
+                for (int co = 0; co < N; co++) atomicAdd(p.dw + (int64_t(co) * 27 + t) * p.cin + ci, acc[co]);
+            }
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------ MMA issuer (warp 4)
+        uint32_t k = 0;
+        bool     ok = true;
+        for (int64_t c = c_begin; c < c_end; c++, k++) {
+            const uint32_t s = k % kWgStages;
+            if (!(ok = mbar_wait(&full_bar[s], (k / kWgStages) & 1u, &abort_sh))) break;
+            tc_fence_after();
+            const uint32_t sa = smem_u32(stages + size_t(s) * p.stage_bytes), sb = sa + p.a_bytes;
+#pragma unroll
+            for (int mm = 0; mm < kWgK / 16; mm++)
+                mma_bf16(tmem, smem_desc(sa + uint32_t(mm) * 4096u, 2048, 128), smem_desc(sb + uint32_t(mm) * (N * 32), N * 16, 128),
+                         kIdesc, (k > 0 || mm > 0) ? 1u : 0u);
+            mma_commit(&empty_bar[s]);
+        }
+        if (ok) mma_commit(&done_bar);
+        // every MMA issued here has completed before TMEM is released
+        mma_commit(&drain_bar);
+        mbar_drain(&drain_bar, 0);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 4) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols) : "memory");
+    }
+}
+
+template <int N>
+int launch_wgrad(const WgParams& p, cudaStream_t s)
+{
+    const size_t smem = size_t(kWgStages) * p.stage_bytes + 1024;
+    NGB_CUDA_TRY(cudaFuncSetAttribute(conv3d_wgrad_tc_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    conv3d_wgrad_tc_kernel<N><<<p.groups * p.splits, kWgThreads, smem, s>>>(p);
+    NGB_LAUNCH_CHECK("conv3d_wgrad_tc_kernel");
+    return NGB_OK;
+}
 }  // namespace
 }  // namespace ngb
 
@@ -509,6 +686,47 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
 #undef NGB_TC
     set_error("unsupported cout %d", cout);
     return NGB_ERR_UNSUPPORTED;
+}
+
+int ngb_conv3d_bwd_weight_tc_supported(int32_t nx, int32_t ny, int32_t nz, int32_t ldx, int32_t cin, int32_t lddy, int32_t cout)
+{
+    const int64_t V = int64_t(nx) * ny * nz;
+    return nx > 0 && ny > 0 && nz > 0 && nx % 8 == 0 && V % kWgK == 0 && cin % 8 == 0 && cin <= 128 && ldx % 8 == 0 &&
+           ldx >= cin && lddy % 8 == 0 && lddy >= cout && (cout == 16 || cout == 32 || cout == 64);
+}
+
+int ngb_conv3d_bwd_weight_tc(int32_t nx, int32_t ny, int32_t nz, const void* x, int32_t ldx, int32_t cin, const void* dy,
+                             int32_t lddy, int32_t cout, float* dw, void* stream)
+{
+    NGB_CHECK_ARG(x && dy && dw, "NULL argument");
+    if (!ngb_conv3d_bwd_weight_tc_supported(nx, ny, nz, ldx, cin, lddy, cout)) {
+        set_error("ngb_conv3d_bwd_weight_tc: unsupported shape (nx %d ny %d nz %d ldx %d cin %d lddy %d cout %d)", nx, ny, nz, ldx,
+                  cin, lddy, cout);
+        return NGB_ERR_UNSUPPORTED;
+    }
+    NGB_CHECK_ARG(aligned16(x) && aligned16(dy), "x and dy must be 16-byte aligned");
+    int dev = 0, sms = 0;
+    NGB_CUDA_TRY(cudaGetDevice(&dev));
+    NGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    WgParams p{};
+    p.nx = nx, p.ny = ny, p.nz = nz, p.cin = cin, p.ldx = ldx, p.lddy = lddy;
+    p.taps = std::min(27, kTcM / cin);
+    p.groups = (27 + p.taps - 1) / p.taps;
+    p.chunks = int64_t(nx) * ny * nz / kWgK;
+    // voxel ranges per tap group: about two CTAs per SM in all, at least 8 stages each
+    p.splits = int(std::max<int64_t>(1, std::min<int64_t>(p.chunks / 8, (2 * int64_t(sms) + p.groups - 1) / p.groups)));
+    p.a_bytes = 4u * 4096u;
+    p.stage_bytes = (p.a_bytes + 4u * uint32_t(cout) * 32u + 1023u) & ~1023u;
+    p.tmem_cols = cout <= 32 ? 32u : 64u;
+    p.x = static_cast<const __nv_bfloat16*>(x);
+    p.dy = static_cast<const __nv_bfloat16*>(dy);
+    p.dw = dw;
+    cudaStream_t s = as_stream(stream);
+    switch (cout) {
+        case 16: return launch_wgrad<16>(p, s);
+        case 32: return launch_wgrad<32>(p, s);
+        default: return launch_wgrad<64>(p, s);
+    }
 }
 
 int ngb_conv3d_tc_wait_selftest(int32_t limit, void* stream)

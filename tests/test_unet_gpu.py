@@ -287,3 +287,51 @@ def test_bounded_wait_times_out_and_reports(ngb, cuda):
     ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), None, ngb._ptr(Y), cout, cout, 1, 0, 0, None))
     ngb.check(L.ngb_conv3d_tc_check(None))
     assert bool(torch.isfinite(Y).all())
+
+
+@pytest.mark.parametrize("dims,cin,cout", [((8, 8, 8), 16, 16), ((16, 8, 8), 32, 64), ((8, 16, 8), 48, 16), ((8, 8, 16), 64, 64),
+                                           ((16, 8, 8), 96, 32), ((24, 8, 8), 16, 32)])
+def test_conv_backward_weight_tensor_cores_match_oracle(ngb, cuda, dims, cin, cout):
+    """The tcgen05 weight gradient (tap groups of 128 / cin rows, K = voxels,
+    operands transposed into shared memory) against the float64 oracle on
+    shapes it takes, every tap group (partial last groups, padded rows for
+    cin = 48 and 96) and several CTAs per group; BF16 products are exact in
+    FP32, so only the summation order differs: within 1e-5 of the largest
+    entry. The mma.sync form on the same input agrees as well."""
+    import torch
+    nx, ny, nz = dims
+    rng = np.random.default_rng(nx * 7 + cin + cout)
+    x = U.bf16(rng.standard_normal((nz, ny, nx, cin)))
+    dy = U.bf16(rng.standard_normal((nz, ny, nx, cout)))
+    dw_ref = U.conv_bwd_weight(x, dy)
+    X = _bf16_tensor(x.reshape(-1, cin), cuda)
+    D = _bf16_tensor(dy.reshape(-1, cout), cuda)
+    L = ngb.lib()
+    assert L.ngb_conv3d_bwd_weight_tc_supported(nx, ny, nz, cin, cin, cout, cout) == 1
+    dW = torch.zeros(cout, 27, cin, dtype=torch.float32, device=cuda)
+    ngb.check(L.ngb_conv3d_bwd_weight_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dW), None))
+    scale = np.abs(dw_ref).max()
+    assert np.abs(dW.cpu().numpy() - dw_ref).max() <= 1e-5 * scale
+    dM = torch.zeros_like(dW)
+    ngb.check(L.ngb_conv3d_bwd_weight_mma(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dM), None))
+    assert float((dW - dM).abs().max()) <= 1e-5 * scale
+    # accumulation into dw (the training path adds the gradients of a batch)
+    ngb.check(L.ngb_conv3d_bwd_weight(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dW), None))
+    assert np.abs(dW.cpu().numpy() - 2 * dw_ref).max() <= 2e-5 * scale
+
+
+def test_conv_backward_weight_tensor_cores_at_64(ngb, cuda):
+    """Level-0 shape of training at 64^3 (cin 16, cout 16; 262144 voxels,
+    many CTAs per tap group adding into dw): tcgen05 against mma.sync."""
+    import torch
+    n, cin, cout = 64, 16, 16
+    g = torch.Generator(device="cpu").manual_seed(5)
+    X = torch.randn(n ** 3, cin, generator=g).to(torch.bfloat16).to(cuda)
+    D = torch.randn(n ** 3, cout, generator=g).to(torch.bfloat16).to(cuda)
+    L = ngb.lib()
+    dW = torch.zeros(cout, 27, cin, dtype=torch.float32, device=cuda)
+    dM = torch.zeros_like(dW)
+    ngb.check(L.ngb_conv3d_bwd_weight_tc(n, n, n, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dW), None))
+    ngb.check(L.ngb_conv3d_bwd_weight_mma(n, n, n, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dM), None))
+    scale = float(dM.abs().max())
+    assert float((dW - dM).abs().max()) <= 1e-4 * scale
