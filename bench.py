@@ -68,7 +68,7 @@ def parse():
                     help="learned: training grid size = the coarsest level of the V-cycle")
     ap.add_argument("--lr", type=float, default=3e-4, help="learned: Adam learning rate")
     ap.add_argument("--train-pairs", type=int, default=2000, help="learned: solver-generated training pairs")
-    ap.add_argument("--epochs", type=int, default=2, help="learned: training epochs")
+    ap.add_argument("--epochs", type=int, default=3, help="learned: training epochs")
     ap.add_argument("--weights", default="", help="learned: load U-Net weights from this file instead of training")
     ap.add_argument("--save-weights", default="", help="learned: save the trained weights here")
     ap.add_argument("--scale", type=int, default=1, help="sphere case size divisor")
@@ -603,9 +603,8 @@ def learned_fcg_run(args, n, dev, b, ws, pcg_seconds):
         train["weights"] = os.path.basename(args.weights)
     else:
         captures = (2, 5, 10, 20, 40, 80, 120, 160, 200, 250)
-        systems = max(1, args.train_pairs // len(captures))
         t0 = time.perf_counter()
-        pairs = fcg.make_training_set(args.train_n, systems, captures, seed=2024, device=dev)
+        pairs = fcg.make_training_set(args.train_n, captures=captures, seed=2024, device=dev, count=args.train_pairs)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         losses = fcg.train(net, pairs, epochs=args.epochs, lr=args.lr)

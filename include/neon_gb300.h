@@ -475,8 +475,10 @@ int ngb_conv3d_bwd_weight(int32_t nx, int32_t ny, int32_t nz, const void* x, int
                           int32_t cout, float* dw, void* stream);
 /* The tcgen05 form alone: an implicit GEMM per group of 128 / cin taps
  * (M = 128 rows (tap, ci), N = cout, K = voxels, FP32 accumulators in TMEM),
- * operands gathered and transposed into shared memory by the CTA; CTAs over
- * voxel ranges add into dw with FP32 atomics. Shapes: nx % 8 == 0, the
+ * operands gathered and transposed into shared memory by the CTA; the CTAs'
+ * partial sums over voxel ranges go to a scratch array (allocated on first
+ * use per device, grown on demand) and are added to dw in a fixed order, so
+ * repeated calls give the same bits. Shapes: nx % 8 == 0, the
  * voxel count a multiple of 64, cin % 8 == 0 and <= 128, cout in
  * {16, 32, 64}, ldx / lddy multiples of 8, x and dy 16-byte aligned. */
 int ngb_conv3d_bwd_weight_tc_supported(int32_t nx, int32_t ny, int32_t nz, int32_t ldx, int32_t cin, int32_t lddy, int32_t cout);

@@ -422,7 +422,9 @@ int launch_tc(const CUtensorMap& map, const TcParams& p, cudaStream_t s)
 // the 8 x 8 block in registers (byte permutes) and store it as one 128-byte
 // core matrix; a fifth warp owns TMEM and issues the MMAs. The staging warps
 // then read their 32-lane quarter of the accumulator and add it to dw
-// (FP32 atomics: CTAs over voxel ranges meet there).
+// through a per-CTA partial: each CTA writes its range's sums to its own slice
+// of a scratch array, and a second kernel adds the slices to dw in a fixed
+// order, so the result does not depend on which CTA finishes first.
 constexpr int kWgThreads = 160;
 constexpr int kWgK = 64;       // voxels per stage
 constexpr int kWgStages = 3;
@@ -434,7 +436,7 @@ struct WgParams {
     uint32_t             a_bytes, stage_bytes, tmem_cols;
     const __nv_bfloat16* x;
     const __nv_bfloat16* dy;
-    float*               dw;
+    float*               part;  // [splits][cout][27][cin] partial sums
 };
 
 // 8 x 8 BF16 transpose: in[i] holds 8 channels of voxel i; returns, for
@@ -545,8 +547,9 @@ __global__ void __launch_bounds__(kWgThreads, 1) conv3d_wgrad_tc_kernel(WgParams
             const int m = warp * 32 + lane;
             if (m < rows) {
                 const int t = t0 + m / p.cin, ci = m % p.cin;
+                float*    part = p.part + int64_t(split) * N * 27 * p.cin;
 #pragma unroll
-                for (int co = 0; co < N; co++) atomicAdd(p.dw + (int64_t(co) * 27 + t) * p.cin + ci, acc[co]);
+                for (int co = 0; co < N; co++) part[(int64_t(co) * 27 + t) * p.cin + ci] = acc[co];
             }
         }
     } else if (lane == 0) {
@@ -578,13 +581,52 @@ __global__ void __launch_bounds__(kWgThreads, 1) conv3d_wgrad_tc_kernel(WgParams
     }
 }
 
-template <int N>
-int launch_wgrad(const WgParams& p, cudaStream_t s)
+// dw[i] += sum over s of part[s][i], s ascending.
+__global__ void wgrad_reduce_kernel(int64_t n, int splits, const float* __restrict__ part, float* __restrict__ dw)
 {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        float acc = 0.f;
+        for (int sp = 0; sp < splits; sp++) acc += part[int64_t(sp) * n + i];
+        dw[i] += acc;
+    }
+}
+
+// Scratch of the partial sums, per device, grown on demand and kept.
+struct WgScratch {
+    std::mutex m;
+    float*     ptr[64] = {};
+    size_t     bytes[64] = {};
+};
+WgScratch g_wg_scratch;
+
+template <int N>
+int launch_wgrad(WgParams p, float* dw, cudaStream_t s)
+{
+    const int64_t n = int64_t(N) * 27 * p.cin;
+    const size_t  need = size_t(p.splits) * size_t(n) * sizeof(float);
+    int           dev = 0;
+    NGB_CUDA_TRY(cudaGetDevice(&dev));
+    NGB_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d", dev);
+    {
+        std::lock_guard<std::mutex> lock(g_wg_scratch.m);
+        if (g_wg_scratch.bytes[dev] < need) {
+            if (g_wg_scratch.ptr[dev]) {
+                NGB_CUDA_TRY(cudaStreamSynchronize(s));
+                cudaFree(g_wg_scratch.ptr[dev]);
+                g_wg_scratch.ptr[dev] = nullptr;
+                g_wg_scratch.bytes[dev] = 0;
+            }
+            NGB_CUDA_TRY(cudaMalloc(&g_wg_scratch.ptr[dev], need));
+            g_wg_scratch.bytes[dev] = need;
+        }
+        p.part = g_wg_scratch.ptr[dev];
+    }
     const size_t smem = size_t(kWgStages) * p.stage_bytes + 1024;
     NGB_CUDA_TRY(cudaFuncSetAttribute(conv3d_wgrad_tc_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     conv3d_wgrad_tc_kernel<N><<<p.groups * p.splits, kWgThreads, smem, s>>>(p);
     NGB_LAUNCH_CHECK("conv3d_wgrad_tc_kernel");
+    wgrad_reduce_kernel<<<int(std::min<int64_t>((n + 255) / 256, 1024)), 256, 0, s>>>(n, p.splits, p.part, dw);
+    NGB_LAUNCH_CHECK("wgrad_reduce_kernel");
     return NGB_OK;
 }
 }  // namespace
@@ -720,12 +762,11 @@ int ngb_conv3d_bwd_weight_tc(int32_t nx, int32_t ny, int32_t nz, const void* x, 
     p.tmem_cols = cout <= 32 ? 32u : 64u;
     p.x = static_cast<const __nv_bfloat16*>(x);
     p.dy = static_cast<const __nv_bfloat16*>(dy);
-    p.dw = dw;
     cudaStream_t s = as_stream(stream);
     switch (cout) {
-        case 16: return launch_wgrad<16>(p, s);
-        case 32: return launch_wgrad<32>(p, s);
-        default: return launch_wgrad<64>(p, s);
+        case 16: return launch_wgrad<16>(p, dw, s);
+        case 32: return launch_wgrad<32>(p, dw, s);
+        default: return launch_wgrad<64>(p, dw, s);
     }
 }
 

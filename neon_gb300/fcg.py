@@ -93,27 +93,39 @@ def cg_pairs(n, seed, captures, device, tol=1e-7, max_iter=5000):
 
 
 def make_training_set(n=128, systems=200, captures=(2, 5, 10, 20, 40, 80, 120, 160, 200, 250), seed=2024,
-                      device="cuda"):
+                      device="cuda", count=None):
+    """Solver pairs from `systems` seeded systems, or, with `count`, from as
+    many systems as it takes to reach exactly `count` pairs (a CG run that
+    converges before a capture point yields fewer pairs)."""
     pairs = []
-    for s in range(systems):
+    s = 0
+    while (s < systems) if count is None else (len(pairs) < count):
         pairs += cg_pairs(n, seed + s, set(captures), device)
-    return pairs
+        s += 1
+    return pairs if count is None else pairs[:count]
 
 
 def train(net, pairs, epochs=2, lr=1e-3, log=None, seed=0):
+    """Adam on the relative loss |M(r) - e|^2 / |e|^2 of each pair, one pair
+    per step. The step stays on the device (input scale, loss and gradient
+    scale as device scalars, no tensor-core time-out check inside the epoch):
+    the host reads the losses and checks the convolutions once per epoch."""
     g = torch.Generator().manual_seed(seed)
     losses = []
     for ep in range(epochs):
         order = torch.randperm(len(pairs), generator=g).tolist()
+        step_losses = []
         for i in order:
             r, e = pairs[i]
-            z = net.forward(r)
-            ee = float((e.double() ** 2).sum())
+            z = net.forward(r, sync=False)
+            ee = (e.double() ** 2).sum()
             diff = z - e
-            losses.append(float((diff.double() ** 2).sum()) / ee)
+            step_losses.append((diff.double() ** 2).sum() / ee)
             net.zero_grad()
-            net.backward((2.0 / ee) * diff)
+            net.backward((2.0 / ee).float() * diff, sync=False)
             net.adam_step(lr=lr)
+        net.check()
+        losses += torch.stack(step_losses).tolist()
         if log:
             log("epoch %d: mean relative loss %.4f" % (ep, sum(losses[-len(pairs):]) / len(pairs)))
     return losses

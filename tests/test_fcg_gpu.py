@@ -1,10 +1,10 @@
-"""Flexible CG with the learned U-Net preconditioner on the fine grid (small
-grids): the training data are solver-generated residual/error pairs, FCG
-reaches the 1e-8 true relative residual without the Jacobi-PCG fallback,
-agrees with Jacobi-PCG's solution and needs fewer iterations than
-Jacobi-PCG; the trained network needs fewer iterations than the untrained
-one. The multilevel form, the one the
-benchmark uses, is tested in test_mg_gpu.py."""
+"""Flexible CG with the learned U-Net preconditioner: the training data are
+solver-generated residual/error pairs and training lowers the loss,
+deterministically; with a trained network as the coarsest solve of a
+V-cycle, FCG reaches the 1e-8 true relative residual without the Jacobi-PCG
+fallback, agrees with Jacobi-PCG's solution and needs fewer iterations than
+Jacobi-PCG, than the cycle without the network and than the cycle with the
+untrained network. More of the multilevel form is tested in test_mg_gpu.py."""
 import numpy as np
 import pytest
 
@@ -45,21 +45,25 @@ def test_training_lowers_the_error_loss(trained):
     assert np.mean(losses[-k:]) < 0.7 * np.mean(losses[:k]), (np.mean(losses[:k]), np.mean(losses[-k:]))
 
 
-def test_fcg_converges_and_beats_jacobi_pcg(ngb, orc, cuda, trained):
+def test_fcg_converges_and_beats_jacobi_pcg(ngb, orc, cuda):
+    """A trained network (the committed neon_gb300/weights/unet_poisson_64.ngbw,
+    trained at 64^3 by bench.py --workload learned) as the 64^3 coarsest
+    solve of a V-cycle inside FCG at 128^3: converges to 1e-8 without the
+    Jacobi-PCG fallback, to the Jacobi-PCG solution, in fewer iterations than
+    Jacobi-PCG, than the same cycle without the network and than the cycle
+    with the untrained network."""
+    import os
     import torch
     from neon_gb300 import fcg
     from neon_gb300.learned import UNet
-    from helpers import P
-    net, _ = trained
-    n = 32
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    net = UNet(seed=0, device=cuda)
+    net.load_weights(os.path.join(root, "neon_gb300", "weights", "unet_poisson_64.ngbw"))
+    n = 128
     b = fcg.grf_k2(n, 999, cuda)
     x = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
-    # at 32^3 the fine-grid form converges without the Jacobi-PCG fallback
-    # (it stalls on larger grids, where the network's BF16 output noise,
-    # amplified by A, grows with n^2; the V-cycle form serves those)
-    res = fcg.fcg_solve(net, b, x, tol=1e-8, max_iter=400, fallback=True)
+    res = fcg.fcg_solve_vcycle(fcg.VCycle(n, 1, net, device=cuda), b, x, tol=1e-8, max_iter=400, fallback=True)
     assert res["converged"] and not res["fallback"], res
-    # Jacobi-PCG on the same system
     d = ngb.poisson_desc(n, n, n, "f32", 1.0)
     ws = ngb.cg_workspace(d, cuda)
     x2 = torch.zeros_like(x)
@@ -67,8 +71,29 @@ def test_fcg_converges_and_beats_jacobi_pcg(ngb, orc, cuda, trained):
     assert pcg["converged"]
     assert float((x - x2).norm() / x2.norm()) < 1e-6
     assert res["iterations"] < pcg["iterations"], (res["iterations"], pcg["iterations"])
-    # the untrained network is worse than the trained one
     x3 = torch.zeros_like(x)
-    raw = fcg.fcg_solve(UNet(seed=0, device=cuda), b, x3, tol=1e-8, max_iter=400, fallback=True)
+    plain = fcg.fcg_solve_vcycle(fcg.VCycle(n, 1, coarse="none", device=cuda), b, x3, tol=1e-8, max_iter=400, fallback=True)
+    assert plain["converged"], plain
+    assert res["iterations"] < plain["iterations"] + plain["fallback_iterations"], (res, plain)
+    x4 = torch.zeros_like(x)
+    raw = fcg.fcg_solve_vcycle(fcg.VCycle(n, 1, UNet(seed=0, device=cuda), device=cuda), b, x4, tol=1e-8, max_iter=400,
+                               fallback=True)
     assert raw["converged"], raw
     assert res["iterations"] < raw["iterations"] + raw["fallback_iterations"], (res, raw)
+
+
+def test_training_is_deterministic(ngb, cuda):
+    """Two trainings from the same seed on the same solver pairs give the
+    same losses bit for bit (every kernel of the step, the tcgen05 weight
+    gradient included, sums in a fixed order)."""
+    from neon_gb300 import fcg
+    from neon_gb300.learned import UNet
+    n = 32
+    pairs = []
+    for s in range(3):
+        pairs += fcg.cg_pairs(n, 300 + s, {2, 8, 32}, cuda)
+    runs = []
+    for _ in range(2):
+        net = UNet(seed=0, device=cuda)
+        runs.append(fcg.train(net, pairs, epochs=1, lr=2e-3))
+    assert runs[0] == runs[1]

@@ -335,3 +335,20 @@ def test_conv_backward_weight_tensor_cores_at_64(ngb, cuda):
     ngb.check(L.ngb_conv3d_bwd_weight_mma(n, n, n, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dM), None))
     scale = float(dM.abs().max())
     assert float((dW - dM).abs().max()) <= 1e-4 * scale
+
+
+def test_conv_backward_weight_tensor_cores_are_deterministic(ngb, cuda):
+    """The CTAs' partial sums meet in a fixed order: repeated calls give the
+    same bits (training runs repeat exactly)."""
+    import torch
+    n, cin, cout = 32, 16, 32
+    g = torch.Generator(device="cpu").manual_seed(11)
+    X = torch.randn(n ** 3, cin, generator=g).to(torch.bfloat16).to(cuda)
+    D = torch.randn(n ** 3, cout, generator=g).to(torch.bfloat16).to(cuda)
+    L = ngb.lib()
+    outs = []
+    for _ in range(3):
+        dW = torch.zeros(cout, 27, cin, dtype=torch.float32, device=cuda)
+        ngb.check(L.ngb_conv3d_bwd_weight_tc(n, n, n, ngb._ptr(X), cin, cin, ngb._ptr(D), cout, cout, ngb._ptr(dW), None))
+        outs.append(dW.cpu().numpy().view(np.uint32))
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
