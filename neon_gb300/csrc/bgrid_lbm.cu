@@ -307,13 +307,14 @@ __global__ void __launch_bounds__(kStagedThreads, 4)
         hd[r] = it < kHalo ? __ldg(&g_halo19.dst[it]) : 0xffffffffu;
         hs[r] = it < kHalo ? __ldg(&g_halo19.src[it]) : 0u;
     }
-    __syncthreads();  // sconn
     // halo values (a missing neighbour block leaves its cells unset: every
-    // voxel pulling from one treats the direction as a wall)
+    // voxel pulling from one treats the direction as a wall); the neighbour
+    // comes from the block's connectivity row directly (the CTA's threads
+    // share it through L1), so no barrier waits for the row in shared memory
     S hv[kPer];
 #pragma unroll
     for (int r = 0; r < kPer; r++) {
-        const uint32_t nb = hd[r] != 0xffffffffu ? sconn[hd[r] >> 16] : NGB_BGRID_NO_BLOCK;
+        const uint32_t nb = hd[r] != 0xffffffffu ? __ldg(p.conn + size_t(b) * 27 + (hd[r] >> 16)) : NGB_BGRID_NO_BLOCK;
         if (nb == NGB_BGRID_NO_BLOCK) hd[r] = 0xffffffffu;
         hv[r] = nb != NGB_BGRID_NO_BLOCK ? __ldg(fin + size_t(nb) * Q * kBlockVoxels + hs[r]) : S();
     }
