@@ -29,33 +29,84 @@ __global__ void bgrid_flag_kernel(const uint8_t* __restrict__ active, int nx, in
     if (lane == 0) block_of[cand] = any ? 1 : 0;
 }
 
-// Single-CTA exclusive scan: block_of[c] = rank among active candidates or -1.
-constexpr int kScanThreads = 1024;
-__global__ void __launch_bounds__(kScanThreads) bgrid_scan_kernel(int32_t* block_of, int64_t ncand, uint32_t* n_blocks)
+// Ranks of the active candidates (block_of[c] = rank or -1) by a three-kernel
+// scan: per-tile counts of kScanTile candidates, an exclusive scan of the
+// tile counts, and per-tile ranks from a CTA-wide scan plus the tile's
+// offset. Every kernel is parallel over tiles except the scan of the tile
+// counts (one per 4096 candidates).
+constexpr int kScanThreads = 1024, kScanPer = 4, kScanTile = kScanThreads * kScanPer;
+
+// Inclusive CTA-wide scan of one value per thread (warp shuffles, then the
+// warp totals); returns the thread's inclusive prefix and the CTA total.
+__device__ __forceinline__ uint32_t cta_scan(uint32_t v, uint32_t& total)
 {
-    __shared__ uint32_t part[kScanThreads];
-    const int64_t       per = (ncand + kScanThreads - 1) / kScanThreads;
-    const int64_t       b0 = threadIdx.x * per, b1 = min(ncand, b0 + per);
-    uint32_t            local = 0;
-    for (int64_t c = b0; c < b1; c++) local += block_of[c] ? 1u : 0u;
-    part[threadIdx.x] = local;
+    __shared__ uint32_t warp_sum[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    if (lane == 31) warp_sum[warp] = v;
     __syncthreads();
-    // Hillis-Steele inclusive scan over the 1024 partial counts
-    for (int off = 1; off < kScanThreads; off <<= 1) {
-        const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint32_t run = part[threadIdx.x] - local;
-    for (int64_t c = b0; c < b1; c++) {
-        if (block_of[c]) {
-            block_of[c] = int32_t(run++);
-        } else {
-            block_of[c] = -1;
+    if (warp == 0) {
+        uint32_t w = warp_sum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
         }
+        warp_sum[lane] = w;
     }
-    if (threadIdx.x == kScanThreads - 1) *n_blocks = part[kScanThreads - 1];
+    __syncthreads();
+    total = warp_sum[kScanThreads / 32 - 1];
+    const uint32_t r = v + (warp > 0 ? warp_sum[warp - 1] : 0u);
+    __syncthreads();  // warp_sum is reused by the next call
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) bgrid_tile_count_kernel(const int32_t* __restrict__ block_of, int64_t ncand,
+                                                                       uint32_t* part)
+{
+    const int64_t c0 = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanPer;
+    uint32_t      n = 0;
+#pragma unroll
+    for (int e = 0; e < kScanPer; e++) n += (c0 + e < ncand && block_of[c0 + e]) ? 1u : 0u;
+    uint32_t total;
+    cta_scan(n, total);
+    if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+// One CTA: part[i] <- sum of part[0 .. i-1]; *n_blocks = sum of all.
+__global__ void __launch_bounds__(kScanThreads) bgrid_part_scan_kernel(uint32_t* part, int64_t nparts, uint32_t* n_blocks)
+{
+    uint32_t carry = 0;
+    for (int64_t base = 0; base < nparts; base += kScanThreads) {
+        const int64_t i = base + threadIdx.x;
+        const uint32_t v = i < nparts ? part[i] : 0u;
+        uint32_t       total;
+        const uint32_t incl = cta_scan(v, total);
+        if (i < nparts) part[i] = carry + incl - v;
+        carry += total;
+    }
+    if (threadIdx.x == 0) *n_blocks = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) bgrid_tile_rank_kernel(int32_t* block_of, int64_t ncand, const uint32_t* part)
+{
+    const int64_t c0 = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanPer;
+    int32_t       f[kScanPer];
+    uint32_t      n = 0;
+#pragma unroll
+    for (int e = 0; e < kScanPer; e++) {
+        f[e] = c0 + e < ncand ? block_of[c0 + e] : 0;
+        n += f[e] ? 1u : 0u;
+    }
+    uint32_t       total;
+    uint32_t       run = part[blockIdx.x] + cta_scan(n, total) - n;
+#pragma unroll
+    for (int e = 0; e < kScanPer; e++)
+        if (c0 + e < ncand) block_of[c0 + e] = f[e] ? int32_t(run++) : -1;
 }
 
 __global__ void bgrid_fill_kernel(const uint8_t* __restrict__ active, int nx, int ny, int nz, int bnx, int bny, int bnz,
@@ -195,8 +246,18 @@ int ngb_bgrid_count(int32_t nx, int32_t ny, int32_t nz, const uint8_t* active, i
     const int64_t blocks = (ncand * 32 + threads - 1) / threads;
     bgrid_flag_kernel<<<dim3(unsigned(blocks)), threads, 0, s>>>(active, nx, ny, nz, bnx, bny, ncand, block_of);
     NGB_LAUNCH_CHECK("bgrid_flag_kernel");
-    bgrid_scan_kernel<<<1, kScanThreads, 0, s>>>(block_of, ncand, n_blocks);
-    NGB_LAUNCH_CHECK("bgrid_scan_kernel");
+    const int64_t nparts = (ncand + kScanTile - 1) / kScanTile;
+    uint32_t*     part = nullptr;  // per-tile counts, stream-ordered scratch
+    NGB_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&part), size_t(nparts) * sizeof(uint32_t), s));
+    bgrid_tile_count_kernel<<<unsigned(nparts), kScanThreads, 0, s>>>(block_of, ncand, part);
+    bgrid_part_scan_kernel<<<1, kScanThreads, 0, s>>>(part, nparts, n_blocks);
+    bgrid_tile_rank_kernel<<<unsigned(nparts), kScanThreads, 0, s>>>(block_of, ncand, part);
+    const cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(part, s);
+    if (e != cudaSuccess) {
+        set_error("bGrid block scan failed: %s", cudaGetErrorString(e));
+        return NGB_ERR_CUDA;
+    }
     return NGB_OK;
 }
 

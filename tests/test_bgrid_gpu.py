@@ -219,3 +219,29 @@ def test_bgrid_drag_matches_numpy(ngb, orc, cuda):
     got = force.cpu().numpy()
     assert np.allclose(got, F, rtol=1e-12, atol=1e-15), (got, F)
     assert got[0] > 0  # the flow pushes the sphere downstream
+
+
+@pytest.mark.parametrize("dims,density", [((512, 512, 512), 0.3), ((1000, 904, 200), 0.55), ((8, 8, 8), 1.0)])
+def test_block_ranks_many_candidates(ngb, cuda, dims, density):
+    """Block ranks over many candidate blocks (262 144 at 512^3: 64 scan tiles;
+    a ragged last tile at 1000 x 904 x 200): the active candidates get ranks
+    0 .. n-1 in candidate order, the others -1, against numpy."""
+    import torch
+    nx, ny, nz = dims
+    bnx, bny, bnz = (nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8
+    rng = np.random.default_rng(nx + nz)
+    on = rng.random(bnx * bny * bnz) < density
+    # one active voxel at a random position inside each active block
+    act = torch.zeros(nx * ny * nz, dtype=torch.uint8, device=cuda)
+    c = np.nonzero(on)[0]
+    bx, by, bz = c % bnx, (c // bnx) % bny, c // (bnx * bny)
+    x = np.minimum(bx * 8 + rng.integers(0, 8, c.size), nx - 1)
+    y = np.minimum(by * 8 + rng.integers(0, 8, c.size), ny - 1)
+    z = np.minimum(bz * 8 + rng.integers(0, 8, c.size), nz - 1)
+    act[torch.from_numpy(x + nx * (y + ny * z)).to(cuda)] = 1
+    block_of = torch.empty(bnx * bny * bnz, dtype=torch.int32, device=cuda)
+    nb = torch.zeros(1, dtype=torch.int32, device=cuda)
+    ngb.check(ngb.lib().ngb_bgrid_count(nx, ny, nz, ngb._ptr(act), ngb._ptr(block_of), ngb._ptr(nb), None))
+    ref = np.where(on, np.cumsum(on) - 1, -1).astype(np.int32)
+    assert int(nb.item()) == int(on.sum())
+    assert np.array_equal(block_of.cpu().numpy(), ref)
