@@ -284,7 +284,9 @@ __global__ void __launch_bounds__(kLbmBlockX) lbm_dense_f64_kernel(const S* __re
 // Whether the FP32-compute launcher runs the analytic cavity as the core + shell kernel pair.
 inline bool lbm_dense_split(int Q, int storage, const DenseParams<float>& p)
 {
-    return p.box && p.nx >= 4 && p.ny >= 6 && p.nz >= 6 && (Q == 19 || storage == NGB_STORE_F32);
+    // D3Q27 with 16-bit storage splits where its core runs as the x-pair kernel (even rows and planes)
+    return p.box && p.nx >= 4 && p.ny >= 6 && p.nz >= 6 &&
+           (Q == 19 || storage == NGB_STORE_F32 || (p.nx % 2 == 0 && p.stride % 2 == 0));
 }
 
 // Host-side launchers (lbm_dense.cu / lbm_dense_f64.cu).

@@ -10,9 +10,9 @@ template <int Q, typename T>
 void launch_core(bool pair, dim3 gpair, dim3 gcore, dim3 block, const T* fi, T* fo, const DenseParams<float>& ps,
                  const DirOffsets& o, cudaStream_t s)
 {
-    if constexpr (Q == 19 && sizeof(T) == 2) {
+    if constexpr (sizeof(T) == 2) {
         if (pair) {
-            gpair.z = (gpair.z + PairWalk<T>::planes - 1) / PairWalk<T>::planes;
+            gpair.z = (gpair.z + PairWalk<T, Q>::planes - 1) / PairWalk<T, Q>::planes;
             lbm_box_core_pair_kernel<Q, T><<<gpair, kPairBlock, 0, s>>>(fi, fo, ps, o);
             return;
         }
@@ -41,10 +41,10 @@ int launch_lbm_dense_f32(int Q, int storage, const void* fin, void* fout, const 
         for (int c = 0; c < 2; c++)
             for (int q = 0; q < 27; q++) ps.wall[c][q] = p.wall[c][q] * NGB_F16OFF_SCALE;
     // Analytic cavity of at least 4 x 6 x 6 cells: core + shell kernels; otherwise one kernel over every
-    // cell. D3Q27 with 16-bit storage keeps the one-kernel form (measured faster: 39.4 vs 36.3 GLUPS at 384^3).
+    // cell (D3Q27 with 16-bit storage and odd rows: the one-cell core measured slower than the one-kernel form).
     const bool split = lbm_dense_split(Q, storage, p);
-    // 16-bit D3Q19 with even rows and planes: the x-pair core kernel (32-bit accesses)
-    const bool pair = split && Q == 19 && storage != NGB_STORE_F32 && p.nx % 2 == 0 && p.stride % 2 == 0;
+    // 16-bit storage with even rows and planes: the x-pair core kernel (32-bit accesses)
+    const bool pair = split && storage != NGB_STORE_F32 && p.nx % 2 == 0 && p.stride % 2 == 0;
     const dim3 gpair((p.nx / 2 + kPairBlock - 1) / kPairBlock, p.ny - 4, p.nz - 4);
     const dim3 gcore((p.nx - 1 + kLbmBlockX - 1) / kLbmBlockX, p.ny - 4, p.nz - 4);
     const dim3 gshell((p.nx - 1 + kLbmBlockX - 1) / kLbmBlockX, 2 * (p.ny - 2) + 2 * (p.nz - 4));

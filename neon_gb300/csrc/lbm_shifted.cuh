@@ -510,14 +510,28 @@ struct PairBits<f16sr_t> {
 // load latency with the prefetch of the next plane (16 planes per thread,
 // up to 128 registers); the other 16-bit forms run one plane per thread at
 // 64 registers (32 warps per SM). Measured at 384^3, same process.
-template <typename S>
+template <typename S, int Q = 19>
 struct PairWalk {
     static constexpr int planes = 1, min_ctas = 16;
 };
 template <>
-struct PairWalk<f16sr_t> {
+struct PairWalk<f16sr_t, 19> {
     static constexpr int planes = 16, min_ctas = 8;
 };
+// D3Q27: 27 pulled values per cell pair, one plane per thread, up to 128 registers
+template <typename S>
+struct PairWalk<S, 27> {
+    static constexpr int planes = 1, min_ctas = 8;
+};
+
+// Directions with c_x = +1 (and as many with -1) of a lattice.
+template <int Q>
+__host__ __device__ constexpr int x_plus_count()
+{
+    int n = 0;
+    for (int q = 0; q < Q; q++) n += Lattice<Q>::cx(q) > 0 ? 1 : 0;
+    return n;
+}
 
 // The 32-bit words one pair pulls along every direction (w), and for the
 // first / last lane of a warp the word beyond the warp's end along each
@@ -525,7 +539,7 @@ struct PairWalk<f16sr_t> {
 // slot holds the pair's own word of the opposite direction (bounce-back).
 template <int Q>
 __device__ __forceinline__ void pair_fetch(const char* P, const DirOffsets& o, int lane, bool first, bool last, uint32_t (&w)[Q],
-                                           uint32_t (&xa)[5], uint32_t (&xb)[5])
+                                           uint32_t (&xa)[x_plus_count<Q>()], uint32_t (&xb)[x_plus_count<Q>()])
 {
     using L = Lattice<Q>;
     int ia = 0, ib = 0;
@@ -550,8 +564,9 @@ __device__ __forceinline__ void pair_fetch(const char* P, const DirOffsets& o, i
 // Words -> the pair's pulled values as FP32 pairs (shuffles, byte permutes,
 // bounce-back at the row ends).
 template <int Q, typename S, bool EDGE>
-__device__ __forceinline__ void pair_unpack(const uint32_t (&w)[Q], const uint32_t (&xa)[5], const uint32_t (&xb)[5], int lane,
-                                            bool first, bool last, const DenseParams<float>& p, float2 (&g)[Q])
+__device__ __forceinline__ void pair_unpack(const uint32_t (&w)[Q], const uint32_t (&xa)[x_plus_count<Q>()],
+                                            const uint32_t (&xb)[x_plus_count<Q>()], int lane, bool first, bool last,
+                                            const DenseParams<float>& p, float2 (&g)[Q])
 {
     using L = Lattice<Q>;
     int ia = 0, ib = 0;
@@ -604,7 +619,10 @@ __device__ __forceinline__ void pair_column(const S* __restrict__ fin, S* __rest
     const int64_t zs = int64_t(p.nx) * p.ny * int64_t(sizeof(S));  // bytes per plane
     const char*   P = reinterpret_cast<const char*>(fin + cell);
     char*         D = reinterpret_cast<char*>(fout + cell);
-    uint32_t      w[Q], xa[5] = {0, 0, 0, 0, 0}, xb[5] = {0, 0, 0, 0, 0};
+    constexpr int kX = x_plus_count<Q>();
+    uint32_t      w[Q], xa[kX], xb[kX];
+#pragma unroll
+    for (int e = 0; e < kX; e++) xa[e] = 0u, xb[e] = 0u;
     pair_fetch<Q>(P, o, lane, first, last, w, xa, xb);
     for (int z = z0; z < z1; z++) {
         float2 g[Q];
@@ -619,10 +637,10 @@ __device__ __forceinline__ void pair_column(const S* __restrict__ fin, S* __rest
 }
 
 template <int Q, typename S>
-__global__ void __launch_bounds__(kPairBlock, PairWalk<S>::min_ctas)
+__global__ void __launch_bounds__(kPairBlock, PairWalk<S, Q>::min_ctas)
     lbm_box_core_pair_kernel(const S* __restrict__ fin, S* __restrict__ fout, DenseParams<float> p, const __grid_constant__ DirOffsets o)
 {
-    constexpr int  ZC = PairWalk<S>::planes;
+    constexpr int  ZC = PairWalk<S, Q>::planes;
     const int      np = p.nx >> 1;  // pairs per row
     const int      t = blockIdx.x * kPairBlock + threadIdx.x, lane = threadIdx.x & 31;
     const bool     live = t < np;
