@@ -42,6 +42,7 @@ struct Dom {
     double        invd[7];  // h^2 / n for n valid neighbours (host-computed: no division on the device)
     float         invf[7];  // the same, rounded to float (no FP64 conversion on the device)
     int32_t       zc;       // planes per CG work item (make_dom: enough items to fill the GPU)
+    int32_t       zc_box;   // the same for the 32 x 32 tiles of the box pass A
 };
 
 // Dot-product accumulator of one thread. For FP32 operands the exact product
@@ -89,6 +90,9 @@ Dom make_dom(const ngb_poisson_desc* d)
     const int64_t cols = int64_t((d->nx + 31) / 32) * ((d->ny + 15) / 16);
     g.zc = 64;
     while (g.zc > 8 && cols * ((d->nz + g.zc - 1) / g.zc) < int64_t(sm_count()) * 4) g.zc /= 2;
+    const int64_t cols_box = int64_t((d->nx + 31) / 32) * ((d->ny + 31) / 32);
+    g.zc_box = 64;
+    while (g.zc_box > 8 && cols_box * ((d->nz + g.zc_box - 1) / g.zc_box) < int64_t(sm_count()) * 4) g.zc_box /= 2;
     return g;
 }
 
@@ -586,122 +590,130 @@ __global__ void __launch_bounds__(kBX) cg_pass_a_kernel(Dom d, CgState* st, cons
 }
 
 // pass A for the analytic box with float fields and fewer than 2^31 cells:
-// the tiles, planes and arithmetic of cg_pass_a_kernel<float, true> (so the
-// results are the same bits), with 32-bit cell indices advanced by one plane
-// per step (one wide multiply-add per address instead of 64-bit index
-// arithmetic), one uniform validity test per plane, and columns outside the
-// grid parked on cell 0 (read, never used or written); 48 registers.
-__global__ void __launch_bounds__(kBX, 5) cg_pass_a_box_kernel(Dom d, CgState* st, const float* __restrict__ r,
-                                                                  const float* __restrict__ p_old, float* __restrict__ p_new,
-                                                                  float* __restrict__ s, double* partials)
+// the planes and arithmetic of cg_pass_a_kernel<float, true> (so the outputs
+// are the same bits) on taller tiles, 32 x 32 columns per CTA with four cells
+// per thread (rows ly0 + 8c), so one barrier per plane serves four cells and
+// the halo is 13 % of a tile instead of 20 %; 32-bit cell indices stepped one
+// plane at a time, one uniform validity test per plane, columns outside the
+// grid parked on cell 0 (read, never used or written); 64 registers, four
+// CTAs per SM.
+constexpr int kBoxR = 4, kBoxTY = 8 * kBoxR, kBoxHalo = 2 * (kTX + 2) + 2 * kBoxTY;
+static_assert(kBoxHalo <= kBX, "box halo");
+
+__host__ __device__ inline int pass_a_box_items(const Dom& d)
 {
+    return ((d.nx + kTX - 1) / kTX) * ((d.ny + kBoxTY - 1) / kBoxTY) * ((d.nz + d.zc_box - 1) / d.zc_box);
+}
+
+__global__ void __launch_bounds__(kBX, 4) cg_pass_a_box_kernel(Dom d, CgState* st, const float* __restrict__ r,
+                                                               const float* __restrict__ p_old, float* __restrict__ p_new,
+                                                               float* __restrict__ s, double* partials)
+{
+    constexpr int R = kBoxR, TY = kBoxTY;
     if (st->converged) return;
     const int    jac = st->jacobi;
     const double beta = st->rz_prev == 0.0 ? 0.0 : st->rz / st->rz_prev;
     const float  tb = float(beta);
     const float  invh2 = 1.0f / (float(d.h) * float(d.h));
     const float  dg6 = invdiag6<float>(d, jac);
-    __shared__ float planes[2][kTYA + 2][kTX + 2];
+    __shared__ float planes[2][TY + 2][kTX + 2];
     const int    lx = threadIdx.x % kTX, ly0 = threadIdx.x / kTX;
     int        hx = 0, hy = 0;
-    const bool halo = threadIdx.x < kHalo;
+    const bool halo = threadIdx.x < kBoxHalo;
     if (threadIdx.x < kTX + 2) {
         hx = threadIdx.x - 1, hy = -1;
     } else if (threadIdx.x < 2 * (kTX + 2)) {
-        hx = threadIdx.x - (kTX + 2) - 1, hy = kTYA;
+        hx = threadIdx.x - (kTX + 2) - 1, hy = TY;
     } else if (halo) {
         const int k = threadIdx.x - 2 * (kTX + 2);
         hx = (k & 1) ? kTX : -1, hy = k >> 1;
     }
-    const int ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + kTYA - 1) / kTYA;
-    const int items = pass_a_items(d);
-    const int pl = d.nx * d.ny;
+    const int     ntx = (d.nx + kTX - 1) / kTX, nty = (d.ny + TY - 1) / TY;
+    const int     items = pass_a_box_items(d);
+    const int     pl = d.nx * d.ny;
     DotAcc<float> acc;
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
-        const int  tx = item % ntx, rest = item / ntx, ty = rest % nty, zc = rest / nty;
-        const int  x = tx * kTX + lx, z0 = zc * d.zc, z1 = min(z0 + d.zc, d.nz);
-        const int  ya = ty * kTYA + ly0, yb = ya + 8;
-        const bool ownA = x < d.nx && ya < d.ny, ownB = x < d.nx && yb < d.ny;
-        const bool fA = x == 0 || x == d.nx - 1 || ya == 0 || ya == d.ny - 1;
-        const bool fB = x == 0 || x == d.nx - 1 || yb == 0 || yb == d.ny - 1;
-        const int  gx = tx * kTX + hx, gy = ty * kTYA + hy;
-        const bool hown = halo && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
-        const bool hface = gx == 0 || gy == 0 || gx == d.nx - 1 || gy == d.ny - 1;
-        // columns outside the grid stay on cell 0 (read, never used or written)
-        const int stA = ownA ? pl : 0, stB = ownB ? pl : 0, sth = hown ? pl : 0;
-        int       iA = (ownA ? x + d.nx * ya : 0) + z0 * stA, iB = (ownB ? x + d.nx * yb : 0) + z0 * stB;
-        int       ih = (hown ? gx + d.nx * gy : 0) + z0 * sth;
-        const float dgA = fA ? 1.f : dg6, dgB = fB ? 1.f : dg6, dgh = hface ? 1.f : dg6;
-        // p' = dgv r + tb p (0 outside the grid); zface: dgv = 1
-        auto pnA = [&](bool zin, bool zface, float rv, float pv) -> float {
-            const float v = float((zface ? 1.f : dgA) * rv) + tb * pv;
-            return (ownA && zin) ? v : 0.f;
-        };
-        auto pnB = [&](bool zin, bool zface, float rv, float pv) -> float {
-            const float v = float((zface ? 1.f : dgB) * rv) + tb * pv;
-            return (ownB && zin) ? v : 0.f;
-        };
-        float pprevA = 0.f, pprevB = 0.f, pcA, pcB, r1A = 0.f, p1A = 0.f, r1B = 0.f, p1B = 0.f, hr, hp;
-        if (z0 >= 1) {
-            pprevA = pnA(true, z0 - 1 == 0, r[iA - stA], p_old[iA - stA]);
-            pprevB = pnB(true, z0 - 1 == 0, r[iB - stB], p_old[iB - stB]);
+        const int tx = item % ntx, rest = item / ntx, ty = rest % nty, zi = rest / nty;
+        const int x = tx * kTX + lx, z0 = zi * d.zc_box, z1 = min(z0 + d.zc_box, d.nz);
+        bool      own[R], fc[R];
+        int       stc[R], ix[R];
+        float     dg[R];
+#pragma unroll
+        for (int c = 0; c < R; c++) {
+            const int y = ty * TY + ly0 + 8 * c;
+            own[c] = x < d.nx && y < d.ny;
+            fc[c] = x == 0 || x == d.nx - 1 || y == 0 || y == d.ny - 1;
+            stc[c] = own[c] ? pl : 0;
+            ix[c] = (own[c] ? x + d.nx * y : 0) + z0 * stc[c];
+            dg[c] = fc[c] ? 1.f : dg6;
         }
-        const bool zf0 = z0 == 0 || z0 == d.nz - 1;
-        pcA = pnA(true, zf0, r[iA], p_old[iA]);
-        pcB = pnB(true, zf0, r[iB], p_old[iB]);
-        hr = r[ih], hp = p_old[ih];
-        if (z0 + 1 < d.nz) {
-            r1A = r[iA + stA], p1A = p_old[iA + stA];
-            r1B = r[iB + stB], p1B = p_old[iB + stB];
+        const int   gx = tx * kTX + hx, gy = ty * TY + hy;
+        const bool  hown = halo && gx >= 0 && gy >= 0 && gx < d.nx && gy < d.ny;
+        const bool  hface = gx == 0 || gy == 0 || gx == d.nx - 1 || gy == d.ny - 1;
+        const int   sth = hown ? pl : 0;
+        int         ih = (hown ? gx + d.nx * gy : 0) + z0 * sth;
+        const float dgh = hface ? 1.f : dg6;
+        // p' = dgv r + tb p (dgv = 1 on the faces), 0 outside the grid
+        float pprev[R], pc[R], r1[R], p1[R];
+#pragma unroll
+        for (int c = 0; c < R; c++) {
+            pprev[c] = 0.f, r1[c] = 0.f, p1[c] = 0.f;
+            if (z0 >= 1) {
+                const float v = float(((z0 - 1 == 0) ? 1.f : dg[c]) * r[ix[c] - stc[c]]) + tb * p_old[ix[c] - stc[c]];
+                pprev[c] = own[c] ? v : 0.f;
+            }
+            const float v = float(((z0 == 0 || z0 == d.nz - 1) ? 1.f : dg[c]) * r[ix[c]]) + tb * p_old[ix[c]];
+            pc[c] = own[c] ? v : 0.f;
+            if (z0 + 1 < d.nz) r1[c] = r[ix[c] + stc[c]], p1[c] = p_old[ix[c] + stc[c]];
         }
+        float hr = r[ih], hp = p_old[ih];
+        // the previous item's last plane may share a buffer with this item's first
         __syncthreads();
         for (int z = z0; z < z1; z++) {
-            float r2A = 0.f, p2A = 0.f, r2B = 0.f, p2B = 0.f, hr2 = 0.f, hp2 = 0.f;
-            if (z + 2 < d.nz) {
-                const int ja = iA + 2 * stA, jb = iB + 2 * stB;
-                r2A = r[ja], p2A = p_old[ja], r2B = r[jb], p2B = p_old[jb];
+            // one plane of lookahead: these loads are used in the next iteration
+            float r2[R], p2[R], hr2 = 0.f, hp2 = 0.f;
+#pragma unroll
+            for (int c = 0; c < R; c++) {
+                r2[c] = 0.f, p2[c] = 0.f;
+                if (z + 2 < d.nz) r2[c] = r[ix[c] + 2 * stc[c]], p2[c] = p_old[ix[c] + 2 * stc[c]];
             }
             if (z + 1 < d.nz) hr2 = r[ih + sth], hp2 = p_old[ih + sth];
-            const bool  zn = z + 1 == d.nz - 1;
-            const float pnextA = pnA(z + 1 < d.nz, zn, r1A, p1A), pnextB = pnB(z + 1 < d.nz, zn, r1B, p1B);
+            const bool zn = z + 1 == d.nz - 1, zin = z + 1 < d.nz;
+            float      pnext[R];
+#pragma unroll
+            for (int c = 0; c < R; c++) {
+                const float v = float((zn ? 1.f : dg[c]) * r1[c]) + tb * p1[c];
+                pnext[c] = (own[c] && zin) ? v : 0.f;
+            }
             const bool  zf = z == 0 || z == d.nz - 1;
             const float hvv = float((zf ? 1.f : dgh) * hr) + tb * hp;
+            // buffer z & 1 was last read in iteration z - 2, before the barrier of iteration z - 1
             float (*plane)[kTX + 2] = planes[z & 1];
-            plane[ly0 + 1][lx + 1] = pcA;
-            plane[ly0 + 9][lx + 1] = pcB;
+#pragma unroll
+            for (int c = 0; c < R; c++) plane[ly0 + 8 * c + 1][lx + 1] = pc[c];
             if (halo) plane[hy + 1][hx + 1] = hown ? hvv : 0.f;
             __syncthreads();
-            {
+#pragma unroll
+            for (int c = 0; c < R; c++) {
+                const int ly = ly0 + 8 * c;
+                // neighbours in the oracle's order +x, -x, +y, -y, +z, -z
                 float sum = 0.f;
-                sum = sum + plane[ly0 + 1][lx + 2];
-                sum = sum + plane[ly0 + 1][lx];
-                sum = sum + plane[ly0 + 2][lx + 1];
-                sum = sum + plane[ly0][lx + 1];
-                sum = sum + pnextA;
-                sum = sum + pprevA;
-                const float sc = (fA || zf) ? pcA : (-sum + 6.f * pcA) * invh2;
-                if (ownA) {
-                    p_new[iA] = pcA, s[iA] = sc;
-                    acc.add(pcA, sc);
+                sum = sum + plane[ly + 1][lx + 2];
+                sum = sum + plane[ly + 1][lx];
+                sum = sum + plane[ly + 2][lx + 1];
+                sum = sum + plane[ly][lx + 1];
+                sum = sum + pnext[c];
+                sum = sum + pprev[c];
+                const float sc = (fc[c] || zf) ? pc[c] : (-sum + 6.f * pc[c]) * invh2;  // Fixed face rows: s = p'
+                if (own[c]) {
+                    p_new[ix[c]] = pc[c], s[ix[c]] = sc;
+                    acc.add(pc[c], sc);
                 }
+                ix[c] += stc[c];
+                pprev[c] = pc[c], pc[c] = pnext[c], r1[c] = r2[c], p1[c] = p2[c];
             }
-            {
-                float sum = 0.f;
-                sum = sum + plane[ly0 + 9][lx + 2];
-                sum = sum + plane[ly0 + 9][lx];
-                sum = sum + plane[ly0 + 10][lx + 1];
-                sum = sum + plane[ly0 + 8][lx + 1];
-                sum = sum + pnextB;
-                sum = sum + pprevB;
-                const float sc = (fB || zf) ? pcB : (-sum + 6.f * pcB) * invh2;
-                if (ownB) {
-                    p_new[iB] = pcB, s[iB] = sc;
-                    acc.add(pcB, sc);
-                }
-            }
-            iA += stA, iB += stB, ih += sth;
-            pprevA = pcA, pcA = pnextA, pprevB = pcB, pcB = pnextB;
-            r1A = r2A, p1A = p2A, r1B = r2B, p1B = p2B, hr = hr2, hp = hp2;
+            ih += sth;
+            hr = hr2, hp = hp2;
         }
     }
     double v[1] = {acc.value()};
@@ -896,7 +908,9 @@ void launch_pass_a(const Dom& d, int grid_a, CgState* st, const T* r, const T* p
     }
     if constexpr (std::is_same<T, float>::value) {
         if (int64_t(d.nx) * d.ny * d.nz < (int64_t(1) << 31)) {
-            cg_pass_a_box_kernel<<<grid_a, kBX, 0, s>>>(d, st, r, pa, pb, sv, partials);
+            // four CTAs per SM, no more than the partials hold (grid_a, the other kernels' grid cap)
+            const int g = std::min(std::min(grid_a, 4 * sm_count()), pass_a_box_items(d));
+            cg_pass_a_box_kernel<<<g, kBX, 0, s>>>(d, st, r, pa, pb, sv, partials);
             return;
         }
     }
