@@ -52,11 +52,13 @@ def test_product_package_does_not_import_oracle():
 
 def test_kernels_per_step_query(ngb):
     """Launch accounting without a GPU: the analytic cavity runs as two kernels
-    (core + wall shell) except for FP64 and 16-bit D3Q27; flag-array grids as one."""
+    (core + wall shell) except for FP64 and for 16-bit storage on an odd x
+    extent (the core kernel takes x-pairs there); flag-array grids as one."""
     d = ngb.lbm_dense_desc(64, 64, 64, 19, "f32", 1.0, box_cavity=True)
     assert ngb.lbm_dense_kernels_per_step(d) == 2
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 19, "f16off", 1.0, box_cavity=True)) == 2
-    assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 27, "f16off", 1.0, box_cavity=True)) == 1
+    assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 27, "f16off", 1.0, box_cavity=True)) == 2
+    assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(63, 64, 64, 27, "f16off", 1.0, box_cavity=True)) == 1
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 19, "f64", 1.0, box_cavity=True)) == 1
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 64, 64, 19, "f32", 1.0, box_cavity=False)) == 1
     assert ngb.lbm_dense_kernels_per_step(ngb.lbm_dense_desc(64, 5, 64, 19, "f32", 1.0, box_cavity=True)) == 1
