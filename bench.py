@@ -659,6 +659,8 @@ def learned_fcg_run(args, n, dev, b, ws, pcg_seconds):
         res = fcg.fcg_solve(net, b, x2, tol=1e-8, max_iter=2000, fallback=True, ws=ws)
     nn_ = n >> levels
     rc = b[:nn_ ** 3].clone()
+    net.forward(rc)  # warm-up: a network loaded from a file has not run yet
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(3):

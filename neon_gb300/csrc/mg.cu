@@ -17,8 +17,10 @@
 //       u2 = 2 c r - c^2 A r with c = omega h^2 / 6;
 //   residual: res = r - A u on Free nodes, 0 on faces.
 //
-// The stencil passes walk columns in z (mg_column_kernel); restriction takes
+// The stencil passes walk 32 x 32 column tiles in z (mg_tile_kernel); restriction takes
 // one thread per coarse node, prolongation one per fine x-pair.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace ngb {
@@ -36,78 +38,150 @@ __device__ __forceinline__ bool interior(const Box& b, int x, int y, int z)
     return x > 0 && y > 0 && z > 0 && x < b.nx - 1 && y < b.ny - 1 && z < b.nz - 1;
 }
 
-// Stencil passes as column walks: a CTA of 32 x 8 threads owns 32 x 8
-// columns and walks kZChunk planes in z; the column's stencil values at
-// z-1 .. z+4 and r at z .. z+3 stay in registers (a prefetch ring three
-// planes deep), the x neighbours come from the adjacent lanes (shuffles; the
-// two tile-edge lanes load theirs), the y neighbours from the rows the
-// CTA's other warps loaded planes earlier (L1).
+// Stencil passes on 32 x 32 column tiles: a CTA of 256 threads owns one
+// tile (four cells per thread, rows ly0 + 8k) and walks a chunk of planes in
+// z. Each plane of v goes through a double-buffered shared tile with a
+// one-cell halo (one barrier per plane), the x and y neighbours come from
+// there, the z neighbours and r from registers loaded one plane ahead.
+// Offsets are 32-bit, relative to the chunk's first plane.
 //   MODE 0: out = v + c (r - A v)        (one Jacobi sweep on u = v)
 //   MODE 1: out = 2 c v - c^2 A v        (two sweeps from zero, v = r)
 //   MODE 2: out = r - A v                (residual)
 //   MODE 3: out = v                      (residual with u = 0, v = r)
 //   MODE 4: out = A v
 // Every mode writes 0 on the face nodes.
-constexpr int kZX = 32, kZY = 8, kZChunk = 32;
+constexpr int kTileR = 4, kTileX = 32, kTileY = 8 * kTileR, kTileHalo = 2 * (kTileX + 2) + 2 * kTileY, kTileThreads = 256;
+static_assert(kTileHalo <= kTileThreads, "one halo cell per thread at most");
+constexpr int kMaxChunk = 32;
+
+// planes per CTA: 32, halved (to 8 at least) until there are four CTAs per SM
+int tile_chunk(const Box& b)
+{
+    static int            sms = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    });
+    const int64_t tiles = int64_t((b.nx + kTileX - 1) / kTileX) * ((b.ny + kTileY - 1) / kTileY);
+    int           zc = kMaxChunk;
+    while (zc > 8 && tiles * ((b.nz + zc - 1) / zc) < int64_t(4) * sms) zc /= 2;
+    return zc;
+}
+
+// the modes that read r keep 64 registers (four CTAs per SM), the others run at three
+template <int MODE>
+constexpr int tile_min_ctas()
+{
+    return (MODE == 0 || MODE == 2) ? 4 : 3;
+}
 
 template <int MODE>
-__global__ void __launch_bounds__(kZX * kZY) mg_column_kernel(Box b, const float* __restrict__ v, const float* __restrict__ r,
-                                                             float* __restrict__ out, float c)
+__global__ void __launch_bounds__(kTileThreads, tile_min_ctas<MODE>())
+    mg_tile_kernel(Box b, const float* __restrict__ v, const float* __restrict__ r, float* __restrict__ out, float c, int zc)
 {
-    const int     lane = threadIdx.x;
-    const int     x = blockIdx.x * kZX + lane, y = blockIdx.y * kZY + threadIdx.y;
-    const int     z0 = blockIdx.z * kZChunk, z1 = min(z0 + kZChunk, b.nz);
-    const bool    col = x < b.nx && y < b.ny;
-    const bool    inner_col = col && x > 0 && y > 0 && x < b.nx - 1 && y < b.ny - 1;
-    const int64_t sy = b.nx, sz = int64_t(b.nx) * b.ny;
-    const int64_t i0 = col ? x + sy * y : 0;
-    auto          at = [&](int zz) { return (col && zz >= 0 && zz < b.nz) ? __ldg(v + i0 + sz * zz) : 0.f; };
-    constexpr bool kR = MODE == 0 || MODE == 2;
-    auto          rat = [&](int zz) { return (kR && col && zz < b.nz) ? __ldg(r + i0 + sz * zz) : 0.f; };
-    // the column's stencil values z-1 .. z+4 and r at z .. z+2 in registers: three planes of
-    // loads stay in flight while a plane is computed (a load used in its own trip exposed the
-    // whole DRAM latency once per plane)
-    // (planes beyond the chunk's last stencil source z1 are not loaded)
-    auto  atc = [&](int zz) { return zz <= z1 ? at(zz) : 0.f; };
-    auto  ratc = [&](int zz) { return zz < z1 ? rat(zz) : 0.f; };
-    float vm = at(z0 - 1), vc = at(z0), v1 = atc(z0 + 1), v2 = atc(z0 + 2), v3 = atc(z0 + 3);
-    float r0 = ratc(z0), r1 = ratc(z0 + 1), r2 = ratc(z0 + 2);
+    constexpr int    R = kTileR, TY = kTileY;
+    constexpr bool   kR = MODE == 0 || MODE == 2;
+    __shared__ float planes[2][TY + 2][kTileX + 2];
+    const int        lx = threadIdx.x % kTileX, ly0 = threadIdx.x / kTileX;
+    // this thread's halo cell (threads < kTileHalo): the rows above and below, then the two side columns
+    int        hx = 0, hy = 0;
+    const bool halo = threadIdx.x < kTileHalo;
+    if (threadIdx.x < kTileX + 2) {
+        hx = threadIdx.x - 1, hy = -1;
+    } else if (threadIdx.x < 2 * (kTileX + 2)) {
+        hx = threadIdx.x - (kTileX + 2) - 1, hy = TY;
+    } else if (halo) {
+        const int k = threadIdx.x - 2 * (kTileX + 2);
+        hx = (k & 1) ? kTileX : -1, hy = k >> 1;
+    }
+    const int     pl = b.nx * b.ny;
+    const int     x = blockIdx.x * kTileX + lx, z0 = blockIdx.z * zc, z1 = min(z0 + zc, b.nz);
+    const int64_t base = int64_t(z0) * pl;  // offsets below are relative to plane z0
+    v += base;
+    out += base;
+    if (kR) r += base;
+    bool own[R], in[R];
+    int  stc[R], ix[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        const int y = blockIdx.y * TY + ly0 + 8 * k;
+        own[k] = x < b.nx && y < b.ny;
+        in[k] = own[k] && x > 0 && y > 0 && x < b.nx - 1 && y < b.ny - 1;
+        stc[k] = own[k] ? pl : 0;  // cells outside the grid stay parked on offset 0 (read, never used or written)
+        ix[k] = own[k] ? x + b.nx * y : 0;
+    }
+    const int  gx = blockIdx.x * kTileX + hx, gy = blockIdx.y * TY + hy;
+    const bool hown = halo && gx >= 0 && gy >= 0 && gx < b.nx && gy < b.ny;
+    const int  sth = hown ? pl : 0;
+    int        ih = hown ? gx + b.nx * gy : 0;
+    float      vm[R], vc[R], v1[R], r0[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        vm[k] = (own[k] && z0 >= 1) ? v[ix[k] - stc[k]] : 0.f;
+        vc[k] = own[k] ? v[ix[k]] : 0.f;
+        v1[k] = (own[k] && z0 + 1 < b.nz) ? v[ix[k] + stc[k]] : 0.f;
+        r0[k] = (kR && own[k]) ? r[ix[k]] : 0.f;
+    }
+    float hv = hown ? v[ih] : 0.f;
     for (int z = z0; z < z1; z++) {
-        const float   v4 = atc(z + 4);
-        const float   r3 = ratc(z + 3);
-        const float   vp = v1;
-        float         left = __shfl_up_sync(0xffffffffu, vc, 1), right = __shfl_down_sync(0xffffffffu, vc, 1);
-        const int64_t i = i0 + sz * z;
-        if (lane == 0) left = (inner_col && z > 0 && z < b.nz - 1) ? __ldg(v + i - 1) : 0.f;
-        if (lane == kZX - 1) right = (inner_col && z > 0 && z < b.nz - 1) ? __ldg(v + i + 1) : 0.f;
-        if (col) {
-            float o = 0.f;
-            if (inner_col && z > 0 && z < b.nz - 1) {
+        // one plane of lookahead: these loads are used in the next iteration
+        float v2[R], r1[R], hv1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            v2[k] = (own[k] && z + 2 < b.nz) ? v[ix[k] + 2 * stc[k]] : 0.f;
+            r1[k] = (kR && own[k] && z + 1 < z1) ? r[ix[k] + stc[k]] : 0.f;
+        }
+        if (hown && z + 1 < z1) hv1 = v[ih + sth];
+        // buffer z & 1 was last read in iteration z - 2, before the barrier of iteration z - 1
+        float (*plane)[kTileX + 2] = planes[z & 1];
+#pragma unroll
+        for (int k = 0; k < R; k++) plane[ly0 + 8 * k + 1][lx + 1] = vc[k];
+        if (halo) plane[hy + 1][hx + 1] = hv;
+        __syncthreads();
+        const bool zin = z > 0 && z < b.nz - 1;
+#pragma unroll
+        for (int k = 0; k < R; k++) {
+            const int ly = ly0 + 8 * k;
+            float     o = 0.f;
+            if (in[k] && zin) {
                 if (MODE == 3) {
-                    o = vc;
+                    o = vc[k];
                 } else {
-                    const float s = ((left + right) + (__ldg(v + i - sy) + __ldg(v + i + sy))) + (vm + vp);
-                    const float av = __fmul_rn(__fmaf_rn(6.f, vc, -s), b.inv_h2);
-                    if (MODE == 0) o = __fmaf_rn(c, r0 - av, vc);
-                    if (MODE == 1) o = __fmaf_rn(-c * c, av, 2.f * c * vc);
-                    if (MODE == 2) o = r0 - av;
+                    const float left = plane[ly + 1][lx], right = plane[ly + 1][lx + 2];
+                    const float dn = plane[ly][lx + 1], up = plane[ly + 2][lx + 1];
+                    const float s = ((left + right) + (dn + up)) + (vm[k] + v1[k]);
+                    const float av = __fmul_rn(__fmaf_rn(6.f, vc[k], -s), b.inv_h2);
+                    if (MODE == 0) o = __fmaf_rn(c, r0[k] - av, vc[k]);
+                    if (MODE == 1) o = __fmaf_rn(-c * c, av, 2.f * c * vc[k]);
+                    if (MODE == 2) o = r0[k] - av;
                     if (MODE == 4) o = av;
                 }
             }
-            out[i] = o;
+            if (own[k]) out[ix[k]] = o;
+            ix[k] += stc[k];
+            vm[k] = vc[k], vc[k] = v1[k], v1[k] = v2[k], r0[k] = r1[k];
         }
-        vm = vc;
-        vc = v1;
-        v1 = v2;
-        v2 = v3;
-        v3 = v4;
-        r0 = r1;
-        r1 = r2;
-        r2 = r3;
+        ih += sth;
+        hv = hv1;
     }
 }
 
-dim3 column_grid(const Box& b) { return dim3((b.nx + kZX - 1) / kZX, (b.ny + kZY - 1) / kZY, (b.nz + kZChunk - 1) / kZChunk); }
+template <int MODE>
+int launch_tile(const Box& b, const float* v, const float* r, float* out, float c, cudaStream_t s)
+{
+    const int zc = tile_chunk(b);
+    // 32-bit offsets within a chunk: (zc + 2) planes of nx * ny cells
+    if (int64_t(b.nx) * b.ny * (zc + 2) >= (int64_t(1) << 31)) {
+        set_error("multilevel kernels take planes of fewer than 2^31 / %d cells (nx * ny = %lld)", zc + 2, (long long)b.nx * b.ny);
+        return NGB_ERR_RANGE;
+    }
+    const dim3 grid((b.nx + kTileX - 1) / kTileX, (b.ny + kTileY - 1) / kTileY, (b.nz + zc - 1) / zc);
+    mg_tile_kernel<MODE><<<grid, kTileThreads, 0, s>>>(b, v, r, out, c, zc);
+    NGB_LAUNCH_CHECK("mg_tile_kernel");
+    return NGB_OK;
+}
 
 __global__ void __launch_bounds__(kMgBX) mg_restrict_kernel(Box f, Box c, const float* __restrict__ res, float* __restrict__ rc,
                                                            float scale)
@@ -198,14 +272,8 @@ int ngb_mg_jacobi(const ngb_poisson_desc* d, const void* u, const void* r, void*
     const Box   b = box_of(d);
     const float c = float(omega * d->h * d->h / 6.0);
     cudaStream_t s = as_stream(stream);
-    const dim3 blk(kZX, kZY);
-    if (u)
-        mg_column_kernel<0><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(u), static_cast<const float*>(r),
-                                                           static_cast<float*>(out), c);
-    else
-        mg_column_kernel<1><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(r), nullptr, static_cast<float*>(out), c);
-    NGB_LAUNCH_CHECK("mg_column_kernel");
-    return NGB_OK;
+    if (u) return launch_tile<0>(b, static_cast<const float*>(u), static_cast<const float*>(r), static_cast<float*>(out), c, s);
+    return launch_tile<1>(b, static_cast<const float*>(r), nullptr, static_cast<float*>(out), c, s);
 }
 
 int ngb_mg_residual(const ngb_poisson_desc* d, const void* u, const void* r, void* out, void* stream)
@@ -215,14 +283,8 @@ int ngb_mg_residual(const ngb_poisson_desc* d, const void* u, const void* r, voi
     NGB_CHECK_ARG(r && out && r != out && u != out, "r/out must be distinct non-NULL device pointers, u must differ from out");
     const Box    b = box_of(d);
     cudaStream_t s = as_stream(stream);
-    const dim3 blk(kZX, kZY);
-    if (u)
-        mg_column_kernel<2><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(u), static_cast<const float*>(r),
-                                                           static_cast<float*>(out), 0.f);
-    else
-        mg_column_kernel<3><<<column_grid(b), blk, 0, s>>>(b, static_cast<const float*>(r), nullptr, static_cast<float*>(out), 0.f);
-    NGB_LAUNCH_CHECK("mg_column_kernel");
-    return NGB_OK;
+    if (u) return launch_tile<2>(b, static_cast<const float*>(u), static_cast<const float*>(r), static_cast<float*>(out), 0.f, s);
+    return launch_tile<3>(b, static_cast<const float*>(r), nullptr, static_cast<float*>(out), 0.f, s);
 }
 
 int ngb_mg_apply(const ngb_poisson_desc* d, const void* u, void* out, void* stream)
@@ -231,10 +293,7 @@ int ngb_mg_apply(const ngb_poisson_desc* d, const void* u, void* out, void* stre
     if (rc) return rc;
     NGB_CHECK_ARG(u && out && u != out, "u/out must be distinct non-NULL device pointers");
     const Box b = box_of(d);
-    mg_column_kernel<4><<<column_grid(b), dim3(kZX, kZY), 0, as_stream(stream)>>>(b, static_cast<const float*>(u), nullptr,
-                                                                                    static_cast<float*>(out), 0.f);
-    NGB_LAUNCH_CHECK("mg_column_kernel");
-    return NGB_OK;
+    return launch_tile<4>(b, static_cast<const float*>(u), nullptr, static_cast<float*>(out), 0.f, as_stream(stream));
 }
 
 int ngb_mg_restrict(const ngb_poisson_desc* fine, const void* res, void* rc_out, double scale, void* stream)

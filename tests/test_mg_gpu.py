@@ -86,6 +86,37 @@ def test_jacobi_and_residual_kernels(ngb, cuda, n, h):
     assert _close(out.reshape(n, n, n), _lap64(u, h) * _interior(n, cuda))
 
 
+@pytest.mark.parametrize("dims", [(37, 70, 19), (96, 33, 45), (130, 66, 9)])
+def test_stencil_passes_on_ragged_tiles(ngb, cuda, dims):
+    """Box sizes that are no multiple of the 32 x 32 column tiles or of the
+    plane chunks, with non-zero values on the faces (the interior nodes next
+    to a face read them): every mode against float64."""
+    import torch
+    nx, ny, nz = dims
+    h = 0.5
+    d = ngb.poisson_desc(nx, ny, nz, "f32", h)
+    g = torch.Generator().manual_seed(nx * ny + nz)
+    u = torch.randn(nz, ny, nx, generator=g, dtype=torch.float64).to(cuda)
+    r = torch.randn(nz, ny, nx, generator=g, dtype=torch.float64).to(cuda)
+    m = torch.zeros_like(u)
+    m[1:-1, 1:-1, 1:-1] = 1
+    out = torch.full((nx * ny * nz,), float("nan"), dtype=torch.float32, device=cuda)
+    w = 6.0 / 7.0
+    c = w * h * h / 6.0
+    uf, rf = u.float().reshape(-1), r.float().reshape(-1)
+    ub, rb = uf.double().reshape(nz, ny, nx), rf.double().reshape(nz, ny, nx)  # the FP32 inputs, exactly
+    ngb.mg_jacobi(d, uf, rf, out, w)
+    assert _close(out.reshape(nz, ny, nx), (ub + c * (rb - _lap64(ub, h))) * m)
+    ngb.mg_jacobi(d, None, rf, out, w)
+    assert _close(out.reshape(nz, ny, nx), (2 * c * rb - c * c * _lap64(rb, h)) * m)
+    ngb.mg_residual(d, uf, rf, out)
+    assert _close(out.reshape(nz, ny, nx), (rb - _lap64(ub, h)) * m)
+    ngb.mg_residual(d, None, rf, out)
+    assert torch.equal(out.reshape(nz, ny, nx), (rb * m).float())
+    ngb.mg_apply(d, uf, out)
+    assert _close(out.reshape(nz, ny, nx), _lap64(ub, h) * m)
+
+
 @pytest.mark.parametrize("n", [12, 40])
 def test_restrict_prolong_kernels_and_adjoint(ngb, cuda, n):
     import torch
