@@ -648,9 +648,15 @@ def learned_fcg_run(args, n, dev, b, ws, pcg_seconds):
         x2 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
         res = solver.solve(b, x2, tol=1e-8, max_iter=2000, refresh_every=10, stall=30, fallback=True)
         solver.close()
+        # the same cycle without the network, through the same C-ABI solve
+        plain_solver = ngb.LearnedSolver(n, levels, None)
+        z = torch.empty_like(b)
+        plain_solver.precondition(b, z)
+        torch.cuda.synchronize()
+        del z
         x3 = torch.zeros(n ** 3, dtype=torch.float64, device=dev)
-        plain = fcg.fcg_solve_vcycle(fcg.VCycle(n, levels, coarse="none", device=dev), b, x3, tol=1e-8, max_iter=4000,
-                                     fallback=True, ws=ws)
+        plain = plain_solver.solve(b, x3, tol=1e-8, max_iter=4000, refresh_every=10, stall=30, fallback=True)
+        plain_solver.close()
         del x3
     else:
         net.forward(b)

@@ -593,7 +593,9 @@ int ngb_unet_read_weights(const char* path, float* weights, int64_t count);
 
 /* Creates the solver for an n^3 grid: n a multiple of 2^levels, the coarsest
  * grid n / 2^levels >= 8 and a multiple of 4 (two poolings); weights: host
- * FP32 array of ngb_unet_weight_count() values. Allocates device memory. */
+ * FP32 array of ngb_unet_weight_count() values, or NULL with count 0 for the
+ * same V-cycle without the network (the level above the coarsest gets no
+ * correction). Allocates device memory. */
 int ngb_learned_create(int32_t n, int32_t levels, const float* weights, int64_t count, ngb_learned_solver** solver);
 int ngb_learned_destroy(ngb_learned_solver* solver);
 /* z = M(r): one application of the preconditioner (FP32 n^3 fields). */

@@ -544,7 +544,8 @@ class LearnedSolver:
     """The learned-preconditioner Poisson solver of the C ABI (ngb_learned_*):
     FCG(1) with a V-cycle whose coarsest solve is the U-Net, FP64 true
     residual, Jacobi-PCG fallback. `weights`: a weight-file path or an FP32
-    host tensor of ngb_unet_weight_count() values."""
+    host tensor of ngb_unet_weight_count() values; None gives the same cycle
+    without the network (no coarsest-level correction)."""
 
     def __init__(self, n, levels, weights):
         import torch
@@ -552,10 +553,14 @@ class LearnedSolver:
         if isinstance(weights, (str, bytes, os.PathLike)):
             from .learned import read_weights
             weights = read_weights(weights)
-        w = weights.detach().to("cpu", torch.float32).contiguous()
-        self._keep = w
         h = ctypes.c_void_p()
-        check(L.ngb_learned_create(int(n), int(levels), ctypes.c_void_p(w.data_ptr()), w.numel(), ctypes.byref(h)))
+        if weights is None:
+            self._keep = None
+            check(L.ngb_learned_create(int(n), int(levels), None, 0, ctypes.byref(h)))
+        else:
+            w = weights.detach().to("cpu", torch.float32).contiguous()
+            self._keep = w
+            check(L.ngb_learned_create(int(n), int(levels), ctypes.c_void_p(w.data_ptr()), w.numel(), ctypes.byref(h)))
         self.handle, self.n, self.levels = h, n, levels
 
     def precondition(self, r, z, stream=None):

@@ -230,8 +230,7 @@ constexpr int halo_count()
 template <int Q>
 struct HaloTable {
     static constexpr int n = halo_count<Q>();
-    uint32_t             dst[n];
-    uint32_t             src[n];
+    uint2                e[n];  // {dst, src}: one 8-byte load per entry
 };
 
 template <int Q>
@@ -252,8 +251,7 @@ constexpr HaloTable<Q> make_halo_table()
                     const int cube = cube_src<Q>(q) + cube_voxel(i, j, k);
                     const int slot = (fx + 1) + 3 * (fy + 1) + 9 * (fz + 1);
                     const int nv = (si - 8 * fx) + 8 * (sj - 8 * fy) + 64 * (sk - 8 * fz);
-                    t.dst[n] = uint32_t(cube) | (uint32_t(slot) << 16);
-                    t.src[n] = uint32_t(q * kBlockVoxels + nv);
+                    t.e[n] = uint2{uint32_t(cube) | (uint32_t(slot) << 16), uint32_t(q * kBlockVoxels + nv)};
                     n++;
                 }
     }
@@ -304,8 +302,9 @@ __global__ void __launch_bounds__(kStagedThreads, 4)
 #pragma unroll
     for (int r = 0; r < kPer; r++) {
         const int it = t + r * kStagedThreads;
-        hd[r] = it < kHalo ? __ldg(&g_halo19.dst[it]) : 0xffffffffu;
-        hs[r] = it < kHalo ? __ldg(&g_halo19.src[it]) : 0u;
+        const uint2 te = it < kHalo ? __ldg(&g_halo19.e[it]) : uint2{0xffffffffu, 0u};
+        hd[r] = te.x;
+        hs[r] = te.y;
     }
     // halo values (a missing neighbour block leaves its cells unset: every
     // voxel pulling from one treats the direction as a wall); the neighbour

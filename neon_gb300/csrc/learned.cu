@@ -130,6 +130,7 @@ using namespace ngb;
 // ---------------------------------------------------------------- the solver object
 struct ngb_learned_solver {
     int n = 0, levels = 0, nc = 0;  // fine size, V-cycle levels, coarsest size (the network's grid)
+    bool net = true;                 // false: the same cycle without the coarsest correction
     double omega = 6.0 / 7.0;
     int    post = 2;
     std::vector<void*> allocs;
@@ -232,10 +233,13 @@ struct ngb_learned_solver {
         const ngb_poisson_desc* d = &desc[l];
         float*                  ul = outl ? outl : u[l];
         NGB_TRY(ngb_mg_jacobi(d, nullptr, rl, ul, omega, s));
-        NGB_TRY(ngb_mg_residual(d, ul, rl, res[l], s));
-        NGB_TRY(ngb_mg_restrict(d, res[l], r[l + 1], 1.0, s));
-        NGB_TRY(cycle(l + 1, r[l + 1], nullptr, s));
-        NGB_TRY(ngb_mg_prolong_add(d, l + 1 == levels ? e_c : u[l + 1], ul, s));
+        // without the network the level above the coarsest gets no correction
+        if (net || l + 1 < levels) {
+            NGB_TRY(ngb_mg_residual(d, ul, rl, res[l], s));
+            NGB_TRY(ngb_mg_restrict(d, res[l], r[l + 1], 1.0, s));
+            NGB_TRY(cycle(l + 1, r[l + 1], nullptr, s));
+            NGB_TRY(ngb_mg_prolong_add(d, l + 1 == levels ? e_c : u[l + 1], ul, s));
+        }
         float* a = ul;
         float* b = tmp[l];
         for (int k = 0; k < post; k++) {
@@ -334,9 +338,10 @@ int ngb_unet_read_weights(const char* path, float* w, int64_t count)
 
 int ngb_learned_create(int32_t n, int32_t levels, const float* weights, int64_t count, ngb_learned_solver** out)
 {
-    NGB_CHECK_ARG(out && weights, "NULL argument");
+    NGB_CHECK_ARG(out, "NULL argument");
     *out = nullptr;
-    NGB_CHECK_ARG(count == total_count(), "weight count %lld != %lld", (long long)count, (long long)total_count());
+    NGB_CHECK_ARG((weights == nullptr && count == 0) || (weights && count == total_count()), "weight count %lld != %lld",
+                  (long long)count, (long long)total_count());
     NGB_CHECK_ARG(levels >= 1 && levels <= 8, "levels must be in [1, 8]");
     NGB_CHECK_ARG(n > 0 && n % (1 << levels) == 0, "n must be a multiple of 2^levels");
     NGB_CHECK_ARG((n >> levels) >= 8 && (n >> levels) % 4 == 0, "the coarsest grid (n / 2^levels) must be >= 8 and a multiple of 4");
@@ -349,6 +354,7 @@ int ngb_learned_create(int32_t n, int32_t levels, const float* weights, int64_t 
     S->n = n;
     S->levels = levels;
     S->nc = n >> levels;
+    S->net = weights != nullptr;
     const int     nc = S->nc;
     const int64_t V0 = int64_t(nc) * nc * nc, V1 = V0 / 8, V2 = V0 / 64;
     int           rc = NGB_OK;
@@ -357,33 +363,35 @@ int ngb_learned_create(int32_t n, int32_t levels, const float* weights, int64_t 
         if ((rc = S->alloc(&(p), (bytes))) != NGB_OK) \
             return fail(rc);                          \
     } while (0)
-    NGB_ALLOC(S->in0, V0 * 16 * 2);
-    NGB_ALLOC(S->a0, V0 * 16 * 2);
-    NGB_ALLOC(S->cat0, V0 * 48 * 2);
-    NGB_ALLOC(S->d0a, V0 * 16 * 2);
-    NGB_ALLOC(S->out, V0 * 16 * 4);
-    NGB_ALLOC(S->p0, V1 * 16 * 2);
-    NGB_ALLOC(S->a1, V1 * 32 * 2);
-    NGB_ALLOC(S->cat1, V1 * 96 * 2);
-    NGB_ALLOC(S->d1a, V1 * 32 * 2);
-    NGB_ALLOC(S->d1b, V1 * 32 * 2);
-    NGB_ALLOC(S->p1, V2 * 32 * 2);
-    NGB_ALLOC(S->a2, V2 * 64 * 2);
-    NGB_ALLOC(S->b2, V2 * 64 * 2);
-    // weights: BF16 copies (round to nearest even) and their tensor-core images
-    const float* p = weights;
-    for (int l = 0; l < kNumLayers; l++) {
-        const size_t          cnt = size_t(layer_count(l));
-        std::vector<uint16_t> h(cnt);
-        for (size_t i = 0; i < cnt; i++) h[i] = bf16_rne(p[i]);
-        p += cnt;
-        NGB_ALLOC(S->wb[l], cnt * 2);
-        NGB_ALLOC(S->wp[l], cnt * 2);
-        if (cudaMemcpy(S->wb[l], h.data(), cnt * 2, cudaMemcpyHostToDevice) != cudaSuccess) {
-            set_error("weight upload failed");
-            return fail(NGB_ERR_CUDA);
+    if (S->net) {
+        NGB_ALLOC(S->in0, V0 * 16 * 2);
+        NGB_ALLOC(S->a0, V0 * 16 * 2);
+        NGB_ALLOC(S->cat0, V0 * 48 * 2);
+        NGB_ALLOC(S->d0a, V0 * 16 * 2);
+        NGB_ALLOC(S->out, V0 * 16 * 4);
+        NGB_ALLOC(S->p0, V1 * 16 * 2);
+        NGB_ALLOC(S->a1, V1 * 32 * 2);
+        NGB_ALLOC(S->cat1, V1 * 96 * 2);
+        NGB_ALLOC(S->d1a, V1 * 32 * 2);
+        NGB_ALLOC(S->d1b, V1 * 32 * 2);
+        NGB_ALLOC(S->p1, V2 * 32 * 2);
+        NGB_ALLOC(S->a2, V2 * 64 * 2);
+        NGB_ALLOC(S->b2, V2 * 64 * 2);
+        // weights: BF16 copies (round to nearest even) and their tensor-core images
+        const float* p = weights;
+        for (int l = 0; l < kNumLayers; l++) {
+            const size_t          cnt = size_t(layer_count(l));
+            std::vector<uint16_t> h(cnt);
+            for (size_t i = 0; i < cnt; i++) h[i] = bf16_rne(p[i]);
+            p += cnt;
+            NGB_ALLOC(S->wb[l], cnt * 2);
+            NGB_ALLOC(S->wp[l], cnt * 2);
+            if (cudaMemcpy(S->wb[l], h.data(), cnt * 2, cudaMemcpyHostToDevice) != cudaSuccess) {
+                set_error("weight upload failed");
+                return fail(NGB_ERR_CUDA);
+            }
+            if ((rc = ngb_conv3d_pack(kLayers[l].cout, kLayers[l].cin, S->wb[l], S->wp[l], nullptr)) != NGB_OK) return fail(rc);
         }
-        if ((rc = ngb_conv3d_pack(kLayers[l].cout, kLayers[l].cin, S->wb[l], S->wp[l], nullptr)) != NGB_OK) return fail(rc);
     }
     // V-cycle levels
     S->u.assign(levels, nullptr);
@@ -448,7 +456,8 @@ int ngb_learned_precondition(ngb_learned_solver* S, const float* r, float* z, vo
 int ngb_learned_solve(ngb_learned_solver* S, const float* b, double* x, const ngb_learned_params* prm, ngb_learned_result* res,
                       void* stream)
 {
-    NvtxRange nvtx("ngb_learned_solve");
+    // the cycle without the network under its own range name (profiles select the learned solve by name)
+    NvtxRange nvtx(S && !S->net ? "ngb_learned_solve_plain" : "ngb_learned_solve");
     NGB_CHECK_ARG(S && b && x && prm, "NULL argument");
     NGB_CHECK_ARG(prm->tol >= 0 && prm->max_iter >= 0 && prm->refresh_every >= 1 && prm->stall >= prm->refresh_every,
                   "bad params (tol >= 0, max_iter >= 0, refresh_every >= 1, stall >= refresh_every)");

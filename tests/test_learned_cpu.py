@@ -43,3 +43,15 @@ def test_create_rejects_bad_sizes(ngb, n, levels, msg):
     assert L.ngb_learned_create(n, levels, w.ctypes.data_as(ctypes.c_void_p), w.size, ctypes.byref(h)) == -1
     assert msg in L.ngb_last_error()
     assert not h.value
+
+
+def test_create_without_network_checks_the_count(ngb):
+    """weights NULL means the cycle without the network and needs count 0; a
+    weight array needs the full count."""
+    L = ngb.lib()
+    h = ctypes.c_void_p()
+    assert L.ngb_learned_create(64, 1, None, 5, ctypes.byref(h)) == -1
+    assert b"weight count" in L.ngb_last_error() and not h.value
+    w = np.zeros(4, np.float32)
+    assert L.ngb_learned_create(64, 1, w.ctypes.data_as(ctypes.c_void_p), 0, ctypes.byref(h)) == -1
+    assert not h.value

@@ -38,6 +38,27 @@ def test_precondition_bit_identical_to_python_vcycle(ngb, cuda, n, levels):
     S.close()
 
 
+@pytest.mark.parametrize("n,levels", [(64, 1), (128, 2)])
+def test_cycle_without_network_bit_identical_to_python(ngb, cuda, n, levels):
+    """weights=None: the same V-cycle without the coarsest correction, equal
+    to VCycle(coarse="none") bit for bit, and its FCG solve converges."""
+    import torch
+    from neon_gb300 import fcg
+    g = torch.Generator(device=cuda).manual_seed(6)
+    r = torch.randn(n ** 3, device=cuda, generator=g) * fcg.free_mask(n, cuda)
+    z_py = fcg.VCycle(n, levels, coarse="none", device=cuda)(r).clone()
+    S = ngb.LearnedSolver(n, levels, None)
+    z_c = torch.full_like(r, float("nan"))
+    S.precondition(r, z_c)
+    torch.cuda.synchronize()
+    assert torch.equal(z_c, z_py)
+    b = _rhs(ngb, n, cuda)
+    x = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
+    got = S.solve(b, x, tol=1e-8, max_iter=4000)
+    assert got["converged"] and not got["fallback"] and got["rel_residual"] <= 1e-8
+    S.close()
+
+
 def test_solve_matches_python_fcg(ngb, cuda):
     import torch
     from neon_gb300 import fcg
