@@ -43,6 +43,7 @@ constexpr int      kTcM = 128;           // voxels per tile (MMA M)
 constexpr int      kTcMaxStages = 8;     // shared-memory pipeline depth (at most)
 constexpr int      kTcThreads = 192;     // 6 warps
 constexpr int      kStripRows = kTcM + 2;  // plane mode: voxels x0 - 1 .. x0 + 128 of an image row
+constexpr int      kZSlots = 4;            // z-run mode: TMEM accumulators of output planes in flight
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;
@@ -137,6 +138,7 @@ struct TmemCols {
 struct TcParams {
     int                  nx, ny, nz, kc;  // kc = Cin / 16
     int                  plane;           // 1: plane mode, 0: tap mode
+    int                  zrun;            // plane mode: output planes per work unit marched in z (0: one plane)
     int                  ntile;           // tiles per work unit (2 / 1)
     int                  nstages;         // pipeline depth
     uint32_t             tmem_cols;       // allocated TMEM columns (two buffers of ntile * N)
@@ -177,6 +179,62 @@ __device__ __forceinline__ Unit unit_of(const TcParams& p, int64_t u)
     return t;
 }
 
+// z-run mode: work unit u covers the two rows y0, y0 + 1 of 128 voxels from
+// x0 on the output planes z0 .. z0 + nzo - 1.
+struct ZUnit {
+    int64_t v0;
+    int     x0, y0, z0, nzo;
+};
+__device__ __forceinline__ ZUnit zunit_of(const TcParams& p, int64_t u)
+{
+    ZUnit         t;
+    const int64_t xt = p.nx / kTcM, yt = p.ny / 2;
+    t.x0 = int(u % xt) * kTcM;
+    const int64_t r = u / xt;
+    t.y0 = int(r % yt) * 2;
+    t.z0 = int(r / yt) * p.zrun;
+    t.nzo = min(p.zrun, p.nz - t.z0);
+    t.v0 = t.x0 + int64_t(p.nx) * (t.y0 + int64_t(p.ny) * t.z0);
+    return t;
+}
+
+// Epilogue of one output tile: bias, ReLU, FP32 (optionally accumulated) or
+// BF16 output of voxel v (this thread's lane of the tile).
+template <int N, bool F32OUT>
+__device__ __forceinline__ void tc_store(const TcParams& p, int64_t v, float (&acc)[N])
+{
+    if (p.bias) {
+#pragma unroll
+        for (int c = 0; c < N; c++) acc[c] += __ldg(p.bias + c);
+    }
+    if constexpr (F32OUT) {
+        float* yo = static_cast<float*>(p.y) + v * p.ldy;
+#pragma unroll
+        for (int c = 0; c < N; c += 4) {
+            float4 o = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
+            if (p.accumulate) {
+                const float4 old = *reinterpret_cast<const float4*>(yo + c);
+                o.x += old.x, o.y += old.y, o.z += old.z, o.w += old.w;
+            }
+            *reinterpret_cast<float4*>(yo + c) = o;
+        }
+    } else {
+        __nv_bfloat16* yo = static_cast<__nv_bfloat16*>(p.y) + v * p.ldy;
+#pragma unroll
+        for (int c = 0; c < N; c += 8) {
+            uint32_t w4[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                float lo = acc[c + 2 * e], hi = acc[c + 2 * e + 1];
+                if (p.relu) lo = fmaxf(lo, 0.f), hi = fmaxf(hi, 0.f);
+                const __nv_bfloat162 h2 = __floats2bfloat162_rn(lo, hi);
+                w4[e] = *reinterpret_cast<const uint32_t*>(&h2);
+            }
+            *reinterpret_cast<uint4*>(yo + c) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        }
+    }
+}
+
 template <int N, bool F32OUT>
 __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_constant__ CUtensorMap xmap, TcParams p)
 {
@@ -186,7 +244,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     uint8_t* wres = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* stages = wres + p.w_region;
 
-    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[2], tempty_bar[2], drain_bar, w_bar;
+    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[kZSlots], tempty_bar[kZSlots], drain_bar,
+        w_bar;
     __shared__ uint32_t     tmem_base_sh;
     __shared__ volatile int abort_sh;
 
@@ -197,7 +256,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
-        for (int a = 0; a < 2; a++) {
+        for (int a = 0; a < kZSlots; a++) {
             mbar_init(&tfull_bar[a], 1);
             mbar_init(&tempty_bar[a], 4);
         }
@@ -229,7 +288,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         }
         uint32_t k = 0;
         bool     ok = true;
-        for (int64_t u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
+        // z-run mode: every input plane z0 - 1 .. z0 + nzo of the unit once, chunk by chunk
+        // (planes outside the grid read as zeros); the MMA issuer applies each to the three
+        // output planes it belongs to
+        for (int64_t u = blockIdx.x; p.zrun && u < p.units && ok; u += gridDim.x) {
+            const ZUnit t = zunit_of(p, u);
+            const int   nsu = (t.nzo + 2) * p.kc;
+            for (int i = 0; i < nsu; i++, k++) {
+                const int      chunk = i % p.kc, pi = i / p.kc;
+                const uint32_t s = k % ns;
+                if (!(ok = mbar_wait(&empty_bar[s], ((k / ns) & 1u) ^ 1u, &abort_sh))) break;
+                uint8_t* st = stages + size_t(s) * p.stage_bytes;
+                mbar_expect_tx(&full_bar[s], p.a_bytes);
+                tma_load_5d(st, &xmap, 0, t.x0 - 1, t.y0 - 1, t.z0 + pi - 1, 2 * chunk, &full_bar[s]);
+            }
+        }
+        for (int64_t u = blockIdx.x; !p.zrun && u < p.units && ok; u += gridDim.x) {
             const Unit t = unit_of(p, u);
             for (int i = 0; i < nst; i++, k++) {
                 // plane: i = dz_index * kc + chunk; tap: i = tap * kc + chunk, tap = 9 dz + 3 dy + dx (indices 0..2)
@@ -260,7 +334,46 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         // ------------------------------------------------ MMA issuer
         uint32_t k = 0, j = 0;
         bool     ok = !p.resident || mbar_wait(&w_bar, 0, &abort_sh);
-        for (int64_t u = blockIdx.x; u < p.units && ok; u += gridDim.x, j++) {
+        // z-run mode: input plane pi (z0 - 1 + pi) feeds output planes pi - dzi (local
+        // index) with the weights of dz index dzi; output plane o (counted over the
+        // CTA's units) accumulates in TMEM slot o % kZSlots, first written at its
+        // input plane pi = o, complete after pi = o + 2
+        uint32_t ob = 0;
+        for (int64_t u = blockIdx.x; p.zrun && u < p.units && ok; u += gridDim.x) {
+            const ZUnit t = zunit_of(p, u);
+            for (int pi = 0; pi < t.nzo + 2 && ok; pi++) {
+                for (int chunk = 0; chunk < p.kc; chunk++, k++) {
+                    const uint32_t s = k % ns;
+                    if (!(ok = mbar_wait(&full_bar[s], (k / ns) & 1u, &abort_sh))) break;
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(stages + size_t(s) * p.stage_bytes);
+                    for (int dzi = 0; dzi < 3; dzi++) {
+                        const int lo = pi - dzi;
+                        if (lo < 0 || lo >= t.nzo) continue;
+                        const uint32_t op = ob + uint32_t(lo), slot = op % kZSlots;
+                        if (dzi == 0 && chunk == 0) {  // this output's first MMAs: its slot must be drained
+                            if (!(ok = mbar_wait(&tempty_bar[slot], ((op / kZSlots) & 1u) ^ 1u, &abort_sh))) break;
+                            tc_fence_after();
+                        }
+                        const uint32_t d0 = tmem + slot * 2u * uint32_t(N);
+                        const uint32_t wb = smem_u32(wres) + uint32_t((dzi * p.kc + chunk) * 9) * slice;
+                        for (int tt = 0; tt < 2; tt++)
+                            for (int tap = 0; tap < 9; tap++) {
+                                const int      dyi = tap / 3, dxi = tap % 3;
+                                const uint32_t arow = uint32_t((tt + dyi) * p.a_row + dxi);
+                                const uint64_t ad = smem_desc(sa + arow * 16u, p.a_lbo, 128);
+                                const uint64_t bd = smem_desc(wb + uint32_t(tap) * slice, N * 16, 128);
+                                mma_bf16(d0 + uint32_t(tt) * N, ad, bd, kIdesc, (dzi > 0 || chunk > 0 || tap > 0) ? 1u : 0u);
+                            }
+                    }
+                    if (!ok) break;
+                    mma_commit(&empty_bar[s]);
+                    if (chunk == p.kc - 1 && pi >= 2) mma_commit(&tfull_bar[(ob + uint32_t(pi - 2)) % kZSlots]);
+                }
+            }
+            ob += uint32_t(t.nzo);
+        }
+        for (int64_t u = blockIdx.x; !p.zrun && u < p.units && ok; u += gridDim.x, j++) {
             const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
             if (!(ok = mbar_wait(&tempty_bar[a], ph ^ 1u, &abort_sh))) break;
             tc_fence_after();
@@ -301,7 +414,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         // ------------------------------------------------ epilogue
         const uint32_t q = uint32_t(warp & 3);  // the TMEM lane quarter this warp may read
         uint32_t       j = 0;
-        for (int64_t u = blockIdx.x; u < p.units; u += gridDim.x, j++) {
+        bool           ok = true;
+        uint32_t       ob = 0;
+        for (int64_t u = blockIdx.x; p.zrun && u < p.units && ok; u += gridDim.x) {
+            const ZUnit t = zunit_of(p, u);
+            for (int lo = 0; lo < t.nzo; lo++) {
+                const uint32_t op = ob + uint32_t(lo), slot = op % kZSlots;
+                if (!(ok = mbar_wait(&tfull_bar[slot], (op / kZSlots) & 1u, &abort_sh))) break;
+                tc_fence_after();
+                for (int tt = 0; tt < 2; tt++) {
+                    float acc[N];
+#pragma unroll
+                    for (int c = 0; c < N; c += 16)
+                        tmem_ld16(tmem + ((q * 32u) << 16) + slot * 2u * uint32_t(N) + uint32_t(tt) * N + c, acc + c);
+                    if (tt == 1) {
+                        tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) mbar_arrive(&tempty_bar[slot]);
+                    }
+                    const int64_t v = t.v0 + int64_t(lo) * p.nx * p.ny + int64_t(tt) * p.nx + q * 32 + lane;
+                    tc_store<N, F32OUT>(p, v, acc);
+                }
+            }
+            ob += uint32_t(t.nzo);
+        }
+        for (int64_t u = blockIdx.x; !p.zrun && u < p.units; u += gridDim.x, j++) {
             const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
             if (!mbar_wait(&tfull_bar[a], ph, &abort_sh)) break;
             tc_fence_after();
@@ -316,36 +453,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
                     if (lane == 0) mbar_arrive(&tempty_bar[a]);
                 }
                 const int64_t v = t.v0 + int64_t(tt) * p.nx + q * 32 + lane;
-                if (p.bias) {
-#pragma unroll
-                    for (int c = 0; c < N; c++) acc[c] += __ldg(p.bias + c);
-                }
-                if constexpr (F32OUT) {
-                    float* yo = static_cast<float*>(p.y) + v * p.ldy;
-#pragma unroll
-                    for (int c = 0; c < N; c += 4) {
-                        float4 o = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
-                        if (p.accumulate) {
-                            const float4 old = *reinterpret_cast<const float4*>(yo + c);
-                            o.x += old.x, o.y += old.y, o.z += old.z, o.w += old.w;
-                        }
-                        *reinterpret_cast<float4*>(yo + c) = o;
-                    }
-                } else {
-                    __nv_bfloat16* yo = static_cast<__nv_bfloat16*>(p.y) + v * p.ldy;
-#pragma unroll
-                    for (int c = 0; c < N; c += 8) {
-                        uint32_t w4[4];
-#pragma unroll
-                        for (int e = 0; e < 4; e++) {
-                            float lo = acc[c + 2 * e], hi = acc[c + 2 * e + 1];
-                            if (p.relu) lo = fmaxf(lo, 0.f), hi = fmaxf(hi, 0.f);
-                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(lo, hi);
-                            w4[e] = *reinterpret_cast<const uint32_t*>(&h2);
-                        }
-                        *reinterpret_cast<uint4*>(yo + c) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
-                    }
-                }
+                tc_store<N, F32OUT>(p, v, acc);
             }
         }
     }
@@ -703,13 +811,28 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
     p.w_region = p.resident ? (p.w_bytes + 1023u) & ~1023u : 0u;
     p.b_bytes = p.resident ? 0u : uint32_t(plane ? 9 : 1) * uint32_t(cout) * 32u;
     p.stage_bytes = ((p.a_bytes + 127u) & ~127u) + ((p.b_bytes + 127u) & ~127u);
+    // z-run mode (plane mode, resident weights, Cout 16 / 32): a unit marches over
+    // up to 16 output planes and stages each input plane once instead of three
+    // times, with kZSlots accumulators of two tiles in TMEM (at most 256 columns,
+    // so two CTAs per SM keep fitting)
+    const bool zrun = plane && p.resident && (cout == 16 || cout == 32);
+    int        zr = 0;
+    if (zrun) {
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 152;
+        const int64_t cols2d = int64_t(nx / kTcM) * (ny / 2);
+        zr = 16;  // shorter runs while the units would not give every CTA (two per SM) four of them
+        while (zr > 4 && cols2d * ((nz + zr - 1) / zr) < int64_t(8) * sms) zr /= 2;
+    }
+    p.zrun = zr;
     uint32_t cols = 32;
-    while (cols < uint32_t(2 * p.ntile * cout)) cols *= 2;
+    while (cols < uint32_t(zr ? kZSlots * 2 * cout : 2 * p.ntile * cout)) cols *= 2;
     p.tmem_cols = cols;
     // depth: as many stages as fit in ~108 KB (two CTAs per SM) or ~200 KB (one), 2 to 8
     const uint32_t budget = (cols <= 256 ? 108u * 1024u : 200u * 1024u) - p.w_region;
     p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, budget / p.stage_bytes)));
-    p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * nz : int64_t(nx) * ny * nz / kTcM;
+    p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * (zr ? (nz + zr - 1) / zr : nz) : int64_t(nx) * ny * nz / kTcM;
     p.wpk = static_cast<const __nv_bfloat16*>(wpacked);
     p.bias = bias, p.y = y, p.ldy = ldy, p.relu = relu, p.accumulate = accumulate;
     if (p.units == 0) return NGB_OK;

@@ -236,6 +236,45 @@ def test_conv_tensor_cores_many_tiles_match_mma(ngb, cuda, dims, cin, cout):
     assert err <= 1e-5 * scale, (err / scale, int(torch.isnan(Y).sum()))
 
 
+@pytest.mark.parametrize("dims", [(79, 128, 512), (37, 4, 128), (3, 2, 128)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (16, 32), (32, 32)])
+def test_conv_tensor_cores_z_runs_match_mma(ngb, cuda, dims, cin, cout):
+    """Plane-mode layers with Cout 16 / 32 march each work unit over a run of
+    output planes (16 at the largest size here, 4 on the small grids; the
+    last run ragged, a grid shorter than one run): every input plane staged
+    once, the three output planes it feeds accumulated in a ring of TMEM
+    slots. Against the mma.sync kernel, FP32 output with bias and with
+    accumulation, BF16 output with ReLU."""
+    import torch
+    nz, ny, nx = dims
+    L = ngb.lib()
+    assert L.ngb_conv3d_tc_supported(nx, ny, nz, cin, cin, cout, cout) == 1
+    g = torch.Generator(device="cpu").manual_seed(7 * cin + cout + nz)
+    X = torch.randn(nx * ny * nz, cin, generator=g).to(torch.bfloat16).to(cuda)
+    W = (torch.randn(cout, 27, cin, generator=g) / (27 * cin) ** 0.5).to(torch.bfloat16).to(cuda)
+    bias = torch.randn(cout, generator=g).to(cuda) * 0.1
+    Wp = torch.empty_like(W)
+    ngb.check(L.ngb_conv3d_pack(cout, cin, ngb._ptr(W), ngb._ptr(Wp), None))
+    ref = torch.zeros(X.shape[0], cout, dtype=torch.float32, device=cuda)
+    ngb.check(L.ngb_conv3d(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(W), None, ngb._ptr(ref), cout, cout, 1, 0, 0, None))
+    ref += bias
+    Y = torch.full_like(ref, float("nan"))
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), ngb._ptr(bias), ngb._ptr(Y), cout, cout, 1, 0, 0,
+                              None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    scale = float(ref.abs().max())
+    assert float((Y - ref).abs().max()) <= 1e-5 * scale, int(torch.isnan(Y).sum())
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), ngb._ptr(bias), ngb._ptr(Y), cout, cout, 1, 0, 1,
+                              None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    assert float((Y - 2 * ref).abs().max()) <= 2e-5 * scale
+    Yb = torch.zeros(X.shape[0], cout, dtype=torch.bfloat16, device=cuda)
+    ngb.check(L.ngb_conv3d_tc(nx, ny, nz, ngb._ptr(X), cin, cin, ngb._ptr(Wp), ngb._ptr(bias), ngb._ptr(Yb), cout, cout, 0, 1, 0,
+                              None))
+    ngb.check(L.ngb_conv3d_tc_check(None))
+    assert float((Yb.float() - ref.clamp(min=0)).abs().max()) <= 2 ** -7 * scale
+
+
 def test_unet_tensor_cores_match_mma_path_at_128(ngb, cuda):
     """At 128^3 level 0 runs in plane mode with many tiles per CTA: the U-Net
     forward pass and the layer gradients on the tensor cores against the
