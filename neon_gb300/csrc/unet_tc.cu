@@ -43,7 +43,7 @@ constexpr int      kTcM = 128;           // voxels per tile (MMA M)
 constexpr int      kTcMaxStages = 8;     // shared-memory pipeline depth (at most)
 constexpr int      kTcThreads = 192;     // 6 warps
 constexpr int      kStripRows = kTcM + 2;  // plane mode: voxels x0 - 1 .. x0 + 128 of an image row
-constexpr int      kZSlots = 4;            // z-run mode: TMEM accumulators of output planes in flight
+constexpr int      kZMax = 8;              // z-run mode: output planes per work unit (at most)
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;
@@ -130,6 +130,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Zeros into 16 TMEM columns of this warp's 32 lanes (z-run accumulators are
+// cleared by the epilogue after it has read them).
+__device__ __forceinline__ void tmem_zero16(uint32_t taddr)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
+        "r"(0u)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 template <int N>
 struct TmemCols {
     static constexpr uint32_t value = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
@@ -198,6 +209,28 @@ __device__ __forceinline__ ZUnit zunit_of(const TcParams& p, int64_t u)
     return t;
 }
 
+// The 18 MMAs of one plane-mode stage (two output rows x the 9 (dy, dx) taps)
+// into the accumulator pair at TMEM column d0. Descriptors are the stage's
+// and the weight slices' base descriptors plus compile-time offsets in the
+// 16-byte address field: A row (tt + dy) * 130 + dx of the staged image, B
+// slice tap (N * 32 bytes each); both stay inside shared memory (< 2^18
+// bytes), so the 14-bit field takes the sum without a carry. `acc`: whether
+// the first tap adds to the accumulators (the other taps always do).
+template <int N>
+__device__ __forceinline__ void plane_stage_mmas(uint32_t d0, uint64_t a0, uint64_t b0, uint32_t acc)
+{
+    constexpr uint32_t kIdesc = idesc_bf16_f32(kTcM, N);
+#pragma unroll
+    for (int tt = 0; tt < 2; tt++)
+#pragma unroll
+        for (int tap = 0; tap < 9; tap++) {
+            constexpr int  kRow = kStripRows;
+            const uint64_t ad = a0 + uint64_t((tt + tap / 3) * kRow + tap % 3);
+            const uint64_t bd = b0 + uint64_t(tap * (N * 32 / 16));
+            mma_bf16(d0 + uint32_t(tt * N), ad, bd, kIdesc, tap > 0 ? 1u : acc);
+        }
+}
+
 // Epilogue of one output tile: bias, ReLU, FP32 (optionally accumulated) or
 // BF16 output of voxel v (this thread's lane of the tile).
 template <int N, bool F32OUT>
@@ -244,8 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     uint8_t* wres = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* stages = wres + p.w_region;
 
-    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[kZSlots], tempty_bar[kZSlots], drain_bar,
-        w_bar;
+    __shared__ uint64_t     full_bar[kTcMaxStages], empty_bar[kTcMaxStages], tfull_bar[kZMax], tempty_bar[kZMax], drain_bar, w_bar;
     __shared__ uint32_t     tmem_base_sh;
     __shared__ volatile int abort_sh;
 
@@ -256,7 +288,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
-        for (int a = 0; a < kZSlots; a++) {
+        for (int a = 0; a < kZMax; a++) {
             mbar_init(&tfull_bar[a], 1);
             mbar_init(&tempty_bar[a], 4);
         }
@@ -276,15 +308,44 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     tc_fence_after();
     const uint32_t tmem = tmem_base_sh;
     const uint32_t half_cols = p.tmem_cols / 2;           // accumulator buffer 1 starts here
+    // z-run mode: tile tt's output plane lo accumulates in TMEM columns
+    // tt * zcols + (zrun - 1 - lo) * N; every MMA adds to its columns, which
+    // start at zero and are cleared again by the epilogue after each read
+    const uint32_t zcols = uint32_t(p.zrun) * N;
+    if (p.zrun) {
+        if (warp >= 2) {
+            const uint32_t q = uint32_t(warp & 3);
+            for (uint32_t c = 0; c < 2 * zcols; c += 16) tmem_zero16(tmem + ((q * 32u) << 16) + c);
+            tmem_wait_st();
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
     const int      nst = (p.plane ? 3 : 27) * p.kc;       // stages per unit
     const uint32_t slice = uint32_t(N) * 32u;             // B bytes of one (tap, chunk)
     const uint32_t b_off = p.stage_bytes - ((p.b_bytes + 127u) & ~127u);
 
     if (warp == 0 && lane == 0) {
         // ------------------------------------------------ TMA producer
-        if (p.resident) {  // the whole packed weight image, once
+        if (p.resident && p.zrun) {
+            // z-run mode: the three dz slices of each (chunk, tap, K half) side by side, so
+            // that one MMA of N = 3 Cout applies an input plane to three output planes:
+            // smem[((((c16 * 9 + tap) * 2 + h) * 3 + dz) * N + n) * 8 + e]
             mbar_expect_tx(&w_bar, p.w_bytes);
-            bulk_load(wres, p.wpk, p.w_bytes, &w_bar);
+            const uint32_t blk = uint32_t(N) * 16u;  // bytes of one (dz, c16, tap, h) block
+            for (int c16 = 0; c16 < p.kc; c16++)
+                for (int tap = 0; tap < 9; tap++)
+                    for (int h = 0; h < 2; h++)
+                        for (int dz = 0; dz < 3; dz++) {
+                            const uint32_t src = uint32_t(((dz * p.kc + c16) * 9 + tap) * 2 + h) * blk;
+                            const uint32_t dst = uint32_t(((c16 * 9 + tap) * 2 + h) * 3 + dz) * blk;
+                            bulk_load(wres + dst, reinterpret_cast<const uint8_t*>(p.wpk) + src, blk, &w_bar);
+                        }
+        } else if (p.resident) {  // the whole packed weight image, once
+            mbar_expect_tx(&w_bar, p.w_bytes);
+            for (uint32_t off = 0; off < p.w_bytes; off += 65536u)  // copies of at most 64 KB
+                bulk_load(wres + off, reinterpret_cast<const uint8_t*>(p.wpk) + off, min(65536u, p.w_bytes - off), &w_bar);
         }
         uint32_t k = 0;
         bool     ok = true;
@@ -334,44 +395,44 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         // ------------------------------------------------ MMA issuer
         uint32_t k = 0, j = 0;
         bool     ok = !p.resident || mbar_wait(&w_bar, 0, &abort_sh);
-        // z-run mode: input plane pi (z0 - 1 + pi) feeds output planes pi - dzi (local
-        // index) with the weights of dz index dzi; output plane o (counted over the
-        // CTA's units) accumulates in TMEM slot o % kZSlots, first written at its
-        // input plane pi = o, complete after pi = o + 2
-        uint32_t ob = 0;
+        // z-run mode: input plane pi (z0 - 1 + pi) feeds the output planes lo = pi - j
+        // (j = 0, 1, 2: weights of dz index j) that lie in the unit: blocks jlo .. jhi,
+        // whose accumulators are adjacent in TMEM, in one MMA of N = (jhi - jlo + 1) Cout
+        // per (tile, tap). Output plane lo's columns must have been read and cleared by
+        // the epilogue before its first MMA (pi = lo); it is complete after pi = lo + 2.
+        uint32_t upar = 0;  // bit lo: parity of the uses of output slot lo so far
         for (int64_t u = blockIdx.x; p.zrun && u < p.units && ok; u += gridDim.x) {
             const ZUnit t = zunit_of(p, u);
             for (int pi = 0; pi < t.nzo + 2 && ok; pi++) {
+                const int jlo = max(0, pi - t.nzo + 1), jhi = min(2, pi);
+                if (pi < t.nzo) {
+                    if (!(ok = mbar_wait(&tempty_bar[pi], ((upar >> pi) & 1u) ^ 1u, &abort_sh))) break;
+                    tc_fence_after();
+                }
+                const uint32_t idesc = idesc_bf16_f32(kTcM, (jhi - jlo + 1) * N);
+                const uint32_t dcol = uint32_t(p.zrun - 1 - pi + jlo) * N;
                 for (int chunk = 0; chunk < p.kc; chunk++, k++) {
                     const uint32_t s = k % ns;
                     if (!(ok = mbar_wait(&full_bar[s], (k / ns) & 1u, &abort_sh))) break;
                     tc_fence_after();
-                    const uint32_t sa = smem_u32(stages + size_t(s) * p.stage_bytes);
-                    for (int dzi = 0; dzi < 3; dzi++) {
-                        const int lo = pi - dzi;
-                        if (lo < 0 || lo >= t.nzo) continue;
-                        const uint32_t op = ob + uint32_t(lo), slot = op % kZSlots;
-                        if (dzi == 0 && chunk == 0) {  // this output's first MMAs: its slot must be drained
-                            if (!(ok = mbar_wait(&tempty_bar[slot], ((op / kZSlots) & 1u) ^ 1u, &abort_sh))) break;
-                            tc_fence_after();
+                    const uint64_t a0 = smem_desc(smem_u32(stages + size_t(s) * p.stage_bytes), p.a_lbo, 128);
+                    const uint64_t b0 = smem_desc(smem_u32(wres) + uint32_t(chunk * 9) * (96u * N), 48 * N, 128) +
+                                        uint64_t(jlo * N);  // rows of block jlo (16 bytes each, >> 4)
+#pragma unroll
+                    for (int tt = 0; tt < 2; tt++)
+#pragma unroll
+                        for (int tap = 0; tap < 9; tap++) {
+                            const uint64_t ad = a0 + uint64_t((tt + tap / 3) * kStripRows + tap % 3);
+                            const uint64_t bd = b0 + uint64_t(tap * 6 * N);  // 96 N bytes per tap, >> 4
+                            mma_bf16(tmem + uint32_t(tt) * zcols + dcol, ad, bd, idesc, 1u);
                         }
-                        const uint32_t d0 = tmem + slot * 2u * uint32_t(N);
-                        const uint32_t wb = smem_u32(wres) + uint32_t((dzi * p.kc + chunk) * 9) * slice;
-                        for (int tt = 0; tt < 2; tt++)
-                            for (int tap = 0; tap < 9; tap++) {
-                                const int      dyi = tap / 3, dxi = tap % 3;
-                                const uint32_t arow = uint32_t((tt + dyi) * p.a_row + dxi);
-                                const uint64_t ad = smem_desc(sa + arow * 16u, p.a_lbo, 128);
-                                const uint64_t bd = smem_desc(wb + uint32_t(tap) * slice, N * 16, 128);
-                                mma_bf16(d0 + uint32_t(tt) * N, ad, bd, kIdesc, (dzi > 0 || chunk > 0 || tap > 0) ? 1u : 0u);
-                            }
-                    }
-                    if (!ok) break;
                     mma_commit(&empty_bar[s]);
-                    if (chunk == p.kc - 1 && pi >= 2) mma_commit(&tfull_bar[(ob + uint32_t(pi - 2)) % kZSlots]);
+                    if (chunk == p.kc - 1 && pi >= 2) {
+                        mma_commit(&tfull_bar[pi - 2]);
+                        upar ^= 1u << (pi - 2);
+                    }
                 }
             }
-            ob += uint32_t(t.nzo);
         }
         for (int64_t u = blockIdx.x; !p.zrun && u < p.units && ok; u += gridDim.x, j++) {
             const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
@@ -392,14 +453,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
                 }
                 if (p.plane) {
                     // the first stage of a unit overwrites each tile's accumulator with its first MMA
-                    for (int tt = 0; tt < 2; tt++)
-                        for (int tap = 0; tap < 9; tap++) {
-                            const int      dyi = tap / 3, dxi = tap % 3;
-                            const uint32_t arow = uint32_t((tt + dyi) * p.a_row + dxi);
-                            const uint64_t ad = smem_desc(sa + arow * 16u, p.a_lbo, 128);
-                            const uint64_t bd = smem_desc(sb + uint32_t(tap) * slice, N * 16, 128);
-                            mma_bf16(d0 + uint32_t(tt) * N, ad, bd, kIdesc, (i > 0 || tap > 0) ? 1u : 0u);
-                        }
+                    plane_stage_mmas<N>(d0, smem_desc(sa, p.a_lbo, 128), smem_desc(sb, N * 16, 128), i > 0 ? 1u : 0u);
                 } else {
                     mma_bf16(d0, smem_desc(sa, p.a_lbo, 128), smem_desc(sb, N * 16, 128), kIdesc, i > 0 ? 1u : 0u);
                 }
@@ -415,28 +469,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         const uint32_t q = uint32_t(warp & 3);  // the TMEM lane quarter this warp may read
         uint32_t       j = 0;
         bool           ok = true;
-        uint32_t       ob = 0;
+        uint32_t       upar = 0;  // bit lo: parity of the uses of output slot lo so far
         for (int64_t u = blockIdx.x; p.zrun && u < p.units && ok; u += gridDim.x) {
             const ZUnit t = zunit_of(p, u);
             for (int lo = 0; lo < t.nzo; lo++) {
-                const uint32_t op = ob + uint32_t(lo), slot = op % kZSlots;
-                if (!(ok = mbar_wait(&tfull_bar[slot], (op / kZSlots) & 1u, &abort_sh))) break;
+                if (!(ok = mbar_wait(&tfull_bar[lo], (upar >> lo) & 1u, &abort_sh))) break;
                 tc_fence_after();
                 for (int tt = 0; tt < 2; tt++) {
-                    float acc[N];
+                    const uint32_t ta = tmem + ((q * 32u) << 16) + uint32_t(tt) * zcols + uint32_t(p.zrun - 1 - lo) * N;
+                    float          acc[N];
 #pragma unroll
-                    for (int c = 0; c < N; c += 16)
-                        tmem_ld16(tmem + ((q * 32u) << 16) + slot * 2u * uint32_t(N) + uint32_t(tt) * N + c, acc + c);
-                    if (tt == 1) {
-                        tc_fence_before();
-                        __syncwarp();
-                        if (lane == 0) mbar_arrive(&tempty_bar[slot]);
+                    for (int c = 0; c < N; c += 16) {
+                        tmem_ld16(ta + c, acc + c);
+                        tmem_zero16(ta + c);
                     }
                     const int64_t v = t.v0 + int64_t(lo) * p.nx * p.ny + int64_t(tt) * p.nx + q * 32 + lane;
                     tc_store<N, F32OUT>(p, v, acc);
                 }
+                tmem_wait_st();
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&tempty_bar[lo]);
+                upar ^= 1u << lo;
             }
-            ob += uint32_t(t.nzo);
         }
         for (int64_t u = blockIdx.x; !p.zrun && u < p.units; u += gridDim.x, j++) {
             const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
@@ -807,14 +862,18 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
     p.a_lbo = uint32_t(bx * by) * 16u;
     p.a_bytes = p.a_lbo * 2u;
     p.w_bytes = uint32_t(27 * cout * cin * 2);
-    p.resident = p.w_bytes <= 56u * 1024u ? 1 : 0;  // most layers: weights loaded once per CTA
+    // most layers: weights loaded once per CTA (two CTAs per SM); a plane-mode layer
+    // with Cout 16 / 32 keeps up to 168 KB of weights resident at one CTA per SM,
+    // which lets it run in z-run mode
+    const bool big_resident = plane && (cout == 16 || cout == 32) && p.w_bytes <= 168u * 1024u;
+    p.resident = (p.w_bytes <= 56u * 1024u || big_resident) ? 1 : 0;
     p.w_region = p.resident ? (p.w_bytes + 1023u) & ~1023u : 0u;
     p.b_bytes = p.resident ? 0u : uint32_t(plane ? 9 : 1) * uint32_t(cout) * 32u;
     p.stage_bytes = ((p.a_bytes + 127u) & ~127u) + ((p.b_bytes + 127u) & ~127u);
     // z-run mode (plane mode, resident weights, Cout 16 / 32): a unit marches over
-    // up to 16 output planes and stages each input plane once instead of three
-    // times, with kZSlots accumulators of two tiles in TMEM (at most 256 columns,
-    // so two CTAs per SM keep fitting)
+    // zr output planes and stages each input plane once instead of three times;
+    // its accumulators (zr planes x two tiles x Cout columns) fill at most 256
+    // TMEM columns, so two CTAs per SM keep fitting
     const bool zrun = plane && p.resident && (cout == 16 || cout == 32);
     int        zr = 0;
     if (zrun) {
@@ -822,15 +881,16 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             sms = 152;
         const int64_t cols2d = int64_t(nx / kTcM) * (ny / 2);
-        zr = 16;  // shorter runs while the units would not give every CTA (two per SM) four of them
-        while (zr > 4 && cols2d * ((nz + zr - 1) / zr) < int64_t(8) * sms) zr /= 2;
+        zr = std::min(kZMax, 128 / cout);  // 8 planes at Cout 16, 4 at Cout 32
+        // shorter runs while the units would not give every CTA (two per SM) four of them
+        while (zr > 2 && cols2d * ((nz + zr - 1) / zr) < int64_t(8) * sms) zr /= 2;
     }
     p.zrun = zr;
     uint32_t cols = 32;
-    while (cols < uint32_t(zr ? kZSlots * 2 * cout : 2 * p.ntile * cout)) cols *= 2;
+    while (cols < uint32_t(zr ? 2 * zr * cout : 2 * p.ntile * cout)) cols *= 2;
     p.tmem_cols = cols;
     // depth: as many stages as fit in ~108 KB (two CTAs per SM) or ~200 KB (one), 2 to 8
-    const uint32_t budget = (cols <= 256 ? 108u * 1024u : 200u * 1024u) - p.w_region;
+    const uint32_t budget = (cols <= 256 && p.w_region <= 56u * 1024u ? 108u * 1024u : 200u * 1024u) - p.w_region;
     p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, budget / p.stage_bytes)));
     p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * (zr ? (nz + zr - 1) / zr : nz) : int64_t(nx) * ny * nz / kTcM;
     p.wpk = static_cast<const __nv_bfloat16*>(wpacked);
