@@ -215,21 +215,60 @@ __global__ void relu_bwd_kernel(int64_t V, int C, const float* __restrict__ dy, 
     }
 }
 
-// 2x2x2 average pooling (fine nx*ny*nz even) and its adjoint.
+// 2x2x2 average pooling (fine nx*ny*nz even) and its adjoint. The forward
+// kernels walk coarse rows (Y, Z) with a block stride and a row's voxels
+// (times channels) with a thread stride: one 32-bit division per row, and
+// blocks that each move many rows (a block per row left the GPU scheduling
+// blocks). Children summed in the order d = 0..7 (bit 0: x, bit 1: y, bit 2: z).
 __global__ void pool2_kernel(Grid3 fine, int C, const __nv_bfloat16* __restrict__ x, int ldx, __nv_bfloat16* __restrict__ y, int ldy)
 {
-    const int     cx = fine.nx / 2, cy = fine.ny / 2, cz = fine.nz / 2;
-    const int64_t Vc = int64_t(cx) * cy * cz;
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < Vc * C; i += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t vc = i / C;
-        const int     c = int(i % C);
-        const int     X = int(vc % cx), Y = int((vc / cx) % cy), Z = int(vc / (int64_t(cx) * cy));
-        float         s = 0.f;
-        for (int d = 0; d < 8; d++) {
-            const int64_t vf = (2 * X + (d & 1)) + int64_t(fine.nx) * ((2 * Y + ((d >> 1) & 1)) + int64_t(fine.ny) * (2 * Z + (d >> 2)));
-            s += __bfloat162float(x[vf * ldx + c]);
+    const int cx = fine.nx / 2, cy = fine.ny / 2, rows = cy * (fine.nz / 2);
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int Y = row % cy, Z = row / cy;
+        for (int t = threadIdx.x; t < cx * C; t += blockDim.x) {
+            const int     X = t / C, c = t - X * C;
+            const int64_t vc = X + int64_t(cx) * (Y + int64_t(cy) * Z);
+            float         s = 0.f;
+#pragma unroll
+            for (int d = 0; d < 8; d++) {
+                const int64_t vf =
+                    (2 * X + (d & 1)) + int64_t(fine.nx) * ((2 * Y + ((d >> 1) & 1)) + int64_t(fine.ny) * (2 * Z + (d >> 2)));
+                s += __bfloat162float(x[vf * ldx + c]);
+            }
+            y[vc * ldy + c] = __float2bfloat16_rn(0.125f * s);
         }
-        y[vc * ldy + c] = __float2bfloat16_rn(0.125f * s);
+    }
+}
+// The same with eight channels per thread (16-byte loads and stores): C, ldx
+// and ldy multiples of 8, x and y 16-byte aligned.
+__global__ void pool2_vec_kernel(Grid3 fine, int G, const uint4* __restrict__ x, int ldx8, uint4* __restrict__ y, int ldy8)
+{
+    const int cx = fine.nx / 2, cy = fine.ny / 2, rows = cy * (fine.nz / 2);
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int Y = row % cy, Z = row / cy;
+        for (int t = threadIdx.x; t < cx * G; t += blockDim.x) {
+            const int     X = t / G, g = t - X * G;
+            const int64_t vc = X + int64_t(cx) * (Y + int64_t(cy) * Z);
+            float         s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int d = 0; d < 8; d++) {
+                const int64_t vf =
+                    (2 * X + (d & 1)) + int64_t(fine.nx) * ((2 * Y + ((d >> 1) & 1)) + int64_t(fine.ny) * (2 * Z + (d >> 2)));
+                const uint4           w = __ldg(x + vf * ldx8 + g);
+                const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&w);
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const float2 f = __bfloat1622float2(h[e]);
+                    s[2 * e] += f.x;
+                    s[2 * e + 1] += f.y;
+                }
+            }
+            uint4            o;
+            __nv_bfloat162* oh = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+            for (int e = 0; e < 4; e++) oh[e] = __floats2bfloat162_rn(0.125f * s[2 * e], 0.125f * s[2 * e + 1]);
+            y[vc * ldy8 + g] = o;
+        }
     }
 }
 __global__ void pool2_bwd_kernel(Grid3 fine, int C, const float* __restrict__ dy, int lddy, float* __restrict__ dx, int lddx,
@@ -246,15 +285,32 @@ __global__ void pool2_bwd_kernel(Grid3 fine, int C, const float* __restrict__ dy
     }
 }
 // Nearest 2x upsampling (coarse -> fine) and its adjoint (sum of the 8 children).
+// Forward: fine rows (y, z) with a block stride, a row's voxels (times
+// channels, or 8-channel groups) with a thread stride.
 __global__ void up2_kernel(Grid3 fine, int C, const __nv_bfloat16* __restrict__ x, int ldx, __nv_bfloat16* __restrict__ y, int ldy)
 {
-    const int cx = fine.nx / 2, cy = fine.ny / 2;
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < fine.V * C; i += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t vf = i / C;
-        const int     c = int(i % C);
-        const int     xx = int(vf % fine.nx), yy = int((vf / fine.nx) % fine.ny), zz = int(vf / (int64_t(fine.nx) * fine.ny));
-        const int64_t vc = (xx / 2) + int64_t(cx) * ((yy / 2) + int64_t(cy) * (zz / 2));
-        y[vf * ldy + c] = x[vc * ldx + c];
+    const int rows = fine.ny * fine.nz;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int yy = row % fine.ny, zz = row / fine.ny;
+        for (int t = threadIdx.x; t < fine.nx * C; t += blockDim.x) {
+            const int     xx = t / C, c = t - xx * C;
+            const int64_t vf = xx + int64_t(fine.nx) * (yy + int64_t(fine.ny) * zz);
+            const int64_t vc = (xx >> 1) + int64_t(fine.nx / 2) * ((yy >> 1) + int64_t(fine.ny / 2) * (zz >> 1));
+            y[vf * ldy + c] = x[vc * ldx + c];
+        }
+    }
+}
+__global__ void up2_vec_kernel(Grid3 fine, int G, const uint4* __restrict__ x, int ldx8, uint4* __restrict__ y, int ldy8)
+{
+    const int rows = fine.ny * fine.nz;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const int yy = row % fine.ny, zz = row / fine.ny;
+        for (int t = threadIdx.x; t < fine.nx * G; t += blockDim.x) {
+            const int     xx = t / G, g = t - xx * G;
+            const int64_t vf = xx + int64_t(fine.nx) * (yy + int64_t(fine.ny) * zz);
+            const int64_t vc = (xx >> 1) + int64_t(fine.nx / 2) * ((yy >> 1) + int64_t(fine.ny / 2) * (zz >> 1));
+            y[vf * ldy8 + g] = __ldg(x + vc * ldx8 + g);
+        }
     }
 }
 __global__ void up2_bwd_kernel(Grid3 fine, int C, const float* __restrict__ dy, int lddy, float* __restrict__ dx, int lddx)
@@ -304,6 +360,8 @@ __global__ void flip_weights_kernel(int cout, int cin, const float* __restrict__
 
 int grid1d(int64_t n) { return int(std::min<int64_t>((n + 255) / 256, 152 * 16)); }
 
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 Grid3 make_grid(int nx, int ny, int nz) { return Grid3{nx, ny, nz, int64_t(nx) * ny * nz}; }
 
 // Network input on the device: channel 0 of the channels-last BF16 input
@@ -322,14 +380,18 @@ __global__ void unet_input_kernel(int64_t V, const float* __restrict__ r, const 
 __global__ void unet_output_kernel(int32_t nx, int32_t ny, int32_t nz, const float* __restrict__ out, int32_t ld,
                                    const double* __restrict__ rr, float scale, float* __restrict__ e)
 {
+    // rows (y, z) with a block stride, a row's voxels with a thread stride (no 64-bit division)
     const int64_t V = int64_t(nx) * ny * nz;
     const double  ms = *rr / double(V);
     const float   sigma = ms > 0.0 ? float(sqrt(ms)) : 1.f;
     const float   k = scale * sigma;
-    for (int64_t v = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < V; v += int64_t(gridDim.x) * blockDim.x) {
-        const int  x = int(v % nx), y = int((v / nx) % ny), z = int(v / (int64_t(nx) * ny));
-        const bool face = x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1;
-        e[v] = face ? 0.f : out[v * ld] * k;
+    for (int row = blockIdx.x; row < ny * nz; row += gridDim.x) {
+        const int y = row % ny, z = row / ny;
+        for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+            const int64_t v = x + int64_t(nx) * row;
+            const bool    face = x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1;
+            e[v] = face ? 0.f : out[v * ld] * k;
+        }
     }
 }
 
@@ -426,10 +488,19 @@ int ngb_relu_bwd(int64_t V, int32_t C, const float* dy, int32_t lddy, const void
 int ngb_pool2(int32_t nx, int32_t ny, int32_t nz, int32_t C, const void* x, int32_t ldx, void* y, int32_t ldy, void* stream)
 {
     NGB_CHECK_ARG(nx % 2 == 0 && ny % 2 == 0 && nz % 2 == 0 && nx > 0 && C > 0 && x && y, "pool2 needs even dims");
+    NGB_CHECK_ARG(int64_t(ny / 2) * (nz / 2) < (int64_t(1) << 31) && int64_t(nx / 2) * C < (int64_t(1) << 31), "pool2: grid too large");
+    const int rows = std::min((ny / 2) * (nz / 2), 152 * 16);
     const Grid3 g = make_grid(nx, ny, nz);
-    pool2_kernel<<<grid1d(g.V / 8 * C), 256, 0, as_stream(stream)>>>(g, C, static_cast<const __nv_bfloat16*>(x), ldx,
-                                                                      static_cast<__nv_bfloat16*>(y), ldy);
-    NGB_LAUNCH_CHECK("pool2_kernel");
+    if (C % 8 == 0 && ldx % 8 == 0 && ldy % 8 == 0 && aligned16(x) && aligned16(y)) {
+        const int G = C / 8;
+        pool2_vec_kernel<<<rows, 256, 0, as_stream(stream)>>>(
+            g, G, static_cast<const uint4*>(x), ldx / 8, static_cast<uint4*>(y), ldy / 8);
+        NGB_LAUNCH_CHECK("pool2_vec_kernel");
+    } else {
+        pool2_kernel<<<rows, 256, 0, as_stream(stream)>>>(
+            g, C, static_cast<const __nv_bfloat16*>(x), ldx, static_cast<__nv_bfloat16*>(y), ldy);
+        NGB_LAUNCH_CHECK("pool2_kernel");
+    }
     return NGB_OK;
 }
 
@@ -446,10 +517,19 @@ int ngb_pool2_bwd(int32_t nx, int32_t ny, int32_t nz, int32_t C, const float* dy
 int ngb_up2(int32_t nx, int32_t ny, int32_t nz, int32_t C, const void* x, int32_t ldx, void* y, int32_t ldy, void* stream)
 {
     NGB_CHECK_ARG(nx % 2 == 0 && ny % 2 == 0 && nz % 2 == 0 && nx > 0 && C > 0 && x && y, "up2 needs even fine dims");
+    NGB_CHECK_ARG(int64_t(ny) * nz < (int64_t(1) << 31) && int64_t(nx) * C < (int64_t(1) << 31), "up2: grid too large");
+    const int rows = int(std::min<int64_t>(int64_t(ny) * nz, 152 * 16));
     const Grid3 g = make_grid(nx, ny, nz);
-    up2_kernel<<<grid1d(g.V * C), 256, 0, as_stream(stream)>>>(g, C, static_cast<const __nv_bfloat16*>(x), ldx,
-                                                               static_cast<__nv_bfloat16*>(y), ldy);
-    NGB_LAUNCH_CHECK("up2_kernel");
+    if (C % 8 == 0 && ldx % 8 == 0 && ldy % 8 == 0 && aligned16(x) && aligned16(y)) {
+        const int G = C / 8;
+        up2_vec_kernel<<<rows, 256, 0, as_stream(stream)>>>(g, G, static_cast<const uint4*>(x), ldx / 8, static_cast<uint4*>(y),
+                                                              ldy / 8);
+        NGB_LAUNCH_CHECK("up2_vec_kernel");
+    } else {
+        up2_kernel<<<rows, 256, 0, as_stream(stream)>>>(g, C, static_cast<const __nv_bfloat16*>(x), ldx,
+                                                          static_cast<__nv_bfloat16*>(y), ldy);
+        NGB_LAUNCH_CHECK("up2_kernel");
+    }
     return NGB_OK;
 }
 
@@ -494,8 +574,9 @@ int ngb_unet_output(int32_t nx, int32_t ny, int32_t nz, const float* out, int32_
 {
     NGB_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1 && ld >= 1, "dims and ld must be positive");
     NGB_CHECK_ARG(out && rr && e, "NULL pointer");
-    const int64_t V = int64_t(nx) * ny * nz;
-    unet_output_kernel<<<stream_grid(V), 256, 0, as_stream(stream)>>>(nx, ny, nz, out, ld, rr, float(scale), e);
+    NGB_CHECK_ARG(int64_t(ny) * nz < (int64_t(1) << 31), "ny * nz must be below 2^31");
+    unet_output_kernel<<<int(std::min<int64_t>(int64_t(ny) * nz, 152 * 16)), 256, 0, as_stream(stream)>>>(nx, ny, nz, out, ld, rr,
+                                                                                                         float(scale), e);
     NGB_LAUNCH_CHECK("unet_output_kernel");
     return NGB_OK;
 }

@@ -82,6 +82,34 @@ def test_pool_and_upsample(ngb, cuda):
     assert np.array_equal(Up.float().cpu().numpy().reshape(x.shape), U.up(P.float().cpu().numpy().reshape(2, 3, 4, 16)))
 
 
+@pytest.mark.parametrize("C,ld,off", [(32, 48, 16), (16, 48, 32), (12, 20, 4), (8, 8, 0)])
+def test_pool_and_upsample_channel_ranges(ngb, cuda, C, ld, off):
+    """Pooling and upsampling on a channel range of wider channels-last
+    buffers: 16-byte vector kernels where the range and strides allow
+    (multiples of 8 channels, 16-byte aligned), the per-channel kernels
+    otherwise; elements outside the range untouched."""
+    import torch
+    rng = np.random.default_rng(C + ld + off)
+    nz, ny, nx = 6, 4, 10
+    x = U.bf16(rng.standard_normal((nz, ny, nx, C)))
+    X = torch.zeros(nx * ny * nz, ld, dtype=torch.bfloat16, device=cuda)
+    X[:, off:off + C] = _bf16_tensor(x.reshape(-1, C), cuda)
+    P = torch.full((nx * ny * nz // 8, ld), 7.0, dtype=torch.bfloat16, device=cuda)
+    L = ngb.lib()
+    pX = ctypes.c_void_p(X.data_ptr() + 2 * off)
+    pP = ctypes.c_void_p(P.data_ptr() + 2 * off)
+    ngb.check(L.ngb_pool2(nx, ny, nz, C, pX, ld, pP, ld, None))
+    got = P[:, off:off + C].float().cpu().numpy().reshape(nz // 2, ny // 2, nx // 2, C)
+    assert np.allclose(got, U.bf16(U.pool(x)), rtol=0, atol=1e-6)
+    assert float(P[:, :off].float().sub(7.0).abs().max() if off else 0.0) == 0.0
+    Up = torch.full_like(X, 5.0)
+    pU = ctypes.c_void_p(Up.data_ptr() + 2 * off)
+    ngb.check(L.ngb_up2(nx, ny, nz, C, pP, ld, pU, ld, None))
+    assert np.array_equal(Up[:, off:off + C].float().cpu().numpy().reshape(x.shape), U.up(got))
+    rest = torch.cat([Up[:, :off], Up[:, off + C:]], 1)
+    assert rest.numel() == 0 or float((rest.float() - 5.0).abs().max()) == 0.0
+
+
 def test_unet_forward_and_gradients_match_oracle(ngb, cuda):
     import torch
     from neon_gb300.learned import UNet
@@ -237,9 +265,10 @@ def test_conv_tensor_cores_many_tiles_match_mma(ngb, cuda, dims, cin, cout):
 
 
 @pytest.mark.parametrize("dims", [(79, 128, 512), (37, 4, 128), (3, 2, 128)])
-@pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (16, 32), (32, 32)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (16, 32), (32, 32), (96, 32)])
 def test_conv_tensor_cores_z_runs_match_mma(ngb, cuda, dims, cin, cout):
-    """Plane-mode layers with Cout 16 / 32 march each work unit over a run of
+    """Plane-mode layers with Cout 16 / 32 (96 -> 32: 162 KB of resident
+    weights at one CTA per SM) march each work unit over a run of
     output planes (16 at the largest size here, 4 on the small grids; the
     last run ragged, a grid shorter than one run): every input plane staged
     once, the three output planes it feeds accumulated in a ring of TMEM
