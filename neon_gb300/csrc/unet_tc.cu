@@ -43,7 +43,7 @@ constexpr int      kTcM = 128;           // voxels per tile (MMA M)
 constexpr int      kTcMaxStages = 8;     // shared-memory pipeline depth (at most)
 constexpr int      kTcThreads = 192;     // 6 warps
 constexpr int      kStripRows = kTcM + 2;  // plane mode: voxels x0 - 1 .. x0 + 128 of an image row
-constexpr int      kZMax = 8;              // z-run mode: output planes per work unit (at most)
+constexpr int      kZMax = 16;             // z-run mode: output planes per work unit (at most)
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 __device__ int g_tc_error;
@@ -190,20 +190,28 @@ __device__ __forceinline__ Unit unit_of(const TcParams& p, int64_t u)
     return t;
 }
 
-// z-run mode: work unit u covers the two rows y0, y0 + 1 of 128 voxels from
-// x0 on the output planes z0 .. z0 + nzo - 1.
+// z-run mode: work unit u covers, on the output planes z0 .. z0 + nzo - 1,
+// the two rows y0, y0 + 1 of 128 voxels from x0 (plane mode), or the 128
+// consecutive voxels of a plane from (x0, y0) (tap mode).
 struct ZUnit {
     int64_t v0;
     int     x0, y0, z0, nzo;
 };
 __device__ __forceinline__ ZUnit zunit_of(const TcParams& p, int64_t u)
 {
-    ZUnit         t;
-    const int64_t xt = p.nx / kTcM, yt = p.ny / 2;
-    t.x0 = int(u % xt) * kTcM;
-    const int64_t r = u / xt;
-    t.y0 = int(r % yt) * 2;
-    t.z0 = int(r / yt) * p.zrun;
+    ZUnit t;
+    if (p.plane) {
+        const int64_t xt = p.nx / kTcM, yt = p.ny / 2;
+        t.x0 = int(u % xt) * kTcM;
+        const int64_t r = u / xt;
+        t.y0 = int(r % yt) * 2;
+        t.z0 = int(r / yt) * p.zrun;
+    } else {
+        const int64_t tpp = int64_t(p.nx) * p.ny / kTcM, vin = (u % tpp) * kTcM;
+        t.x0 = int(vin % p.nx);
+        t.y0 = int(vin / p.nx);
+        t.z0 = int(u / tpp) * p.zrun;
+    }
     t.nzo = min(p.zrun, p.nz - t.z0);
     t.v0 = t.x0 + int64_t(p.nx) * (t.y0 + int64_t(p.ny) * t.z0);
     return t;
@@ -312,10 +320,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
     // tt * zcols + (zrun - 1 - lo) * N; every MMA adds to its columns, which
     // start at zero and are cleared again by the epilogue after each read
     const uint32_t zcols = uint32_t(p.zrun) * N;
+    const int      ztiles = p.plane ? 2 : 1;
     if (p.zrun) {
         if (warp >= 2) {
             const uint32_t q = uint32_t(warp & 3);
-            for (uint32_t c = 0; c < 2 * zcols; c += 16) tmem_zero16(tmem + ((q * 32u) << 16) + c);
+            for (uint32_t c = 0; c < uint32_t(ztiles) * zcols; c += 16) tmem_zero16(tmem + ((q * 32u) << 16) + c);
             tmem_wait_st();
         }
         tc_fence_before();
@@ -350,18 +359,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
         uint32_t k = 0;
         bool     ok = true;
         // z-run mode: every input plane z0 - 1 .. z0 + nzo of the unit once, chunk by chunk
-        // (planes outside the grid read as zeros); the MMA issuer applies each to the three
-        // output planes it belongs to
+        // (tap mode: once per (dy, dx) tap, the box shifted by it; planes outside the
+        // grid read as zeros); the MMA issuer applies each to the three output planes
+        // it belongs to
+        const int taps = p.plane ? 1 : 9;  // stages per input plane and chunk
         for (int64_t u = blockIdx.x; p.zrun && u < p.units && ok; u += gridDim.x) {
             const ZUnit t = zunit_of(p, u);
-            const int   nsu = (t.nzo + 2) * p.kc;
+            const int   nsu = (t.nzo + 2) * taps * p.kc;
             for (int i = 0; i < nsu; i++, k++) {
-                const int      chunk = i % p.kc, pi = i / p.kc;
+                const int      chunk = i % p.kc, tap = (i / p.kc) % taps, pi = i / (p.kc * taps);
                 const uint32_t s = k % ns;
                 if (!(ok = mbar_wait(&empty_bar[s], ((k / ns) & 1u) ^ 1u, &abort_sh))) break;
                 uint8_t* st = stages + size_t(s) * p.stage_bytes;
                 mbar_expect_tx(&full_bar[s], p.a_bytes);
-                tma_load_5d(st, &xmap, 0, t.x0 - 1, t.y0 - 1, t.z0 + pi - 1, 2 * chunk, &full_bar[s]);
+                const int dyi = p.plane ? 0 : tap / 3, dxi = p.plane ? 0 : tap % 3;
+                tma_load_5d(st, &xmap, 0, t.x0 + dxi - 1, t.y0 + dyi - 1, t.z0 + pi - 1, 2 * chunk, &full_bar[s]);
             }
         }
         for (int64_t u = blockIdx.x; !p.zrun && u < p.units && ok; u += gridDim.x) {
@@ -411,23 +423,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
                 }
                 const uint32_t idesc = idesc_bf16_f32(kTcM, (jhi - jlo + 1) * N);
                 const uint32_t dcol = uint32_t(p.zrun - 1 - pi + jlo) * N;
-                for (int chunk = 0; chunk < p.kc; chunk++, k++) {
+                const int      taps = p.plane ? 1 : 9;
+                for (int r = 0; r < taps * p.kc && ok; r++, k++) {
+                    const int      chunk = r % p.kc, tap = r / p.kc;
                     const uint32_t s = k % ns;
                     if (!(ok = mbar_wait(&full_bar[s], (k / ns) & 1u, &abort_sh))) break;
                     tc_fence_after();
                     const uint64_t a0 = smem_desc(smem_u32(stages + size_t(s) * p.stage_bytes), p.a_lbo, 128);
                     const uint64_t b0 = smem_desc(smem_u32(wres) + uint32_t(chunk * 9) * (96u * N), 48 * N, 128) +
                                         uint64_t(jlo * N);  // rows of block jlo (16 bytes each, >> 4)
+                    if (p.plane) {
 #pragma unroll
-                    for (int tt = 0; tt < 2; tt++)
+                        for (int tt = 0; tt < 2; tt++)
 #pragma unroll
-                        for (int tap = 0; tap < 9; tap++) {
-                            const uint64_t ad = a0 + uint64_t((tt + tap / 3) * kStripRows + tap % 3);
-                            const uint64_t bd = b0 + uint64_t(tap * 6 * N);  // 96 N bytes per tap, >> 4
-                            mma_bf16(tmem + uint32_t(tt) * zcols + dcol, ad, bd, idesc, 1u);
-                        }
+                            for (int tp = 0; tp < 9; tp++) {
+                                const uint64_t ad = a0 + uint64_t((tt + tp / 3) * kStripRows + tp % 3);
+                                const uint64_t bd = b0 + uint64_t(tp * 6 * N);  // 96 N bytes per tap, >> 4
+                                mma_bf16(tmem + uint32_t(tt) * zcols + dcol, ad, bd, idesc, 1u);
+                            }
+                    } else {  // tap mode: the stage holds the box of this (dy, dx) tap
+                        mma_bf16(tmem + dcol, a0, b0 + uint64_t(tap * 6 * N), idesc, 1u);
+                    }
                     mma_commit(&empty_bar[s]);
-                    if (chunk == p.kc - 1 && pi >= 2) {
+                    if (r == taps * p.kc - 1 && pi >= 2) {
                         mma_commit(&tfull_bar[pi - 2]);
                         upar ^= 1u << (pi - 2);
                     }
@@ -475,7 +493,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) conv3d_tc_kernel(const __grid_c
             for (int lo = 0; lo < t.nzo; lo++) {
                 if (!(ok = mbar_wait(&tfull_bar[lo], (upar >> lo) & 1u, &abort_sh))) break;
                 tc_fence_after();
-                for (int tt = 0; tt < 2; tt++) {
+                for (int tt = 0; tt < ztiles; tt++) {
                     const uint32_t ta = tmem + ((q * 32u) << 16) + uint32_t(tt) * zcols + uint32_t(p.zrun - 1 - lo) * N;
                     float          acc[N];
 #pragma unroll
@@ -870,29 +888,31 @@ int ngb_conv3d_tc(int nx, int ny, int nz, const void* x, int ldx, int cin, const
     p.w_region = p.resident ? (p.w_bytes + 1023u) & ~1023u : 0u;
     p.b_bytes = p.resident ? 0u : uint32_t(plane ? 9 : 1) * uint32_t(cout) * 32u;
     p.stage_bytes = ((p.a_bytes + 127u) & ~127u) + ((p.b_bytes + 127u) & ~127u);
-    // z-run mode (plane mode, resident weights, Cout 16 / 32): a unit marches over
-    // zr output planes and stages each input plane once instead of three times;
-    // its accumulators (zr planes x two tiles x Cout columns) fill at most 256
-    // TMEM columns, so two CTAs per SM keep fitting
-    const bool zrun = plane && p.resident && (cout == 16 || cout == 32);
+    // z-run mode (resident weights, Cout 16 / 32): a unit marches over zr output
+    // planes and stages each input plane once instead of three times; its
+    // accumulators (zr planes x the unit's tiles x Cout columns) fill at most
+    // 256 TMEM columns, so two CTAs per SM keep fitting
+    const bool zrun = p.resident && (cout == 16 || cout == 32);
+    const int  ztiles = plane ? 2 : 1;
     int        zr = 0;
     if (zrun) {
         int dev = 0, sms = 152;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             sms = 152;
-        const int64_t cols2d = int64_t(nx / kTcM) * (ny / 2);
-        zr = std::min(kZMax, 128 / cout);  // 8 planes at Cout 16, 4 at Cout 32
+        const int64_t cols2d = plane ? int64_t(nx / kTcM) * (ny / 2) : int64_t(nx) * ny / kTcM;
+        zr = std::min(kZMax, 256 / (ztiles * cout));  // plane mode 8 / 4 planes at Cout 16 / 32, tap mode 16 / 8
         // shorter runs while the units would not give every CTA (two per SM) four of them
         while (zr > 2 && cols2d * ((nz + zr - 1) / zr) < int64_t(8) * sms) zr /= 2;
     }
     p.zrun = zr;
     uint32_t cols = 32;
-    while (cols < uint32_t(zr ? 2 * zr * cout : 2 * p.ntile * cout)) cols *= 2;
+    while (cols < uint32_t(zr ? ztiles * zr * cout : 2 * p.ntile * cout)) cols *= 2;
     p.tmem_cols = cols;
     // depth: as many stages as fit in ~108 KB (two CTAs per SM) or ~200 KB (one), 2 to 8
     const uint32_t budget = (cols <= 256 && p.w_region <= 56u * 1024u ? 108u * 1024u : 200u * 1024u) - p.w_region;
     p.nstages = int(std::min<uint32_t>(kTcMaxStages, std::max<uint32_t>(2u, budget / p.stage_bytes)));
-    p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * (zr ? (nz + zr - 1) / zr : nz) : int64_t(nx) * ny * nz / kTcM;
+    p.units = plane ? int64_t(nx / kTcM) * (ny / 2) * (zr ? (nz + zr - 1) / zr : nz)
+                    : (zr ? int64_t(nx) * ny / kTcM * ((nz + zr - 1) / zr) : int64_t(nx) * ny * nz / kTcM);
     p.wpk = static_cast<const __nv_bfloat16*>(wpacked);
     p.bias = bias, p.y = y, p.ldy = ldy, p.relu = relu, p.accumulate = accumulate;
     if (p.units == 0) return NGB_OK;

@@ -264,12 +264,12 @@ def test_conv_tensor_cores_many_tiles_match_mma(ngb, cuda, dims, cin, cout):
     assert err <= 1e-5 * scale, (err / scale, int(torch.isnan(Y).sum()))
 
 
-@pytest.mark.parametrize("dims", [(79, 128, 512), (37, 4, 128), (3, 2, 128)])
+@pytest.mark.parametrize("dims", [(79, 128, 512), (37, 4, 128), (3, 2, 128), (20, 8, 64), (9, 3, 128), (64, 64, 64)])
 @pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (16, 32), (32, 32), (96, 32)])
 def test_conv_tensor_cores_z_runs_match_mma(ngb, cuda, dims, cin, cout):
-    """Plane-mode layers with Cout 16 / 32 (96 -> 32: 162 KB of resident
-    weights at one CTA per SM) march each work unit over a run of
-    output planes (16 at the largest size here, 4 on the small grids; the
+    """Layers with Cout 16 / 32 and resident weights (plane mode, 96 -> 32 with
+    162 KB of weights at one CTA per SM; tap mode for rows of 64 voxels or an
+    odd row count) march each work unit over a run of output planes (16 at the largest size here, 4 on the small grids; the
     last run ragged, a grid shorter than one run): every input plane staged
     once, the three output planes it feeds accumulated in a ring of TMEM
     slots. Against the mma.sync kernel, FP32 output with bias and with
