@@ -41,6 +41,7 @@ struct Dom {
     const int8_t* bd;
     double        invd[7];  // h^2 / n for n valid neighbours (host-computed: no division on the device)
     float         invf[7];  // the same, rounded to float (no FP64 conversion on the device)
+    float         ih2_hi, ih2_lo;  // 1/h^2 as a float pair (hi + lo, about 48 bits)
     int32_t       zc;       // planes per CG work item (make_dom: enough items to fill the GPU)
     int32_t       zc_box;   // the same for the 32 x 32 tiles of the box pass A
 };
@@ -84,6 +85,9 @@ Dom make_dom(const ngb_poisson_desc* d)
     g.invd[0] = 1.0;
     for (int n = 1; n <= 6; n++) g.invd[n] = d->h * d->h / double(n);
     for (int n = 0; n <= 6; n++) g.invf[n] = float(g.invd[n]);
+    const double ih2 = 1.0 / (d->h * d->h);
+    g.ih2_hi = float(ih2);
+    g.ih2_lo = float(ih2 - double(g.ih2_hi));
     // CG work items are 32 x 16 (pass A) column tiles times zc planes: at
     // least four per SM, with chunks as long as that allows (each costs two
     // extra planes of loads at its start)
@@ -367,7 +371,7 @@ __global__ void __launch_bounds__(kBX) fcg_update_kernel(int64_t n, double* __re
 template <typename T>
 __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const T* __restrict__ bvec, const double* __restrict__ xh,
                                                       T* __restrict__ r, T* __restrict__ p, T* __restrict__ xlo,
-                                                      double* partials)
+                                                      double* partials, float* __restrict__ rt_hi, float* __restrict__ rt_lo)
 {
     const double invh2 = 1.0 / (d.h * d.h);
     double       v[3] = {0.0, 0.0, 0.0};
@@ -391,6 +395,11 @@ __global__ void __launch_bounds__(kBX) cg_init_kernel(Dom d, CgState* st, const 
         r[c.i] = rc;
         p[c.i] = T(0);
         xlo[c.i] = T(0);
+        if (rt_hi) {  // FP32 fields: the true residual kept as a float pair for the refreshes
+            const float hi = float(rt);
+            rt_hi[c.i] = hi;
+            rt_lo[c.i] = float(rt - double(hi));
+        }
         rzacc.add(rc, T(invdiag_of<T>(d, c.x, c.y, c.z, c.i, st->jacobi) * rc));
         v[2] += rt * rt;
     }
@@ -836,6 +845,93 @@ __global__ void __launch_bounds__(kBX) cg_refresh2_kernel(Dom d, CgState* st, co
     }
 }
 
+// Float-pair arithmetic (about 48 significant bits on the FP32 pipe): Knuth's
+// TwoSum, Dekker's TwoProduct by fma, and the pair sum normalised.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b)
+{
+    const float s = a + b, bb = s - a;
+    return FF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF ff_norm(float hi, float lo)
+{
+    const float s = hi + lo;
+    return FF{s, lo - (s - hi)};
+}
+__device__ __forceinline__ FF ff_add(FF a, float b)
+{
+    const FF t = two_sum(a.hi, b);
+    return ff_norm(t.hi, t.lo + a.lo);
+}
+
+// Refresh for FP32 fields, incremental: the true residual b - A x_hi is kept
+// as a float pair (rt_hi, rt_lo) since the start of the solve; folding x_lo
+// into x_hi changes it by -A x_lo, computed here in float-pair arithmetic
+// (A x_lo is small against b - A x_hi only near convergence, where the pair's
+// 48 bits keep it exact to far below the tolerance). So the refresh needs
+// two FP64 operations per cell (x_hi += x_lo) instead of an FP64 stencil of
+// x_hi, which GB300's FP64 rate made the largest cost of a refresh. Then
+// r = rt_hi, rz = <r, z>, rel = |rt| / |b|; x_lo is cleared by the next
+// kernel (cells here read their neighbours' x_lo).
+__global__ void __launch_bounds__(kBX) cg_refresh_ff_kernel(Dom d, CgState* st, double* __restrict__ xh, const float* __restrict__ xlo,
+                                                            float* __restrict__ r, float* __restrict__ rt_hi,
+                                                            float* __restrict__ rt_lo, double* partials)
+{
+    if (st->converged || !st->refresh) return;
+    const int     jac = st->jacobi;
+    double        v[2] = {0.0, 0.0};
+    DotAcc<float> rzacc, rracc;
+    for (int64_t seg = blockIdx.x; seg < d.segs; seg += gridDim.x) {
+        const Cell c = seg_cell(d, seg);
+        if (c.x < 0) continue;
+        const float xc = xlo[c.i];
+        xh[c.i] = xh[c.i] + double(xc);
+        float rh = 0.f;
+        if (!is_fixed(d, c.x, c.y, c.z, c.i)) {  // Fixed cells keep r = 0
+            // A x_lo = (n x_c - sum of the valid neighbours) / h^2, as a float pair
+            int n = 0;
+            for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int, int, int, int64_t) { n++; });
+            const float p = float(n) * xc;
+            FF          a{p, __fmaf_rn(float(n), xc, -p)};
+            for_each_ngh(d, c.x, c.y, c.z, c.i, [&](int, int, int, int64_t j) { a = ff_add(a, -xlo[j]); });
+            const float ph = a.hi * d.ih2_hi;
+            const float pl = __fmaf_rn(a.hi, d.ih2_hi, -ph) + (a.hi * d.ih2_lo + a.lo * d.ih2_hi);
+            // rt -= A x_lo
+            const FF t = two_sum(rt_hi[c.i], -ph);
+            const FF rt = ff_norm(t.hi, t.lo + (rt_lo[c.i] - pl));
+            rt_hi[c.i] = rt.hi;
+            rt_lo[c.i] = rt.lo;
+            rh = rt.hi;
+        }
+        r[c.i] = rh;
+        rzacc.add(rh, float(invdiag_of<float>(d, c.x, c.y, c.z, c.i, jac) * rh));
+        rracc.add(rh, rh);
+    }
+    v[0] = rzacc.value();
+    v[1] = rracc.value();
+    double out[2];
+    if (grid_sum<2>(v, partials, &st->ticket, out) && threadIdx.x == 0) {
+        st->rz = out[0];
+        st->rel = sqrt(out[1]) / st->bnorm;
+        st->refreshes += 1;
+        st->refresh = 0;
+        if (st->rel <= st->tol)
+            st->converged = 1;
+        else if (st->last)
+            st->converged = 2;
+    }
+}
+
+// x_lo = 0 after an incremental refresh (a separate launch: the refresh reads
+// neighbours' x_lo). Runs whenever the refresh ran: its condition is the IF
+// node's, not st->refresh, which the refresh has cleared.
+__global__ void __launch_bounds__(kBX) cg_clear_xlo_kernel(int64_t n, float* __restrict__ xlo)
+{
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) xlo[i] = 0.f;
+}
+
 __global__ void rhs_kernel(Dom d, int field, const double* __restrict__ centres, const double* __restrict__ amps, double sigma,
                            void* f)
 {
@@ -874,6 +970,7 @@ struct Workspace {
     CgState* st;
     double*  partials;
     void *   r, *p0, *p1, *s, *xlo;
+    float *  rt_hi, *rt_lo;  // FP32 fields: the true residual as a float pair (null for FP64 fields)
     size_t   bytes;
 };
 
@@ -893,6 +990,12 @@ Workspace layout(const ngb_poisson_desc* d, void* base)
     for (auto f : fields) {
         *f = p + off;
         off += align256(V * esz);
+    }
+    if (d->field != NGB_STORE_F64) {
+        w.rt_hi = reinterpret_cast<float*>(p + off);
+        off += align256(V * 4);
+        w.rt_lo = reinterpret_cast<float*>(p + off);
+        off += align256(V * 4);
     }
     w.bytes = off;
     return w;
@@ -932,7 +1035,7 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
     T *r = static_cast<T*>(w.r), *p0 = static_cast<T*>(w.p0), *p1 = static_cast<T*>(w.p1), *sv = static_cast<T*>(w.s),
       *xlo = static_cast<T*>(w.xlo);
     const auto t0 = std::chrono::steady_clock::now();
-    cg_init_kernel<T><<<grid, kBX, 0, s>>>(d, w.st, b, x, r, p0, xlo, w.partials);
+    cg_init_kernel<T><<<grid, kBX, 0, s>>>(d, w.st, b, x, r, p0, xlo, w.partials, w.rt_hi, w.rt_lo);
     NGB_LAUNCH_CHECK("cg_init_kernel");
     NGB_CUDA_TRY(cudaMemsetAsync(p1, 0, size_t(desc->nx) * desc->ny * desc->nz * sizeof(T), s));
 
@@ -981,8 +1084,15 @@ int solve_t(const ngb_poisson_desc* desc, const T* b, double* x, const Workspace
                 e = cudaStreamBeginCaptureToGraph(cs_body, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                   cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                cg_refresh1_kernel<T><<<grid, kBX, 0, cs_body>>>(d, w.st, x, xlo);
-                cg_refresh2_kernel<T><<<grid, kBX, 0, cs_body>>>(d, w.st, b, x, r, w.partials);
+                if constexpr (std::is_same<T, float>::value) {  // incremental float-pair refresh
+                    cg_refresh_ff_kernel<<<grid, kBX, 0, cs_body>>>(d, w.st, x, xlo, r, w.rt_hi, w.rt_lo, w.partials);
+                    const int64_t V = int64_t(desc->nx) * desc->ny * desc->nz;
+                    cg_clear_xlo_kernel<<<int(std::min<int64_t>((V + kBX - 1) / kBX, int64_t(sm_count()) * 8)), kBX, 0, cs_body>>>(V,
+                                                                                                                           xlo);
+                } else {
+                    cg_refresh1_kernel<T><<<grid, kBX, 0, cs_body>>>(d, w.st, x, xlo);
+                    cg_refresh2_kernel<T><<<grid, kBX, 0, cs_body>>>(d, w.st, b, x, r, w.partials);
+                }
                 cudaGraph_t body = nullptr;
                 e = cudaStreamEndCapture(cs_body, &body);
             }
@@ -1064,7 +1174,7 @@ int time_passes_t(const ngb_poisson_desc* desc, const T* b, double* x, const Wor
     NGB_CUDA_TRY(cudaMemcpyAsync(w.st, &init, sizeof(CgState), cudaMemcpyHostToDevice, s));
     T *r = static_cast<T*>(w.r), *p0 = static_cast<T*>(w.p0), *p1 = static_cast<T*>(w.p1), *sv = static_cast<T*>(w.s),
       *xlo = static_cast<T*>(w.xlo);
-    cg_init_kernel<T><<<grid, kBX, 0, s>>>(d, w.st, b, x, r, p0, xlo, w.partials);
+    cg_init_kernel<T><<<grid, kBX, 0, s>>>(d, w.st, b, x, r, p0, xlo, w.partials, w.rt_hi, w.rt_lo);
     NGB_LAUNCH_CHECK("cg_init_kernel");
     NGB_CUDA_TRY(cudaMemsetAsync(p1, 0, size_t(desc->nx) * desc->ny * desc->nz * sizeof(T), s));
     const int   grid_a = std::min(grid, pass_a_items(d)), grid_b = std::min(grid, pass_b_items(d));
