@@ -23,6 +23,7 @@
 #include <vector>
 #include <random>
 #include <limits>
+#include <type_traits>
 
 namespace oracle {
 
@@ -123,6 +124,11 @@ inline void gaussian_sources(int nx, int ny, int nz, uint64_t seed, double* cent
 //   refresh when (it+1) % refresh_every == 0 or sqrt(rr)/|b| <= tol:
 //           x_hi += x_lo; x_lo = 0; r = T(b - A x_hi) (double); rz = <r,z>;
 //           converged iff |b - A x_hi| / |b| <= tol.
+//   T = float (the GPU's cg_refresh_ff_kernel): the true residual b - A x_hi
+//   is kept as a float pair (hi, lo) from the start, and a refresh subtracts
+//   A x_lo from it in float-pair arithmetic (TwoSum, TwoProduct by fma, the
+//   neighbours in the order +x, -x, +y, -y, +z, -z, 1/h^2 as a float pair)
+//   before x_lo is folded into x_hi; r = hi, |b - A x_hi| from hi.
 struct PcgResult {
     int    iterations = 0;
     bool   converged = false;
@@ -167,11 +173,63 @@ struct PcgOracle {
         for (size_t i = 0; i < V; i++) res[i] = bd[i] == Fixed ? 0.0 : double(b[i]) - ax[i];
     }
 
+    // Float-pair helpers (the GPU's FF arithmetic, IEEE single, no contraction).
+    struct FF {
+        float hi, lo;
+    };
+    static FF two_sum(float a, float b)
+    {
+        const float s = a + b, bb = s - a;
+        return FF{s, (a - (s - bb)) + (b - bb)};
+    }
+    static FF ff_norm(float hi, float lo)
+    {
+        const float s = hi + lo;
+        return FF{s, lo - (s - hi)};
+    }
+    static FF ff_add(FF a, float b)
+    {
+        const FF t = two_sum(a.hi, b);
+        return ff_norm(t.hi, t.lo + a.lo);
+    }
+
+    // rt -= A x_lo on Free cells (float pair); returns the new high part (0 on Fixed cells).
+    float ff_refresh_cell(int x, int y, int z, const std::vector<float>& xlo, float& rt_hi, float& rt_lo, float ih_hi,
+                          float ih_lo) const
+    {
+        const size_t i = plin(x, y, z, nx, ny);
+        if (bd[i] == Fixed) return 0.f;
+        static const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+        int              n = 0;
+        for (auto& o : off) {
+            const int X = x + o[0], Y = y + o[1], Z = z + o[2];
+            if (X >= 0 && Y >= 0 && Z >= 0 && X < nx && Y < ny && Z < nz) n++;
+        }
+        const float xc = xlo[i];
+        const float pp = float(n) * xc;
+        FF          a{pp, std::fma(float(n), xc, -pp)};
+        for (auto& o : off) {
+            const int X = x + o[0], Y = y + o[1], Z = z + o[2];
+            if (X >= 0 && Y >= 0 && Z >= 0 && X < nx && Y < ny && Z < nz) a = ff_add(a, -xlo[plin(X, Y, Z, nx, ny)]);
+        }
+        const float ph = a.hi * ih_hi;
+        const float pl = std::fma(a.hi, ih_hi, -ph) + (a.hi * ih_lo + a.lo * ih_hi);
+        const FF    t = two_sum(rt_hi, -ph);
+        const FF    rt = ff_norm(t.hi, t.lo + (rt_lo - pl));
+        rt_hi = rt.hi;
+        rt_lo = rt.lo;
+        return rt.hi;
+    }
+
     PcgResult solve(const T* b, double* x_hi, double tol, int max_iter, int refresh_every) const
     {
+        constexpr bool      kFF = std::is_same<T, float>::value;
         const size_t        V = bd.size();
         std::vector<T>      r(V), p(V, T(0)), s(V), xlo(V, T(0));
         std::vector<double> tr(V);
+        std::vector<float>  rt_hi(kFF ? V : 0), rt_lo(kFF ? V : 0);
+        const double        ih2 = 1.0 / (h * h);
+        const float         ih_hi = float(ih2), ih_lo = float(ih2 - double(ih_hi));
         double              bnorm2 = 0;
         for (size_t i = 0; i < V; i++)
             if (bd[i] == Free) bnorm2 += double(b[i]) * double(b[i]);
@@ -183,6 +241,10 @@ struct PcgOracle {
             r[i] = T(tr[i]);
             rz += double(r[i]) * double(T(invdiag[i] * r[i]));
             rr += tr[i] * tr[i];
+            if constexpr (kFF) {
+                rt_hi[i] = float(tr[i]);
+                rt_lo[i] = float(tr[i] - double(rt_hi[i]));
+            }
         }
         res.rel_residual = bnorm > 0 ? std::sqrt(rr) / bnorm : 0.0;
         if (bnorm == 0 || res.rel_residual <= tol) {
@@ -215,17 +277,33 @@ struct PcgOracle {
             const bool want = ((it + 1) % refresh_every == 0) || (std::sqrt(rr) / bnorm <= tol) || last;
             if (want) {
                 res.refreshes++;
-                for (size_t i = 0; i < V; i++) {
-                    x_hi[i] += double(xlo[i]);
-                    xlo[i] = T(0);
-                }
-                true_residual(b, x_hi, tr.data());
                 rz = 0;
                 double trr = 0;
-                for (size_t i = 0; i < V; i++) {
-                    r[i] = T(tr[i]);
-                    rz += double(r[i]) * double(T(invdiag[i] * r[i]));
-                    trr += tr[i] * tr[i];
+                if constexpr (kFF) {
+                    for (int z = 0; z < nz; z++)
+                        for (int y = 0; y < ny; y++)
+                            for (int x = 0; x < nx; x++) {
+                                const size_t i = plin(x, y, z, nx, ny);
+                                const float  rh = ff_refresh_cell(x, y, z, xlo, rt_hi[i], rt_lo[i], ih_hi, ih_lo);
+                                r[i] = rh;
+                                rz += double(rh) * double(float(invdiag[i] * rh));
+                                trr += double(rh) * double(rh);
+                            }
+                    for (size_t i = 0; i < V; i++) {
+                        x_hi[i] += double(xlo[i]);
+                        xlo[i] = T(0);
+                    }
+                } else {
+                    for (size_t i = 0; i < V; i++) {
+                        x_hi[i] += double(xlo[i]);
+                        xlo[i] = T(0);
+                    }
+                    true_residual(b, x_hi, tr.data());
+                    for (size_t i = 0; i < V; i++) {
+                        r[i] = T(tr[i]);
+                        rz += double(r[i]) * double(T(invdiag[i] * r[i]));
+                        trr += tr[i] * tr[i];
+                    }
                 }
                 res.rel_residual = std::sqrt(trr) / bnorm;
                 if (res.rel_residual <= tol) {
