@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--extra", action="store_true", help="also time the other storage/lattice forms")
     ap.add_argument("--no-sections", action="store_true",
-                    help="cavity: leave out the poisson, storage_16bit and sphere sections of the line")
+                    help="cavity: leave out the poisson, storage_16bit, sphere and unet sections of the line")
     ap.add_argument("--profiles", default="", help="cavity: write the centre-line velocity profiles into this directory")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "sphere", "poisson", "learned", "unet", "accuracy"],
                     help="cavity: dense LBM (default, the headline); sphere: bGrid flow over a sphere; "
@@ -438,6 +438,7 @@ def run_ours(args):
             line["storage_16bit"] = storage_16bit_section(ngb, torch, dev, n, args, per_step_ms)
             line["poisson"] = poisson_section(args)
             line["sphere"] = sphere_section(args)
+            line["unet"] = unet_section(args)
         if extra:
             line["variants"] = extra
         print(json.dumps(line), flush=True)
@@ -761,6 +762,16 @@ def sphere_section(args):
     return run_sphere(a2, emit=False)
 
 
+def unet_section(args):
+    """The learned preconditioner's network at 512^3 (config 4's tensor-core
+    path): TFLOP/s of one forward application against the measured BF16 peak."""
+    import copy
+    a2 = copy.copy(args)
+    a2.n, a2.steps, a2.warmup = 512, 10, 3
+    line = run_unet(a2, emit=False)
+    return {k: line[k] for k in ("metric", "value", "unit", "ms_per_step", "config", "roofline", "clocks", "gpu_launches")}
+
+
 def bf16_peak():
     """Dense BF16 tensor peak (TFLOP/s, burst) measured on this machine, else the fallback."""
     try:
@@ -770,7 +781,7 @@ def bf16_peak():
         return 1900.0, "fallback"
 
 
-def run_unet(args):
+def run_unet(args, emit=True):
     """Forward applications of the learned preconditioner's network (3-level
     U-Net, 16/32/64 channels, BF16 operands on the tcgen05 tensor cores, FP32
     accumulate) at --n^3 with seeded weights and a seeded input; a step is one
@@ -819,7 +830,9 @@ def run_unet(args):
             "roofline": {"bound": "tensor", "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(tflops / peak, 4), "peak_kind": kind, "traffic": None},
             "clocks": clocks, "gpu_launches": 17 * args.steps}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_accuracy(args):
